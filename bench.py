@@ -1,0 +1,310 @@
+"""Benchmark: the plain full-quality single frame (1920x1080 output at supersample 2, so a
+3840x2160 bin grid; 1000 points per bin, 8,294,400,000 points per frame; synthetic genome seed 1
+with 8 xforms plus a final xform; adaptive DE radius 9, min 0, curve 0.4; log-density tonemap).
+
+A step is one frame: warmup (20 discarded passes), the chaos game over all walkers until the
+frame's points are drawn, density estimation, tonemap.  `value` is points per second with the
+genome and all buffers resident in HBM; `e2e` is the same frame through the C ABI's rf_render
+from a host genome to a pinned host RGBA8 image (upload and read-back inside the timed region).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
+
+With N > 1 (torchrun) every rank renders an independent replica (its own seed); value is the
+points of all ranks over the slowest rank's time.  --impl reference times the reference's path
+as restated on the CPU (the reference has no CPU path of its own; the oracle port of
+flame.glsl's iteration, all host threads) on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W_OUT, H_OUT, SS = 1920, 1080, 2
+W, H = W_OUT * SS, H_OUT * SS
+POINTS = 1000 * W * H  # 8,294,400,000
+FUSE = 20
+DE = (9, 0, 0.4)
+GENOME = dict(kind=1, seed=1, n_xforms=8, final_xform=True, force_parametric=True)
+CONFIG_NAME = "plain 1080p frame, supersample 2 (3840x2160 bins), 1000 points/bin, DE r9 c0.4"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic():
+    """DRAM bytes per chaos launch from the committed ncu summary of this workload (or None)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "chaos_kernel_1080p.json")) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    except Exception:
+        return None
+
+
+def cpu_baseline(genome_xml, seconds=12.0, threads=None):
+    """The oracle's FP32 transcription of flame.glsl's draw pass on the host cores, on a bounded
+    sample of this workload (same genome, same bin grid): returns (Gpoints/s, threads, sample)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    g = O.Genome(genome_xml)
+    threads = threads or os.cpu_count() or 1
+    walkers = 256 * 64 * threads
+    t0 = time.perf_counter()
+    n, _, _ = g.cpu_baseline(walkers, 2, W, H, threads)
+    rate = n / max(time.perf_counter() - t0, 1e-6)
+    passes = max(2, int(seconds * rate / walkers))
+    t0 = time.perf_counter()
+    n, _, _ = g.cpu_baseline(walkers, passes, W, H, threads)
+    dt = time.perf_counter() - t0
+    sample = "%d walkers x %d passes = %.3g points of the frame's %.3g, %dx%d bins" % (walkers, passes, n, POINTS, W, H)
+    return n / dt / 1e9, threads, sample, dt
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    import refrakt_gb300 as R
+    R.build()
+    comp = R.FlameCompiler()
+    xml = R.Flame.synthesize(comp, GENOME["kind"], GENOME["seed"], W, H, n_xforms=GENOME["n_xforms"],
+                             final_xform=GENOME["final_xform"], force_parametric=GENOME["force_parametric"]).to_xml()
+    vals = []
+    last = None
+    for i in range(args.warmup + args.steps):
+        v, thr, sample, dt = cpu_baseline(xml, seconds=max(3.0, 30.0 / (args.warmup + args.steps)))
+        if i >= args.warmup:
+            vals.append(v)
+        last = (thr, sample)
+    v = statistics.median(vals)
+    line = {"metric": "Gpoints/s histogrammed", "value": v, "unit": "Gpoints/s", "impl": "reference",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": POINTS / (v * 1e9) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic genome (seed 1), no dataset",
+            "config": {"workload": CONFIG_NAME, "points_per_frame": POINTS, "bins": [W, H], "genome": GENOME},
+            "cpu_baseline": {"value": v, "unit": "Gpoints/s", "cores": last[0], "kind": "port", "sample": last[1]},
+            "e2e": {"value": v, "unit": "Gpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_native(args):
+    import numpy as np
+    import torch
+    import refrakt_gb300 as R
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    R.build()
+    comp = R.FlameCompiler()
+    flame = R.Flame.synthesize(comp, GENOME["kind"], GENOME["seed"], W, H, n_xforms=GENOME["n_xforms"],
+                               final_xform=GENOME["final_xform"], force_parametric=GENOME["force_parametric"])
+    xml = flame.to_xml()
+    info = flame.info()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    cta = args.cta
+    walkers = sms * args.ctas_per_sm * cta
+    sim = R.Sim(walkers, cta_slots=cta, steps_per_launch=args.steps_per_launch, seed=1000 + rank, device=local)
+    passes = (POINTS + walkers - 1) // walkers
+    launches = (passes + args.steps_per_launch - 1) // args.steps_per_launch
+    bins = torch.zeros(H, W, 4, device="cuda")
+    hits = torch.zeros(H, W, dtype=torch.int32, device="cuda")
+    de = torch.zeros_like(bins)
+    img = torch.zeros(H_OUT, W_OUT, 4, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    sim.set_stream(stream)
+
+    def frame(ev=None):
+        sim.warmup(flame, FUSE - 1)
+        bins.zero_()
+        hits.zero_()
+        if ev:
+            ev[0].record(stream)
+        sim.draw_to_bins(flame, bins, hits, W, H, passes, sync=False)
+        if ev:
+            ev[1].record(stream)
+        R.density_estimate(bins, W, H, DE[0], DE[1], DE[2], de, stream=stream)
+        R.tonemap(de, W, H, SS, info["gamma"], info["brightness"], info["vibrancy"], 0.0, None, img, stream=stream)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        frame()
+    barrier()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        t0.record(stream)
+        for i in range(args.steps):
+            frame(evs[i])
+        t1.record(stream)
+        barrier()
+    ms = t0.elapsed_time(t1)
+    draw_ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = POINTS * ws / (ms_step * 1e-3) / 1e9
+
+    # end to end through the C ABI: host genome in, pinned host image out
+    out = torch.empty(H_OUT, W_OUT, 4, dtype=torch.uint8, pin_memory=True)
+    out_np = out.numpy()
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        barrier()
+        t_a = time.perf_counter()
+        f2 = R.Flame.from_xml(xml, comp)
+        _, st = sim.render(f2, W_OUT, H_OUT, POINTS, supersample=SS, fuse_passes=FUSE, out=out_np)
+        barrier()
+        if i >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t_a) * 1e3)
+    e2e_step = statistics.median(e2e_ms)
+    if ws > 1:
+        t = torch.tensor([e2e_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_step = float(t.item())
+    e2e_value = POINTS * ws / (e2e_step * 1e-3) / 1e9
+    prog_bytes = info["total_params"] * 4  # order of the uploaded genome
+    h2d = prog_bytes + 256 * 16
+    d2h = W_OUT * H_OUT * 4
+
+    peak, peak_kind = _peaks()
+    per_launch_ms = draw_ms / launches
+    bytes_per_point = 20  # payload of the histogram reductions: float4 RGBA + uint32 count
+    pts_per_launch = walkers * args.steps_per_launch
+    achieved = bytes_per_point * pts_per_launch / (per_launch_ms * 1e-3) / 1e9
+    traffic = _traffic()
+    line = {
+        "metric": "Gpoints/s histogrammed", "value": value, "unit": "Gpoints/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic genome (seed 1); no dataset",
+        "config": {"workload": CONFIG_NAME, "points_per_frame": POINTS, "bins": [W, H], "output": [W_OUT, H_OUT],
+                   "genome": GENOME, "walkers": walkers, "cta_slots": cta, "steps_per_launch": args.steps_per_launch,
+                   "passes_per_frame": passes, "fuse_passes": FUSE, "density_estimation": list(DE),
+                   "l2": "bins (3840x2160x20 B = 166 MB) exceed the 129 MB L2", "parallelism": "replicas" if ws > 1 else "single"},
+        "s_per_frame": ms_step / 1e3,
+        "draw_ms_per_frame": draw_ms,
+        "gpu_launches": (launches + (FUSE + args.steps_per_launch - 1) // args.steps_per_launch + 4) * args.steps,
+        "e2e": {"value": e2e_value, "unit": "Gpoints/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "s_per_frame": e2e_step / 1e3},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "chaos_kernel", "peak_source": peak_kind,
+                     "algorithmic_bytes_per_point": bytes_per_point, "points_per_launch": pts_per_launch,
+                     "launch_ms": per_launch_ms,
+                     "note": "atomic-reduction payload per point; the chaos game is bound by SM issue and L2 "
+                             "reduction throughput, not DRAM"},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        if ws == 1 and not args.no_cpu_baseline:
+            v, thr, sample, _ = cpu_baseline(xml)
+            line["cpu_baseline"] = {"value": v, "unit": "Gpoints/s", "cores": thr, "kind": "port", "sample": sample}
+        print(json.dumps(line))
+    sim.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--cta", type=int, default=1024)
+    ap.add_argument("--ctas-per-sm", type=int, default=16)
+    ap.add_argument("--steps-per-launch", type=int, default=32)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_native(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

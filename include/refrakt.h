@@ -1,0 +1,238 @@
+/*
+ * refrakt_gb300 — C ABI of the GB300 fractal-flame renderer.
+ *
+ * Drop-in for the chaos-game path of untrioctium/refrakt, whose interface is two C++
+ * classes: `flame_compiler` (src/variation_table.hpp:20-59) and `flame`
+ * (src/flame.hpp:41-173).  Each entry point below names the reference member it replaces.
+ *
+ * Conventions
+ *  - Every function returns an `int` status (RF_OK = 0) unless stated otherwise; on failure
+ *    rf_last_error() returns a message for the calling thread.
+ *  - Handles are opaque.  Device pointers are plain CUDA device addresses; `stream` arguments
+ *    are `cudaStream_t` values passed as `void*` (NULL = the legacy default stream).
+ *  - Histogram ("bins") layout, row-major, row 0 = top row (the reference writes row
+ *    (H - y - 1), shaders/flame.glsl:84):
+ *      bins_rgba : float[4 * W * H]  — (sum palette.r, sum palette.g, sum palette.b, sum opacity)
+ *                  per bin, the reference's vec4 bins (flame.glsl:84);
+ *      bins_hits : uint32[W * H]     — exact count of points drawn into the bin.
+ *  - There is no process-wide mutable state: every simulation lives in its own rf_sim.
+ */
+#ifndef REFRAKT_GB300_H
+#define REFRAKT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RF_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define RF_API __attribute__((visibility("default")))
+#else
+#define RF_API
+#endif
+
+enum rf_status {
+    RF_OK = 0,
+    RF_ERR_INVALID_ARG = 1,   /* null handle, bad size, inconsistent arguments */
+    RF_ERR_PARSE = 2,         /* malformed flam3 XML or variation YAML */
+    RF_ERR_UNKNOWN_NAME = 3,  /* unknown attribute in a genome (flame.cpp:196) */
+    RF_ERR_UNSUPPORTED = 4,   /* variation that does not compile in the reference, or unknown to the kernels */
+    RF_ERR_CAPACITY = 5,      /* parameter buffer over 1024 floats, too many xforms, too large a histogram */
+    RF_ERR_CUDA = 6,          /* a CUDA runtime call failed */
+    RF_ERR_NEEDS_WARMUP = 7,  /* rf_draw_to_bins before rf_warmup for this flame (flame.hpp:86) */
+    RF_ERR_IO = 8,            /* file could not be read or written */
+    RF_ERR_NO_DEVICE = 9      /* no CUDA device of the supported architecture */
+};
+
+typedef struct rf_compiler rf_compiler;
+typedef struct rf_flame rf_flame;
+typedef struct rf_sim rf_sim;
+
+/* Message describing the last failure on this thread (never NULL). */
+RF_API const char* rf_last_error(void);
+RF_API int rf_abi_version(void);
+
+/* ------------------------------------------------------------------------------------------
+ * Variation table — replaces flame_compiler (src/variation_table.hpp:20-59).
+ * ---------------------------------------------------------------------------------------- */
+
+/* flame_compiler::flame_compiler() (variation_table.cpp:182-215).  `yaml_path` = NULL uses the
+   built-in table of the reference's variations.yaml; a path loads that file and checks each
+   entry against the kernels' implementations. */
+RF_API int  rf_compiler_create(const char* yaml_path, rf_compiler** out);
+RF_API void rf_compiler_destroy(rf_compiler* c);
+/* is_variation / is_param / is_common (variation_table.hpp:39-41): 1 = yes, 0 = no. */
+RF_API int  rf_compiler_is_variation(const rf_compiler* c, const char* name);
+RF_API int  rf_compiler_is_param(const rf_compiler* c, const char* name);
+RF_API int  rf_compiler_is_common(const rf_compiler* c, const char* name);
+/* 1 when the GPU kernels evaluate this variation (0 for the reference's non-compiling ones). */
+RF_API int  rf_compiler_is_supported(const rf_compiler* c, const char* name);
+/* param_owner (variation_table.hpp:43): writes the owning variation's name. */
+RF_API int  rf_compiler_param_owner(const rf_compiler* c, const char* param, char* buf, size_t cap);
+/* variations() (variation_table.hpp:47): count and i-th name (map order). */
+RF_API int  rf_compiler_num_variations(const rf_compiler* c);
+RF_API int  rf_compiler_variation_name(const rf_compiler* c, int i, char* buf, size_t cap);
+/* get_parameters_for_variation (variation_table.hpp:44): comma-separated list. */
+RF_API int  rf_compiler_variation_params(const rf_compiler* c, const char* name, char* buf, size_t cap);
+
+/* ------------------------------------------------------------------------------------------
+ * Genomes — replaces flame::load_flame and the public genome fields (flame.hpp:41-61, 84).
+ * ---------------------------------------------------------------------------------------- */
+
+/* flame::load_flame(path, compiler) (flame.cpp:160-226); NULL result there = error status here. */
+RF_API int  rf_flame_load(const char* flam3_path, const rf_compiler* c, rf_flame** out);
+RF_API int  rf_flame_load_xml(const char* flam3_xml, const rf_compiler* c, rf_flame** out);
+RF_API void rf_flame_free(rf_flame* f);
+/* Serialise (flam3 XML, reference attribute set).  *needed receives the byte count incl. NUL. */
+RF_API int  rf_flame_to_xml(const rf_flame* f, char* buf, size_t cap, size_t* needed);
+
+/* Seeded synthetic genomes for the benchmark workloads (no reference counterpart). */
+enum rf_synth_kind {
+    RF_SYNTH_SMALL = 0,      /* 3 xforms, linear/sinusoidal/spherical, affine U[-1,1] */
+    RF_SYNTH_RANDOM = 1,     /* n xforms, 3 variations each from the supported set, affine U[-1.2,1.2] */
+    RF_SYNTH_CONTRACT = 2,   /* 6 xforms, linear parts x0.05, translations U[-0.02,0.02] */
+    RF_SYNTH_SPACEFILL = 3   /* 16 xforms, spherical + swirl */
+};
+typedef struct {
+    int32_t  kind;              /* rf_synth_kind */
+    uint32_t n_xforms;          /* RF_SYNTH_RANDOM only; 0 = 8 */
+    uint64_t seed;
+    int32_t  final_xform;       /* RF_SYNTH_RANDOM: 1 adds a final xform */
+    int32_t  force_parametric;  /* RF_SYNTH_RANDOM: xforms 0..2 carry julian, ngon, pdj */
+    uint32_t width, height;     /* bin grid the camera is framed for */
+} rf_synth_desc;
+RF_API int  rf_flame_synthesize(const rf_synth_desc* d, const rf_compiler* c, rf_flame** out);
+
+typedef struct {
+    uint32_t size[2];           /* flame.hpp:47 */
+    float    center[2];
+    float    scale, rotate;
+    int32_t  estimator_radius, estimator_min;
+    float    estimator_curve;
+    float    gamma, vibrancy, brightness;
+    uint32_t num_xforms;
+    int32_t  has_final;
+    uint32_t total_params;      /* flat parameter buffer size (flame.cpp:68) */
+} rf_flame_info;
+RF_API int  rf_flame_get_info(const rf_flame* f, rf_flame_info* out);
+/* The mutable view fields the reference UI edits in place (main.cpp:324-381). */
+RF_API int  rf_flame_set_view(rf_flame* f, const float center[2], float scale, float rotate);
+RF_API int  rf_flame_set_tonemap(rf_flame* f, float gamma, float brightness, float vibrancy);
+RF_API int  rf_flame_set_estimator(rf_flame* f, int radius, int min_radius, float curve);
+/* Edit one xform attribute by its flam3 name (weight, color, coefs index via "coefs0".."coefs5",
+   a variation or parameter name).  xform = -1 addresses the final xform. */
+RF_API int  rf_flame_set_xform_value(rf_flame* f, int xform, const char* name, float value);
+/* copy_flame_data_to_buffer (flame.cpp:74-103): writes the flat FP32 parameter buffer. */
+RF_API int  rf_flame_param_buffer(const rf_flame* f, float* out, size_t cap, size_t* count);
+/* buffer_map_ as JSON (flame.cpp:33-71, printed by print_debug_info, flame.hpp:130). */
+RF_API int  rf_flame_param_layout(const rf_flame* f, char* buf, size_t cap, size_t* needed);
+/* The 2x3 screen affine draw_to_bins builds (flame.cpp:289-296) for a W x H bin grid. */
+RF_API int  rf_flame_screen_affine(const rf_flame* f, uint32_t width, uint32_t height, float out6[6]);
+/* RNG draws one evaluation of xform i consumes (i = -1: final xform), first_run colour excluded. */
+RF_API int  rf_flame_xform_draws(const rf_flame* f, int xform);
+
+/* ------------------------------------------------------------------------------------------
+ * Simulation — replaces flame::set_sim_parameters / warmup / draw_to_bins (flame.cpp:105-330).
+ * ---------------------------------------------------------------------------------------- */
+
+typedef struct {
+    uint64_t walkers;           /* total walker slots N (multiple of the shuffle domain * temporal_samples) */
+    uint32_t temporal_samples;  /* T (flame.cpp:109) */
+    uint32_t shuffle_count;     /* permutations in the walker-shuffle table (flame.cpp:110) */
+    uint64_t seed;              /* slot i's JSF32 state = warmup_ctx(i + seed * N) */
+    uint32_t cta_slots;         /* walkers per CTA: 256, 512 or 1024 (0 = 1024) */
+    uint32_t cluster_ctas;      /* CTAs per thread-block cluster sharing one walker shuffle
+                                   through distributed shared memory: 1, 2, 4 (or 8 with 512-slot
+                                   CTAs); 0 = 1.  The shuffle domain is cta_slots * cluster_ctas. */
+    uint32_t steps_per_launch;  /* passes per persistent launch L (0 = 32; 1 = the reference's
+                                   per-pass global gather) */
+    int32_t  device;            /* CUDA device ordinal */
+} rf_sim_desc;
+
+/* flame::set_sim_parameters(total_particles, temporal_samples, shuffle_count). */
+RF_API int  rf_sim_create(const rf_sim_desc* d, rf_sim** out);
+RF_API int  rf_sim_destroy(rf_sim* s);
+RF_API int  rf_sim_set_stream(rf_sim* s, void* stream);
+/* Records the xform index every 256-walker group used per pass (debug / parity). */
+RF_API int  rf_sim_enable_xid_trace(rf_sim* s, uint32_t max_passes);
+RF_API int  rf_sim_read_xid_trace(rf_sim* s, uint8_t* out, size_t cap, uint32_t* passes);
+/* flame::needs_warmup() (flame.hpp:86): 1 when f is not the warmed flame or was edited since. */
+RF_API int  rf_needs_warmup(const rf_sim* s, const rf_flame* f);
+/* flame::warmup(num_passes, tss_width) (flame.cpp:228-281): one first-run pass (start points,
+   jitter, random colours) followed by num_passes passes, nothing drawn. */
+RF_API int  rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_width);
+
+/* Splat strategy for rf_draw_to_bins. */
+enum rf_splat { RF_SPLAT_AUTO = 0, RF_SPLAT_GLOBAL = 1, RF_SPLAT_WARP = 2 };
+/* flame::draw_to_bins(bins, bins_width, num_iter) (flame.cpp:283-330): num_iter passes over
+   every walker, drawing into caller-owned device bins.  bins_hits may be NULL.  When `drawn`
+   is non-NULL the call synchronises and stores the number of points binned (the reference's
+   return value); when NULL it returns without synchronising. */
+RF_API int  rf_draw_to_bins(rf_sim* s, rf_flame* f, float* bins_rgba, uint32_t* bins_hits,
+                     uint32_t width, uint32_t height, uint32_t num_iter, uint64_t* drawn);
+RF_API int  rf_set_splat(rf_sim* s, int splat);
+/* [0] points binned and [1] points emitted (opacity > 0) by the last rf_draw_to_bins call,
+   [2] walker-steps since rf_warmup. */
+RF_API int  rf_sim_counters(rf_sim* s, uint64_t out[3]);
+
+/* ------------------------------------------------------------------------------------------
+ * Image passes — replace the GL density-estimation raster pass (main.cpp:490-515,
+ * shaders/density_{vert,frag}.glsl) and the tonemap compute pass (main.cpp:522-535,
+ * shaders/tonemap.glsl).  All pointers are device pointers.
+ * ---------------------------------------------------------------------------------------- */
+
+/* Adaptive density estimation: out (float4 per bin) = every bin with a > 0 spread over a disc
+   of radius max(min, min(R, int(R / a^curve))), kernel (1 - d^2) * (2/pi) / r^2 with
+   d = |offset| / (r + 0.5); r = 0 copies the bin.  R <= 100 (main.cpp:502). */
+RF_API int rf_density_estimate(const float* bins_rgba, uint32_t width, uint32_t height, int radius,
+                        int min_radius, float curve, float* out_rgba, void* stream);
+/* FP64 statistics of the density channel: out[0] = sum of a, out[1] = max a, out[2] = bins with a > 0. */
+RF_API int rf_hist_stats(const float* rgba, uint32_t width, uint32_t height, double* out3, void* stream);
+/* Log-density tonemap (tonemap.glsl:18-38) with a box supersample filter of ss x ss bins:
+   per bin c *= 0.5*brightness*log10(1 + a*k2)/a, mean over each ss x ss block, then
+   gamma/vibrancy/clamp.  k2 <= 0 selects k2 = bins / sum(a) from rf_hist_stats.  Output is
+   (width/ss) x (height/ss); out_f32 (float4) and/or out_rgba8 may be NULL. */
+RF_API int rf_tonemap(const float* rgba, uint32_t width, uint32_t height, uint32_t ss, float gamma,
+               float brightness, float vibrancy, float k2, float* out_f32, uint8_t* out_rgba8,
+               void* stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Walker shuffle — replaces create_shuffle_buffer / make_shuffle_buffers (shuffle_buffers.cpp).
+ * ---------------------------------------------------------------------------------------- */
+/* `count` keyed permutations of [0, n) (n <= 65536) into device memory out[count * n]. */
+RF_API int rf_shuffle_generate(uint32_t n, uint32_t count, uint64_t seed, uint16_t* out, void* stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Single-step probe (parity tests): one dispatch() of xform i (-1 = final) per point.
+ * in_xyc: device float[3n]; rng: device uint32[4n] (advanced in place); out: device float[4n].
+ * ---------------------------------------------------------------------------------------- */
+RF_API int rf_probe_xform(rf_flame* f, int xform, uint32_t n, const float* in_xyc, uint32_t* rng,
+                   int first_run, float* out_xycw, void* stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Host convenience: one whole frame from host memory to host memory (end-to-end path).
+ * ---------------------------------------------------------------------------------------- */
+typedef struct {
+    uint32_t width, height;     /* output image size */
+    uint32_t supersample;       /* bins = (width*ss) x (height*ss) */
+    uint32_t fuse_passes;       /* rf_warmup passes */
+    uint64_t points;            /* target points (rounded up to whole passes) */
+    float    tss_width;
+    float    k2;                /* tonemap k2 (<= 0: automatic) */
+    int32_t  density_estimation;/* 1: run the adaptive DE with the genome's estimator fields */
+} rf_render_desc;
+/* Renders `f` into out_rgba8 (host memory, width*height*4 bytes).  stats (may be NULL):
+   [0] points computed, [1] points binned, [2] milliseconds on the device. */
+RF_API int rf_render(rf_sim* s, rf_flame* f, const rf_render_desc* d, uint8_t* out_rgba8, double* stats);
+
+/* Writes an RGBA8 image as an uncompressed PNG. */
+RF_API int rf_write_png(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

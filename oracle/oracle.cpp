@@ -1191,26 +1191,37 @@ int orc_density_estimate(const double* in, uint32_t w, uint32_t h, int R, int mi
     return 0;
 }
 
-// tonemap.glsl:18-38; a = 0 (where the shader divides 0/0) maps to opaque black.
-int orc_tonemap(const double* in, uint32_t w, uint32_t h, double gamma, double brightness, double vibrancy,
-                double k2, double* out) {
-    for (size_t i = 0; i < (size_t)w * h; i++) {
-        const double* c = in + 4 * i;
-        double* o = out + 4 * i;
-        double a = c[3];
-        if (!(a > 0.0)) { o[0] = o[1] = o[2] = 0.0; o[3] = 1.0; continue; }
-        double ls = 0.5 * brightness * std::log(1.0 + a * k2) * 0.434294481903251827651128918916 / a;
-        double r = c[0] * ls, g_ = c[1] * ls, b = c[2] * ls, al = a * ls;
-        double ig = 1.0 / gamma;
-        double z = std::pow(al, ig);
-        double gf = z / al;
-        double rgb[3] = {r, g_, b};
-        for (int k = 0; k < 3; k++) {
-            double v = std::pow(rgb[k], ig) * (1.0 - vibrancy) + gf * rgb[k] * vibrancy;
-            o[k] = std::min(std::max(v, 0.0), 1.0);
+// tonemap.glsl:18-38 with an ss x ss box filter: per bin c *= 0.5*brightness*log10(1+a*k2)/a,
+// mean over each block, then gamma / vibrancy / clamp.  ss = 1 is the shader itself.  A block
+// without density (where the shader divides 0 by 0) maps to opaque black.
+int orc_tonemap(const double* in, uint32_t w, uint32_t h, uint32_t ss, double gamma, double brightness,
+                double vibrancy, double k2, double* out) {
+    if (ss == 0 || w % ss || h % ss) return -1;
+    const uint32_t ow = w / ss, oh = h / ss;
+    for (uint32_t oy = 0; oy < oh; oy++)
+        for (uint32_t ox = 0; ox < ow; ox++) {
+            double acc[4] = {0, 0, 0, 0};
+            for (uint32_t j = 0; j < ss; j++)
+                for (uint32_t i = 0; i < ss; i++) {
+                    const double* c = in + (((size_t)(oy * ss + j)) * w + ox * ss + i) * 4;
+                    double a = c[3];
+                    if (!(a > 0.0)) continue;
+                    double ls = 0.5 * brightness * std::log(1.0 + a * k2) * 0.434294481903251827651128918916 / a;
+                    for (int k = 0; k < 4; k++) acc[k] += c[k] * ls;
+                }
+            double* o = out + ((size_t)oy * ow + ox) * 4;
+            const double n = (double)ss * ss;
+            double al = acc[3] / n;
+            if (!(al > 0.0)) { o[0] = o[1] = o[2] = 0.0; o[3] = 1.0; continue; }
+            double ig = 1.0 / gamma;
+            double gf = std::pow(al, ig) / al;
+            for (int k = 0; k < 3; k++) {
+                double v = acc[k] / n;
+                double t = std::pow(v, ig) * (1.0 - vibrancy) + gf * v * vibrancy;
+                o[k] = std::min(std::max(t, 0.0), 1.0);
+            }
+            o[3] = 1.0;
         }
-        o[3] = 1.0;
-    }
     return 0;
 }
 

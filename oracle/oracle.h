@@ -96,8 +96,9 @@ uint64_t orc_cpu_baseline(const orc_genome* g, uint64_t walkers, uint32_t passes
    symmetric restatement: d = |delta|^2/(r+0.5)^2. in/out W*H*4 doubles. */
 int orc_density_estimate(const double* in, uint32_t w, uint32_t h, int radius, int min_radius,
                          double curve, double* out);
-/* Log-density tonemap (shaders/tonemap.glsl:18-38).  out W*H*4 doubles. */
-int orc_tonemap(const double* in, uint32_t w, uint32_t h, double gamma, double brightness,
+/* Log-density tonemap (shaders/tonemap.glsl:18-38) with an ss x ss box filter applied after the
+   per-bin log scaling.  out (W/ss)*(H/ss)*4 doubles. */
+int orc_tonemap(const double* in, uint32_t w, uint32_t h, uint32_t ss, double gamma, double brightness,
                 double vibrancy, double k2, double* out);
 /* Box supersample filter: out[(W/ss)*(H/ss)*4] = mean of ss*ss blocks. */
 int orc_downsample(const double* in, uint32_t w, uint32_t h, uint32_t ss, double* out);

@@ -85,8 +85,9 @@ def lib():
         L.orc_cpu_baseline.restype = ctypes.c_uint64
         L.orc_density_estimate.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
-        L.orc_tonemap.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double,
-                                  ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
+        L.orc_tonemap.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                  ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_void_p]
         L.orc_downsample.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                      ctypes.c_void_p]
         _lib = L
@@ -242,11 +243,12 @@ def density_estimate(rgba, radius, min_radius, curve):
     return out
 
 
-def tonemap(rgba, gamma, brightness, vibrancy, k2):
+def tonemap(rgba, gamma, brightness, vibrancy, k2, ss=1):
     rgba = np.ascontiguousarray(rgba, np.float64)
     h, w = rgba.shape[:2]
-    out = np.zeros_like(rgba)
-    lib().orc_tonemap(_ptr(rgba), w, h, gamma, brightness, vibrancy, k2, _ptr(out))
+    out = np.zeros((h // ss, w // ss, 4), np.float64)
+    if lib().orc_tonemap(_ptr(rgba), w, h, ss, gamma, brightness, vibrancy, k2, _ptr(out)) != 0:
+        raise ValueError("tonemap failed")
     return out
 
 

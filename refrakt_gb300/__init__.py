@@ -1,0 +1,401 @@
+"""refrakt_gb300 — GB300-native fractal-flame chaos game behind the reference's interface.
+
+Python mirror of the C ABI (include/refrakt.h).  The names follow the reference's C++ classes:
+``FlameCompiler`` is ``flame_compiler`` (src/variation_table.hpp:20-59); ``Flame`` holds a genome
+(``flame::load_flame``, src/flame.cpp:160-226); ``Sim`` owns walkers, RNG states and the
+shuffle table (``flame::set_sim_parameters``, flame.cpp:105-158) and runs ``warmup`` and
+``draw_to_bins`` (flame.cpp:228-330).  Every call goes to the CUDA library; nothing here computes
+on the CPU, and a missing library raises instead of falling back.
+
+Device buffers are passed as torch CUDA tensors (or raw device addresses).
+"""
+import ctypes
+import json
+import os
+
+__all__ = ["RefraktError", "FlameCompiler", "Flame", "Sim", "library", "build", "density_estimate",
+           "tonemap", "hist_stats", "shuffle_generate", "probe_xform", "write_png", "render",
+           "SYNTH_SMALL", "SYNTH_RANDOM", "SYNTH_CONTRACT", "SYNTH_SPACEFILL",
+           "SPLAT_AUTO", "SPLAT_GLOBAL", "SPLAT_WARP"]
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "librefrakt_gb300.so")
+
+SYNTH_SMALL, SYNTH_RANDOM, SYNTH_CONTRACT, SYNTH_SPACEFILL = 0, 1, 2, 3
+SPLAT_AUTO, SPLAT_GLOBAL, SPLAT_WARP = 0, 1, 2
+
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "PARSE", 3: "UNKNOWN_NAME", 4: "UNSUPPORTED", 5: "CAPACITY",
+          6: "CUDA", 7: "NEEDS_WARMUP", 8: "IO", 9: "NO_DEVICE"}
+
+
+class RefraktError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (STATUS.get(status, status), message))
+        self.status = status
+        self.message = message
+
+
+class SynthDesc(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("n_xforms", ctypes.c_uint32), ("seed", ctypes.c_uint64),
+                ("final_xform", ctypes.c_int32), ("force_parametric", ctypes.c_int32),
+                ("width", ctypes.c_uint32), ("height", ctypes.c_uint32)]
+
+
+class FlameInfo(ctypes.Structure):
+    _fields_ = [("size", ctypes.c_uint32 * 2), ("center", ctypes.c_float * 2), ("scale", ctypes.c_float),
+                ("rotate", ctypes.c_float), ("estimator_radius", ctypes.c_int32),
+                ("estimator_min", ctypes.c_int32), ("estimator_curve", ctypes.c_float),
+                ("gamma", ctypes.c_float), ("vibrancy", ctypes.c_float), ("brightness", ctypes.c_float),
+                ("num_xforms", ctypes.c_uint32), ("has_final", ctypes.c_int32),
+                ("total_params", ctypes.c_uint32)]
+
+
+class SimDesc(ctypes.Structure):
+    _fields_ = [("walkers", ctypes.c_uint64), ("temporal_samples", ctypes.c_uint32),
+                ("shuffle_count", ctypes.c_uint32), ("seed", ctypes.c_uint64), ("cta_slots", ctypes.c_uint32),
+                ("cluster_ctas", ctypes.c_uint32), ("steps_per_launch", ctypes.c_uint32), ("device", ctypes.c_int32)]
+
+
+class RenderDesc(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("supersample", ctypes.c_uint32),
+                ("fuse_passes", ctypes.c_uint32), ("points", ctypes.c_uint64), ("tss_width", ctypes.c_float),
+                ("k2", ctypes.c_float), ("density_estimation", ctypes.c_int32)]
+
+
+_lib = None
+
+_SIGS = {
+    "rf_last_error": ([], ctypes.c_char_p),
+    "rf_abi_version": ([], ctypes.c_int),
+    "rf_compiler_create": ([ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rf_compiler_destroy": ([ctypes.c_void_p], None),
+    "rf_compiler_is_variation": ([ctypes.c_void_p, ctypes.c_char_p], ctypes.c_int),
+    "rf_compiler_is_param": ([ctypes.c_void_p, ctypes.c_char_p], ctypes.c_int),
+    "rf_compiler_is_common": ([ctypes.c_void_p, ctypes.c_char_p], ctypes.c_int),
+    "rf_compiler_is_supported": ([ctypes.c_void_p, ctypes.c_char_p], ctypes.c_int),
+    "rf_compiler_param_owner": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+    "rf_compiler_num_variations": ([ctypes.c_void_p], ctypes.c_int),
+    "rf_compiler_variation_name": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+    "rf_compiler_variation_params": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+    "rf_flame_load": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rf_flame_load_xml": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rf_flame_free": ([ctypes.c_void_p], None),
+    "rf_flame_to_xml": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    "rf_flame_synthesize": ([ctypes.POINTER(SynthDesc), ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rf_flame_get_info": ([ctypes.c_void_p, ctypes.POINTER(FlameInfo)], ctypes.c_int),
+    "rf_flame_set_view": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_float, ctypes.c_float], ctypes.c_int),
+    "rf_flame_set_tonemap": ([ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_float], ctypes.c_int),
+    "rf_flame_set_estimator": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float], ctypes.c_int),
+    "rf_flame_set_xform_value": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_float], ctypes.c_int),
+    "rf_flame_param_buffer": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    "rf_flame_param_layout": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    "rf_flame_screen_affine": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+    "rf_flame_xform_draws": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rf_sim_create": ([ctypes.POINTER(SimDesc), ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rf_sim_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "rf_sim_set_stream": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rf_sim_enable_xid_trace": ([ctypes.c_void_p, ctypes.c_uint32], ctypes.c_int),
+    "rf_sim_read_xid_trace": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
+    "rf_needs_warmup": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rf_warmup": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_float], ctypes.c_int),
+    "rf_draw_to_bins": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                         ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+    "rf_set_splat": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rf_sim_counters": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+    "rf_density_estimate": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
+                             ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rf_hist_stats": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p], ctypes.c_int),
+    "rf_tonemap": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                    ctypes.c_float, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rf_shuffle_generate": ([ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rf_probe_xform": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                        ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rf_render": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(RenderDesc), ctypes.c_void_p,
+                   ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    "rf_write_png": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
+}
+
+
+def build(force=False):
+    """Compile the CUDA library for sm_103a (refrakt_gb300/nvbuild.py)."""
+    from . import nvbuild
+    return nvbuild.build(force=force)
+
+
+def library():
+    """The loaded CUDA library.  Raises if it has not been built — there is no fallback."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("refrakt_gb300 CUDA library not built (%s); run "
+                              "`python -c 'import refrakt_gb300 as r; r.build()'`" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise RefraktError(rc, library().rf_last_error().decode(errors="replace"))
+
+
+def _ptr(x):
+    """Device address of a torch tensor, an int, or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return ctypes.c_void_p(x)
+    if hasattr(x, "data_ptr"):
+        if hasattr(x, "is_cuda") and not x.is_cuda:
+            raise ValueError("expected a CUDA tensor")
+        if hasattr(x, "is_contiguous") and not x.is_contiguous():
+            raise ValueError("expected a contiguous tensor")
+        return ctypes.c_void_p(x.data_ptr())
+    raise TypeError("expected a device tensor or address, got %r" % type(x))
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return ctypes.c_void_p(s)
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _string_out(fn, *args):
+    need = ctypes.c_size_t(0)
+    _check(fn(*args, None, 0, ctypes.byref(need)))
+    buf = ctypes.create_string_buffer(need.value)
+    _check(fn(*args, buf, need.value, ctypes.byref(need)))
+    return buf.value.decode()
+
+
+class FlameCompiler:
+    """flame_compiler (src/variation_table.hpp:20-59): the variation table.
+
+    ``yaml_path=None`` uses the built-in copy of the reference's table; a path reads a
+    variations.yaml and checks each entry against the device implementations."""
+
+    def __init__(self, yaml_path=None):
+        h = ctypes.c_void_p()
+        _check(library().rf_compiler_create(yaml_path.encode() if yaml_path else None, ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rf_compiler_destroy(self._h)
+            self._h = None
+
+    def is_variation(self, name):
+        return bool(library().rf_compiler_is_variation(self._h, name.encode()))
+
+    def is_param(self, name):
+        return bool(library().rf_compiler_is_param(self._h, name.encode()))
+
+    def is_common(self, name):
+        return bool(library().rf_compiler_is_common(self._h, name.encode()))
+
+    def is_supported(self, name):
+        return bool(library().rf_compiler_is_supported(self._h, name.encode()))
+
+    def param_owner(self, param):
+        buf = ctypes.create_string_buffer(256)
+        _check(library().rf_compiler_param_owner(self._h, param.encode(), buf, 256))
+        return buf.value.decode()
+
+    def variations(self):
+        n = library().rf_compiler_num_variations(self._h)
+        out = []
+        buf = ctypes.create_string_buffer(256)
+        for i in range(n):
+            _check(library().rf_compiler_variation_name(self._h, i, buf, 256))
+            out.append(buf.value.decode())
+        return out
+
+    def get_parameters_for_variation(self, name):
+        buf = ctypes.create_string_buffer(1024)
+        _check(library().rf_compiler_variation_params(self._h, name.encode(), buf, 1024))
+        s = buf.value.decode()
+        return s.split(",") if s else []
+
+
+class Flame:
+    """A genome (src/flame.hpp:41-61).  Construct with ``load_flame``, ``from_xml`` or ``synthesize``."""
+
+    def __init__(self, handle, compiler):
+        self._h = handle
+        self._compiler = compiler
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rf_flame_free(self._h)
+            self._h = None
+
+    @classmethod
+    def load_flame(cls, path, compiler):
+        h = ctypes.c_void_p()
+        _check(library().rf_flame_load(path.encode(), compiler._h, ctypes.byref(h)))
+        return cls(h, compiler)
+
+    @classmethod
+    def from_xml(cls, xml, compiler):
+        h = ctypes.c_void_p()
+        _check(library().rf_flame_load_xml(xml.encode() if isinstance(xml, str) else xml, compiler._h, ctypes.byref(h)))
+        return cls(h, compiler)
+
+    @classmethod
+    def synthesize(cls, compiler, kind, seed, width, height, n_xforms=0, final_xform=False, force_parametric=False):
+        d = SynthDesc(kind, n_xforms, seed, int(final_xform), int(force_parametric), width, height)
+        h = ctypes.c_void_p()
+        _check(library().rf_flame_synthesize(ctypes.byref(d), compiler._h, ctypes.byref(h)))
+        return cls(h, compiler)
+
+    def to_xml(self):
+        return _string_out(library().rf_flame_to_xml, self._h)
+
+    def info(self):
+        i = FlameInfo()
+        _check(library().rf_flame_get_info(self._h, ctypes.byref(i)))
+        return {"size": tuple(i.size), "center": tuple(i.center), "scale": i.scale, "rotate": i.rotate,
+                "estimator_radius": i.estimator_radius, "estimator_min": i.estimator_min,
+                "estimator_curve": i.estimator_curve, "gamma": i.gamma, "vibrancy": i.vibrancy,
+                "brightness": i.brightness, "num_xforms": i.num_xforms, "has_final": bool(i.has_final),
+                "total_params": i.total_params}
+
+    def set_view(self, center, scale, rotate):
+        c = (ctypes.c_float * 2)(*center)
+        _check(library().rf_flame_set_view(self._h, c, scale, rotate))
+
+    def set_tonemap(self, gamma, brightness, vibrancy):
+        _check(library().rf_flame_set_tonemap(self._h, gamma, brightness, vibrancy))
+
+    def set_estimator(self, radius, min_radius, curve):
+        _check(library().rf_flame_set_estimator(self._h, radius, min_radius, curve))
+
+    def set_xform_value(self, xform, name, value):
+        _check(library().rf_flame_set_xform_value(self._h, xform, name.encode(), value))
+
+    def param_buffer(self):
+        import numpy as np
+        n = ctypes.c_size_t(0)
+        _check(library().rf_flame_param_buffer(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, np.float32)
+        _check(library().rf_flame_param_buffer(self._h, out.ctypes.data_as(ctypes.c_void_p), n.value, ctypes.byref(n)))
+        return out
+
+    def param_layout(self):
+        return json.loads(_string_out(library().rf_flame_param_layout, self._h))
+
+    def screen_affine(self, width, height):
+        out = (ctypes.c_float * 6)()
+        _check(library().rf_flame_screen_affine(self._h, width, height, out))
+        return list(out)
+
+    def xform_draws(self, xform):
+        return library().rf_flame_xform_draws(self._h, xform)
+
+
+class Sim:
+    """Walker slots, RNG states and the shuffle table — ``flame::set_sim_parameters`` plus the
+    per-flame ``warmup`` / ``draw_to_bins`` (src/flame.cpp:105-330)."""
+
+    def __init__(self, walkers, temporal_samples=1, shuffle_count=1024, seed=0, cta_slots=1024, cluster_ctas=1,
+                 steps_per_launch=32, device=0):
+        d = SimDesc(walkers, temporal_samples, shuffle_count, seed, cta_slots, cluster_ctas, steps_per_launch, device)
+        h = ctypes.c_void_p()
+        _check(library().rf_sim_create(ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+        self.walkers = walkers
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rf_sim_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_stream(self, stream):
+        _check(library().rf_sim_set_stream(self._h, _stream(stream)))
+
+    def enable_xid_trace(self, passes):
+        _check(library().rf_sim_enable_xid_trace(self._h, passes))
+
+    def read_xid_trace(self, passes):
+        import numpy as np
+        groups = self.walkers // 256
+        out = np.zeros((passes, groups), np.uint8)
+        got = ctypes.c_uint32(0)
+        _check(library().rf_sim_read_xid_trace(self._h, out.ctypes.data_as(ctypes.c_void_p), out.nbytes, ctypes.byref(got)))
+        return out
+
+    def needs_warmup(self, flame):
+        return bool(library().rf_needs_warmup(self._h, flame._h))
+
+    def warmup(self, flame, num_passes, tss_width=0.02):
+        _check(library().rf_warmup(self._h, flame._h, num_passes, tss_width))
+
+    def set_splat(self, splat):
+        _check(library().rf_set_splat(self._h, splat))
+
+    def draw_to_bins(self, flame, bins_rgba, bins_hits, width, height, num_iter, sync=True):
+        drawn = ctypes.c_uint64(0)
+        _check(library().rf_draw_to_bins(self._h, flame._h, _ptr(bins_rgba), _ptr(bins_hits), width, height,
+                                          num_iter, ctypes.byref(drawn) if sync else None))
+        return drawn.value if sync else None
+
+    def counters(self):
+        out = (ctypes.c_uint64 * 3)()
+        _check(library().rf_sim_counters(self._h, out))
+        return {"drawn": out[0], "emitted": out[1], "steps": out[2]}
+
+    def render(self, flame, width, height, points, supersample=1, fuse_passes=20, tss_width=0.0, k2=0.0,
+               density_estimation=True, out=None):
+        """One frame from genome to host RGBA8 (rf_render).  Returns (image, stats)."""
+        import numpy as np
+        img = out if out is not None else np.zeros((height, width, 4), np.uint8)
+        d = RenderDesc(width, height, supersample, fuse_passes, points, tss_width, k2, int(density_estimation))
+        st = (ctypes.c_double * 3)()
+        _check(library().rf_render(self._h, flame._h, ctypes.byref(d), img.ctypes.data_as(ctypes.c_void_p), st))
+        return img, {"points": st[0], "binned": st[1], "ms": st[2]}
+
+
+def render(sim, flame, *a, **k):
+    return sim.render(flame, *a, **k)
+
+
+def density_estimate(bins_rgba, width, height, radius, min_radius, curve, out, stream=None):
+    _check(library().rf_density_estimate(_ptr(bins_rgba), width, height, radius, min_radius, curve, _ptr(out),
+                                         _stream(stream)))
+
+
+def hist_stats(rgba, width, height, stream=None):
+    out = (ctypes.c_double * 3)()
+    _check(library().rf_hist_stats(_ptr(rgba), width, height, out, _stream(stream)))
+    return {"sum": out[0], "max": out[1], "nonzero": int(out[2])}
+
+
+def tonemap(rgba, width, height, ss, gamma, brightness, vibrancy, k2, out_f32=None, out_rgba8=None, stream=None):
+    _check(library().rf_tonemap(_ptr(rgba), width, height, ss, gamma, brightness, vibrancy, k2, _ptr(out_f32),
+                                _ptr(out_rgba8), _stream(stream)))
+
+
+def shuffle_generate(n, count, seed, out, stream=None):
+    _check(library().rf_shuffle_generate(n, count, seed, _ptr(out), _stream(stream)))
+
+
+def probe_xform(flame, xform, xyc, rng, out, first_run=False, stream=None):
+    n = xyc.shape[0]
+    _check(library().rf_probe_xform(flame._h, xform, n, _ptr(xyc), _ptr(rng), int(first_run), _ptr(out),
+                                    _stream(stream)))
+
+
+def write_png(path, rgba8):
+    import numpy as np
+    a = np.ascontiguousarray(rgba8, np.uint8)
+    h, w = a.shape[:2]
+    _check(library().rf_write_png(path.encode(), a.ctypes.data_as(ctypes.c_void_p), w, h))

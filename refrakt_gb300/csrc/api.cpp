@@ -1,0 +1,705 @@
+// C ABI of refrakt_gb300 (include/refrakt.h): the host runtime around the device kernels.
+//
+// Replaces the reference's flame_compiler / flame classes (src/variation_table.hpp:20-59,
+// src/flame.hpp:41-173) and its GL dispatch loop (src/flame.cpp:105-330, src/main.cpp:490-535).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+#include "internal.h"
+#include "kernels.h"
+
+namespace rfk {
+
+static thread_local std::string g_err;
+int fail(int status, const std::string& msg) {
+    g_err = msg;
+    return status;
+}
+void clear_error() { g_err.clear(); }
+
+static int cuda_fail(cudaError_t e, const char* what) {
+    return fail(RF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define RF_CUDA(call)                                   \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+static std::atomic<uint64_t> g_uid{1};
+
+}  // namespace rfk
+
+using namespace rfk;
+
+struct rf_compiler {
+    std::shared_ptr<const Registry> reg;
+};
+
+struct rf_flame {
+    Genome g;
+    std::shared_ptr<const Registry> reg;
+    uint64_t uid = 0;
+    uint64_t version = 0;
+};
+
+struct rf_sim {
+    rf_sim_desc d{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t N = 0;
+    uint32_t T = 1, ppts = 0, cta = 1024, cluster = 1, L = 32, table_size = 1024;
+    float4* walk[2] = {nullptr, nullptr};
+    int cur = 0;
+    uint4* rng = nullptr;
+    uint16_t* table = nullptr;
+    uint32_t* base_prog = nullptr;
+    uint32_t* progs = nullptr;
+    uint32_t prog_stride = 0, prog_words = 0;
+    float4* palette = nullptr;
+    unsigned long long* counters = nullptr;  // [0] drawn [1] emitted [2] steps [3] call drawn [4] call emitted
+    uint8_t* trace = nullptr;
+    uint32_t trace_passes = 0;
+    uint64_t warmed_uid = 0, warmed_version = 0;
+    uint32_t pass = 0;
+    int splat = RF_SPLAT_AUTO;
+    // rf_render scratch
+    float4* r_bins = nullptr;
+    uint32_t* r_hits = nullptr;
+    float4* r_de = nullptr;
+    uchar4* r_img = nullptr;
+    double* r_stats = nullptr;
+    size_t r_bins_n = 0, r_img_n = 0;
+};
+
+namespace {
+
+int set_device(const rf_sim* s) {
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return RF_OK;
+}
+
+size_t copy_out(const std::string& s, char* buf, size_t cap) {
+    if (buf && cap) {
+        size_t n = std::min(cap - 1, s.size());
+        memcpy(buf, s.data(), n);
+        buf[n] = 0;
+    }
+    return s.size() + 1;
+}
+
+// the chaos kernel reads these counters as unsigned long long
+int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4* bins, uint32_t* hits,
+                  uint32_t W, uint32_t H, const float ss[6]) {
+    uint32_t done = 0;
+    while (done < passes) {
+        const uint32_t steps = std::min(s->L, passes - done);
+        ChaosArgs a{};
+        a.progs = s->progs;
+        a.prog_stride = s->prog_stride;
+        a.prog_words = s->prog_words;
+        a.walk_in = s->walk[s->cur];
+        a.walk_out = s->walk[s->cur ^ 1];
+        a.rng = s->rng;
+        a.table = s->table;
+        a.table_size = s->table_size;
+        a.ppts = s->ppts;
+        a.chunks_per_ts = s->ppts / (s->cta * s->cluster);
+        a.pass0 = s->pass;
+        a.steps = steps;
+        a.seed = s->d.seed;
+        a.first_run = (first_run && done == 0) ? 1 : 0;
+        a.draw = draw ? 1 : 0;
+        if (ss) memcpy(a.ss, ss, sizeof(a.ss));
+        a.W = W;
+        a.H = H;
+        a.bins = bins;
+        a.hits = hits;
+        a.palette = s->palette;
+        a.counters = s->counters;
+        a.trace = s->trace;
+        a.trace_passes = s->trace_passes;
+        a.n_groups = (uint32_t)(s->N / kGroup);
+        const uint32_t grid = (uint32_t)(s->N / s->cta);
+        cudaError_t e = launch_chaos((int)s->cta, (int)s->cluster, a, grid, s->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "chaos kernel launch");
+        s->cur ^= 1;
+        s->pass += steps;
+        done += steps;
+    }
+    return RF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* rf_last_error(void) { return g_err.c_str(); }
+int rf_abi_version(void) { return RF_ABI_VERSION; }
+
+// ---------------------------------------------------------------------------------------------
+// compiler
+// ---------------------------------------------------------------------------------------------
+int rf_compiler_create(const char* yaml_path, rf_compiler** out) {
+    if (!out) return fail(RF_ERR_INVALID_ARG, "rf_compiler_create: out is NULL");
+    *out = nullptr;
+    auto* c = new rf_compiler();
+    if (yaml_path) {
+        if (int rc = load_registry_yaml(yaml_path, c->reg)) { delete c; return rc; }
+    } else {
+        c->reg = builtin_registry();
+    }
+    *out = c;
+    return RF_OK;
+}
+void rf_compiler_destroy(rf_compiler* c) { delete c; }
+int rf_compiler_is_variation(const rf_compiler* c, const char* n) { return (c && n && c->reg->vars.count(n)) ? 1 : 0; }
+int rf_compiler_is_param(const rf_compiler* c, const char* n) { return (c && n && c->reg->param_owner.count(n)) ? 1 : 0; }
+int rf_compiler_is_common(const rf_compiler* c, const char* n) { return (c && n && c->reg->common.count(n)) ? 1 : 0; }
+int rf_compiler_is_supported(const rf_compiler* c, const char* n) {
+    if (!c || !n) return 0;
+    auto it = c->reg->vars.find(n);
+    return (it != c->reg->vars.end() && it->second.kernel_id >= 0) ? 1 : 0;
+}
+int rf_compiler_param_owner(const rf_compiler* c, const char* p, char* buf, size_t cap) {
+    if (!c || !p) return fail(RF_ERR_INVALID_ARG, "rf_compiler_param_owner: null argument");
+    auto it = c->reg->param_owner.find(p);
+    if (it == c->reg->param_owner.end()) return fail(RF_ERR_UNKNOWN_NAME, std::string("not a parameter: ") + p);
+    copy_out(it->second, buf, cap);
+    return RF_OK;
+}
+int rf_compiler_num_variations(const rf_compiler* c) { return c ? (int)c->reg->vars.size() : 0; }
+int rf_compiler_variation_name(const rf_compiler* c, int i, char* buf, size_t cap) {
+    if (!c || i < 0 || i >= (int)c->reg->vars.size()) return fail(RF_ERR_INVALID_ARG, "variation index out of range");
+    auto it = c->reg->vars.begin();
+    std::advance(it, i);
+    copy_out(it->first, buf, cap);
+    return RF_OK;
+}
+int rf_compiler_variation_params(const rf_compiler* c, const char* name, char* buf, size_t cap) {
+    if (!c || !name) return fail(RF_ERR_INVALID_ARG, "rf_compiler_variation_params: null argument");
+    auto it = c->reg->vars.find(name);
+    if (it == c->reg->vars.end()) return fail(RF_ERR_UNKNOWN_NAME, std::string("not a variation: ") + name);
+    std::string s;
+    for (size_t k = 0; k < it->second.params.size(); k++) s += (k ? "," : "") + it->second.params[k];
+    copy_out(s, buf, cap);
+    return RF_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// flames
+// ---------------------------------------------------------------------------------------------
+static int new_flame(Genome&& g, const rf_compiler* c, rf_flame** out) {
+    auto* f = new rf_flame();
+    f->g = std::move(g);
+    f->reg = c->reg;
+    f->uid = g_uid.fetch_add(1);
+    *out = f;
+    return RF_OK;
+}
+
+int rf_flame_load_xml(const char* xml, const rf_compiler* c, rf_flame** out) {
+    if (!xml || !c || !out) return fail(RF_ERR_INVALID_ARG, "rf_flame_load_xml: null argument");
+    *out = nullptr;
+    Genome g;
+    if (int rc = genome_from_xml(xml, *c->reg, g)) return rc;
+    return new_flame(std::move(g), c, out);
+}
+
+int rf_flame_load(const char* path, const rf_compiler* c, rf_flame** out) {
+    if (!path || !c || !out) return fail(RF_ERR_INVALID_ARG, "rf_flame_load: null argument");
+    *out = nullptr;
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return fail(RF_ERR_IO, std::string("cannot read ") + path);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    return rf_flame_load_xml(ss.str().c_str(), c, out);
+}
+
+void rf_flame_free(rf_flame* f) { delete f; }
+
+int rf_flame_to_xml(const rf_flame* f, char* buf, size_t cap, size_t* needed) {
+    if (!f) return fail(RF_ERR_INVALID_ARG, "rf_flame_to_xml: null flame");
+    size_t n = copy_out(genome_to_xml(f->g), buf, cap);
+    if (needed) *needed = n;
+    return RF_OK;
+}
+
+int rf_flame_synthesize(const rf_synth_desc* d, const rf_compiler* c, rf_flame** out) {
+    if (!d || !c || !out) return fail(RF_ERR_INVALID_ARG, "rf_flame_synthesize: null argument");
+    *out = nullptr;
+    Genome g;
+    if (int rc = genome_synthesize(d->kind, d->seed, d->n_xforms, d->final_xform, d->force_parametric, d->width,
+                                   d->height, *c->reg, g))
+        return rc;
+    return new_flame(std::move(g), c, out);
+}
+
+int rf_flame_get_info(const rf_flame* f, rf_flame_info* o) {
+    if (!f || !o) return fail(RF_ERR_INVALID_ARG, "rf_flame_get_info: null argument");
+    const Genome& g = f->g;
+    o->size[0] = g.size[0]; o->size[1] = g.size[1];
+    o->center[0] = g.center[0]; o->center[1] = g.center[1];
+    o->scale = g.scale; o->rotate = g.rotate;
+    o->estimator_radius = g.est_radius; o->estimator_min = g.est_min; o->estimator_curve = g.est_curve;
+    o->gamma = g.gamma; o->vibrancy = g.vibrancy; o->brightness = g.brightness;
+    o->num_xforms = (uint32_t)g.xforms.size();
+    o->has_final = g.has_final ? 1 : 0;
+    std::vector<float> buf;
+    o->total_params = (genome_param_buffer(g, buf, nullptr) == 0) ? (uint32_t)buf.size() : 0;
+    return RF_OK;
+}
+
+int rf_flame_set_view(rf_flame* f, const float center[2], float scale, float rotate) {
+    if (!f || !center) return fail(RF_ERR_INVALID_ARG, "rf_flame_set_view: null argument");
+    f->g.center[0] = center[0]; f->g.center[1] = center[1];
+    f->g.scale = scale; f->g.rotate = rotate;
+    return RF_OK;  // the view does not invalidate walkers (draw_to_bins rebuilds the screen affine)
+}
+
+int rf_flame_set_tonemap(rf_flame* f, float gamma, float brightness, float vibrancy) {
+    if (!f) return fail(RF_ERR_INVALID_ARG, "rf_flame_set_tonemap: null flame");
+    f->g.gamma = gamma; f->g.brightness = brightness; f->g.vibrancy = vibrancy;
+    return RF_OK;
+}
+
+int rf_flame_set_estimator(rf_flame* f, int radius, int min_radius, float curve) {
+    if (!f) return fail(RF_ERR_INVALID_ARG, "rf_flame_set_estimator: null flame");
+    f->g.est_radius = radius; f->g.est_min = min_radius; f->g.est_curve = curve;
+    return RF_OK;
+}
+
+int rf_flame_set_xform_value(rf_flame* f, int xi, const char* name, float v) {
+    if (!f || !name) return fail(RF_ERR_INVALID_ARG, "rf_flame_set_xform_value: null argument");
+    Xform* x = nullptr;
+    if (xi < 0) { if (!f->g.has_final) return fail(RF_ERR_INVALID_ARG, "genome has no final xform"); x = &f->g.final_xf; }
+    else if (xi < (int)f->g.xforms.size()) x = &f->g.xforms[xi];
+    else return fail(RF_ERR_INVALID_ARG, "xform index out of range");
+    Xform before = *x;
+    std::string n = name;
+    if (n == "weight") x->weight = v;
+    else if (n == "color") x->color = v;
+    else if (n == "color_speed") x->color_speed = v;
+    else if (n == "opacity") x->opacity = v;
+    else if (n == "animate") x->rotation_frequency = v > 0 ? 1.0f : 0.0f;
+    else if (n.size() == 6 && n.compare(0, 5, "coefs") == 0 && n[5] >= '0' && n[5] <= '5') x->affine[n[5] - '0'] = v;
+    else if (n.size() == 5 && n.compare(0, 4, "post") == 0 && n[4] >= '0' && n[4] <= '5') {
+        if (!x->has_post) { x->has_post = true; float id[6] = {1, 0, 0, 1, 0, 0}; memcpy(x->post, id, sizeof id); }
+        x->post[n[4] - '0'] = v;
+    } else if (f->reg->param_owner.count(n)) x->params[n] = v;
+    else if (f->reg->vars.count(n)) x->vars[n] = v;
+    else return fail(RF_ERR_UNKNOWN_NAME, "unknown xform field " + n);
+    if (int rc = genome_validate(f->g, *f->reg)) { *x = before; return rc; }
+    f->version++;
+    return RF_OK;
+}
+
+int rf_flame_param_buffer(const rf_flame* f, float* out, size_t cap, size_t* count) {
+    if (!f) return fail(RF_ERR_INVALID_ARG, "rf_flame_param_buffer: null flame");
+    std::vector<float> buf;
+    if (int rc = genome_param_buffer(f->g, buf, nullptr)) return rc;
+    if (out) memcpy(out, buf.data(), std::min(cap, buf.size()) * sizeof(float));
+    if (count) *count = buf.size();
+    return RF_OK;
+}
+
+int rf_flame_param_layout(const rf_flame* f, char* out, size_t cap, size_t* needed) {
+    if (!f) return fail(RF_ERR_INVALID_ARG, "rf_flame_param_layout: null flame");
+    std::vector<float> buf;
+    std::string js;
+    genome_param_buffer(f->g, buf, &js);
+    size_t n = copy_out(js, out, cap);
+    if (needed) *needed = n;
+    return RF_OK;
+}
+
+int rf_flame_screen_affine(const rf_flame* f, uint32_t w, uint32_t h, float out6[6]) {
+    if (!f || !out6) return fail(RF_ERR_INVALID_ARG, "rf_flame_screen_affine: null argument");
+    if (f->g.size[1] == 0) return fail(RF_ERR_INVALID_ARG, "genome size is zero");
+    genome_screen_affine(f->g, w, h, out6);
+    return RF_OK;
+}
+
+int rf_flame_xform_draws(const rf_flame* f, int xi) {
+    if (!f) return -1;
+    return genome_xform_draws(f->g, *f->reg, xi);
+}
+
+// ---------------------------------------------------------------------------------------------
+// simulation
+// ---------------------------------------------------------------------------------------------
+int rf_sim_create(const rf_sim_desc* d, rf_sim** out) {
+    if (!d || !out) return fail(RF_ERR_INVALID_ARG, "rf_sim_create: null argument");
+    *out = nullptr;
+    const uint32_t cta = d->cta_slots ? d->cta_slots : 1024;
+    const uint32_t T = d->temporal_samples ? d->temporal_samples : 1;
+    const uint32_t cluster = d->cluster_ctas ? d->cluster_ctas : 1;
+    if (cta != 256 && cta != 512 && cta != 1024) return fail(RF_ERR_INVALID_ARG, "cta_slots must be 256, 512 or 1024");
+    const bool ok_cluster = cluster == 1 || (cluster == 2 && cta >= 512) || (cluster == 4 && cta >= 512) ||
+                            (cluster == 8 && cta == 512);
+    if (!ok_cluster) return fail(RF_ERR_INVALID_ARG, "cluster_ctas must be 1, 2 or 4 (8 with 512-slot CTAs)");
+    const uint32_t domain = cta * cluster;
+    if (d->walkers == 0 || d->walkers % T) return fail(RF_ERR_INVALID_ARG, "walkers must be a positive multiple of temporal_samples");
+    const uint64_t ppts = d->walkers / T;
+    if (ppts % domain) return fail(RF_ERR_INVALID_ARG, "walkers per temporal sample must be a multiple of cta_slots * cluster_ctas");
+    if (ppts > 0x7fffffffull) return fail(RF_ERR_CAPACITY, "too many walkers per temporal sample");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(RF_ERR_NO_DEVICE, "no CUDA device");
+    if (d->device < 0 || d->device >= ndev) return fail(RF_ERR_INVALID_ARG, "device ordinal out of range");
+    auto* s = new rf_sim();
+    s->d = *d;
+    s->device = d->device;
+    s->N = d->walkers;
+    s->T = T;
+    s->ppts = (uint32_t)ppts;
+    s->cta = cta;
+    s->cluster = cluster;
+    s->L = d->steps_per_launch ? std::min<uint32_t>(d->steps_per_launch, 256) : 32;
+    s->table_size = d->shuffle_count ? d->shuffle_count : 1024;
+    auto cleanup = [&](int rc) { rf_sim_destroy(s); return rc; };
+    if (int rc = set_device(s)) { delete s; return rc; }
+    cudaError_t e;
+#define ALLOC(ptr, bytes) \
+    if ((e = cudaMalloc((void**)&(ptr), (bytes))) != cudaSuccess) return cleanup(cuda_fail(e, "cudaMalloc"));
+    ALLOC(s->walk[0], s->N * sizeof(float4));
+    ALLOC(s->walk[1], s->N * sizeof(float4));
+    ALLOC(s->rng, s->N * sizeof(uint4));
+    ALLOC(s->table, (size_t)s->table_size * domain * sizeof(uint16_t));
+    ALLOC(s->base_prog, kProgMaxWords * sizeof(uint32_t));
+    s->prog_stride = kProgMaxWords;
+    ALLOC(s->progs, (size_t)T * s->prog_stride * sizeof(uint32_t));
+    ALLOC(s->palette, 256 * sizeof(float4));
+    ALLOC(s->counters, 8 * sizeof(unsigned long long));
+#undef ALLOC
+    if ((e = launch_init_rng(s->rng, s->N, d->seed, s->stream)) != cudaSuccess) return cleanup(cuda_fail(e, "rng init"));
+    if ((e = launch_shuffle_table(s->table, domain, s->table_size, d->seed, s->stream)) != cudaSuccess)
+        return cleanup(cuda_fail(e, "shuffle table"));
+    if ((e = cudaMemsetAsync(s->counters, 0, 8 * sizeof(unsigned long long), s->stream)) != cudaSuccess)
+        return cleanup(cuda_fail(e, "memset"));
+    if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cleanup(cuda_fail(e, "sim init"));
+    *out = s;
+    return RF_OK;
+}
+
+int rf_sim_destroy(rf_sim* s) {
+    if (!s) return RF_OK;
+    cudaSetDevice(s->device);
+    cudaStreamSynchronize(s->stream);
+    void* ptrs[] = {s->walk[0], s->walk[1], s->rng, s->table, s->base_prog, s->progs, s->palette, s->counters,
+                    s->trace, s->r_bins, s->r_hits, s->r_de, s->r_img, s->r_stats};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete s;
+    return RF_OK;
+}
+
+int rf_sim_set_stream(rf_sim* s, void* stream) {
+    if (!s) return fail(RF_ERR_INVALID_ARG, "rf_sim_set_stream: null sim");
+    s->stream = (cudaStream_t)stream;
+    return RF_OK;
+}
+
+int rf_sim_enable_xid_trace(rf_sim* s, uint32_t max_passes) {
+    if (!s) return fail(RF_ERR_INVALID_ARG, "rf_sim_enable_xid_trace: null sim");
+    if (int rc = set_device(s)) return rc;
+    if (s->trace) { cudaFree(s->trace); s->trace = nullptr; s->trace_passes = 0; }
+    if (max_passes == 0) return RF_OK;
+    const size_t bytes = (size_t)max_passes * (s->N / kGroup);
+    RF_CUDA(cudaMalloc((void**)&s->trace, bytes));
+    RF_CUDA(cudaMemsetAsync(s->trace, 0xff, bytes, s->stream));
+    s->trace_passes = max_passes;
+    return RF_OK;
+}
+
+int rf_sim_read_xid_trace(rf_sim* s, uint8_t* out, size_t cap, uint32_t* passes) {
+    if (!s || !s->trace) return fail(RF_ERR_INVALID_ARG, "xid trace not enabled");
+    if (int rc = set_device(s)) return rc;
+    const size_t bytes = std::min(cap, (size_t)s->trace_passes * (s->N / kGroup));
+    RF_CUDA(cudaStreamSynchronize(s->stream));
+    RF_CUDA(cudaMemcpy(out, s->trace, bytes, cudaMemcpyDeviceToHost));
+    if (passes) *passes = std::min(s->pass, s->trace_passes);
+    return RF_OK;
+}
+
+int rf_needs_warmup(const rf_sim* s, const rf_flame* f) {
+    if (!s || !f) return 1;
+    return (s->warmed_uid != f->uid || s->warmed_version != f->version) ? 1 : 0;
+}
+
+int rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_width) {
+    if (!s || !f) return fail(RF_ERR_INVALID_ARG, "rf_warmup: null argument");
+    if (int rc = set_device(s)) return rc;
+    std::vector<uint32_t> prog;
+    if (int rc = genome_program(f->g, *f->reg, prog)) return rc;
+    if (int rc = genome_validate(f->g, *f->reg)) return rc;
+    s->prog_words = (uint32_t)prog.size();
+    RF_CUDA(cudaMemcpyAsync(s->base_prog, prog.data(), prog.size() * 4, cudaMemcpyHostToDevice, s->stream));
+    RF_CUDA(launch_animate(s->base_prog, s->prog_words, s->T, tss_width, s->progs, s->prog_stride, s->stream));
+    RF_CUDA(cudaMemcpyAsync(s->palette, f->g.palette, sizeof(f->g.palette), cudaMemcpyHostToDevice, s->stream));
+    RF_CUDA(cudaMemsetAsync(s->counters, 0, 8 * sizeof(unsigned long long), s->stream));
+    // the pageable uploads above complete before the call returns; keep the host copy alive
+    RF_CUDA(cudaStreamSynchronize(s->stream));
+    s->pass = 0;
+    // flame::warmup: one first-run pass (sample points, jitter, random colours), then num_passes
+    if (int rc = launch_passes(s, 1 + num_passes, true, false, nullptr, nullptr, 0, 0, nullptr)) return rc;
+    s->warmed_uid = f->uid;
+    s->warmed_version = f->version;
+    return RF_OK;
+}
+
+int rf_set_splat(rf_sim* s, int splat) {
+    if (!s) return fail(RF_ERR_INVALID_ARG, "rf_set_splat: null sim");
+    s->splat = splat;
+    return RF_OK;
+}
+
+int rf_draw_to_bins(rf_sim* s, rf_flame* f, float* bins_rgba, uint32_t* bins_hits, uint32_t W, uint32_t H,
+                    uint32_t num_iter, uint64_t* drawn) {
+    if (!s || !f || !bins_rgba) return fail(RF_ERR_INVALID_ARG, "rf_draw_to_bins: null argument");
+    if (W == 0 || H == 0 || W > 65536 || H > 65536) return fail(RF_ERR_INVALID_ARG, "bin grid must be 1..65536 on each side");
+    if (rf_needs_warmup(s, f)) return fail(RF_ERR_NEEDS_WARMUP, "flame changed or not warmed up: call rf_warmup");
+    if (f->g.size[1] == 0) return fail(RF_ERR_INVALID_ARG, "genome size is zero");
+    if (((uintptr_t)bins_rgba) & 15) return fail(RF_ERR_INVALID_ARG, "bins_rgba must be 16-byte aligned");
+    if (int rc = set_device(s)) return rc;
+    float ss[6];
+    genome_screen_affine(f->g, W, H, ss);
+    // [0] drawn, [1] emitted count this call
+    RF_CUDA(cudaMemsetAsync(s->counters, 0, 2 * sizeof(unsigned long long), s->stream));
+    if (int rc = launch_passes(s, num_iter, false, true, (float4*)bins_rgba, bins_hits, W, H, ss)) return rc;
+    if (drawn) {
+        unsigned long long c[1];
+        RF_CUDA(cudaStreamSynchronize(s->stream));
+        RF_CUDA(cudaMemcpy(c, s->counters, sizeof c, cudaMemcpyDeviceToHost));
+        *drawn = c[0];
+    }
+    return RF_OK;
+}
+
+int rf_sim_counters(rf_sim* s, uint64_t out[3]) {
+    if (!s || !out) return fail(RF_ERR_INVALID_ARG, "rf_sim_counters: null argument");
+    if (int rc = set_device(s)) return rc;
+    unsigned long long c[3];
+    RF_CUDA(cudaStreamSynchronize(s->stream));
+    RF_CUDA(cudaMemcpy(c, s->counters, sizeof c, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 3; i++) out[i] = c[i];
+    return RF_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// image passes
+// ---------------------------------------------------------------------------------------------
+int rf_density_estimate(const float* in, uint32_t w, uint32_t h, int radius, int min_radius, float curve, float* out,
+                        void* stream) {
+    if (!in || !out || w == 0 || h == 0) return fail(RF_ERR_INVALID_ARG, "rf_density_estimate: bad arguments");
+    if (radius < 0 || radius > 100 || min_radius < 0 || min_radius > 100)
+        return fail(RF_ERR_INVALID_ARG, "estimator radii must be within 0..100 (main.cpp:502)");
+    if (in == out) return fail(RF_ERR_INVALID_ARG, "rf_density_estimate: in and out must differ");
+    RF_CUDA(launch_density((const float4*)in, w, h, radius, min_radius, curve, (float4*)out, (cudaStream_t)stream));
+    return RF_OK;
+}
+
+int rf_hist_stats(const float* rgba, uint32_t w, uint32_t h, double* out3, void* stream) {
+    if (!rgba || !out3) return fail(RF_ERR_INVALID_ARG, "rf_hist_stats: null argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    double* d = nullptr;
+    RF_CUDA(cudaMallocAsync((void**)&d, 3 * sizeof(double), st));
+    cudaError_t e = launch_stats((const float4*)rgba, w, h, d, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out3, d, 3 * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "rf_hist_stats");
+    uint64_t nz;
+    memcpy(&nz, &out3[2], 8);
+    out3[2] = (double)nz;
+    return RF_OK;
+}
+
+int rf_tonemap(const float* rgba, uint32_t w, uint32_t h, uint32_t ss, float gamma, float brightness, float vibrancy,
+               float k2, float* out_f32, uint8_t* out8, void* stream) {
+    if (!rgba || w == 0 || h == 0 || ss == 0 || w % ss || h % ss)
+        return fail(RF_ERR_INVALID_ARG, "rf_tonemap: bad arguments (width and height must be multiples of ss)");
+    cudaStream_t st = (cudaStream_t)stream;
+    double* stats = nullptr;
+    if (!(k2 > 0.0f)) {
+        RF_CUDA(cudaMallocAsync((void**)&stats, 3 * sizeof(double), st));
+        cudaError_t e = launch_stats((const float4*)rgba, w, h, stats, st);
+        if (e != cudaSuccess) { cudaFreeAsync(stats, st); return cuda_fail(e, "stats"); }
+    }
+    cudaError_t e = launch_tonemap((const float4*)rgba, w, h, ss, gamma, brightness, vibrancy, k2, stats,
+                                   (float4*)out_f32, (uchar4*)out8, st);
+    if (stats) cudaFreeAsync(stats, st);
+    if (e != cudaSuccess) return cuda_fail(e, "tonemap");
+    return RF_OK;
+}
+
+int rf_shuffle_generate(uint32_t n, uint32_t count, uint64_t seed, uint16_t* out, void* stream) {
+    if (!out || n == 0 || n > 65536 || count == 0) return fail(RF_ERR_INVALID_ARG, "rf_shuffle_generate: bad arguments");
+    RF_CUDA(launch_shuffle_table(out, n, count, seed, (cudaStream_t)stream));
+    return RF_OK;
+}
+
+int rf_probe_xform(rf_flame* f, int xform, uint32_t n, const float* in, uint32_t* rng, int first_run, float* out,
+                   void* stream) {
+    if (!f || !in || !rng || !out) return fail(RF_ERR_INVALID_ARG, "rf_probe_xform: null argument");
+    if (xform >= (int)f->g.xforms.size() || (xform < 0 && !f->g.has_final))
+        return fail(RF_ERR_INVALID_ARG, "xform index out of range");
+    std::vector<uint32_t> prog;
+    if (int rc = genome_program(f->g, *f->reg, prog)) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    uint32_t* d = nullptr;
+    RF_CUDA(cudaMallocAsync((void**)&d, prog.size() * 4, st));
+    cudaError_t e = cudaMemcpyAsync(d, prog.data(), prog.size() * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && n) e = launch_probe(d, xform, n, in, rng, first_run, out, st);
+    cudaFreeAsync(d, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "rf_probe_xform");
+    return RF_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// end-to-end frame
+// ---------------------------------------------------------------------------------------------
+int rf_render(rf_sim* s, rf_flame* f, const rf_render_desc* d, uint8_t* out, double* stats) {
+    if (!s || !f || !d || !out) return fail(RF_ERR_INVALID_ARG, "rf_render: null argument");
+    const uint32_t ss = d->supersample ? d->supersample : 1;
+    if (d->width == 0 || d->height == 0) return fail(RF_ERR_INVALID_ARG, "rf_render: empty image");
+    if (f->g.size[1] == 0) return fail(RF_ERR_INVALID_ARG, "genome size is zero");
+    const uint32_t W = d->width * ss, H = d->height * ss;
+    if (W > 65536 || H > 65536) return fail(RF_ERR_INVALID_ARG, "rf_render: bin grid too large");
+    if (int rc = set_device(s)) return rc;
+    const size_t nb = (size_t)W * H, ni = (size_t)d->width * d->height;
+    if (s->r_bins_n != nb) {
+        cudaFree(s->r_bins); cudaFree(s->r_hits); cudaFree(s->r_de);
+        s->r_bins = nullptr; s->r_hits = nullptr; s->r_de = nullptr; s->r_bins_n = 0;
+        RF_CUDA(cudaMalloc((void**)&s->r_bins, nb * sizeof(float4)));
+        RF_CUDA(cudaMalloc((void**)&s->r_hits, nb * sizeof(uint32_t)));
+        RF_CUDA(cudaMalloc((void**)&s->r_de, nb * sizeof(float4)));
+        s->r_bins_n = nb;
+    }
+    if (s->r_img_n != ni) {
+        cudaFree(s->r_img);
+        s->r_img = nullptr; s->r_img_n = 0;
+        RF_CUDA(cudaMalloc((void**)&s->r_img, ni * sizeof(uchar4)));
+        s->r_img_n = ni;
+    }
+    if (!s->r_stats) RF_CUDA(cudaMalloc((void**)&s->r_stats, 4 * sizeof(double)));
+    float ssa[6];
+    genome_screen_affine(f->g, W, H, ssa);
+    cudaEvent_t e0, e1;
+    RF_CUDA(cudaEventCreate(&e0));
+    RF_CUDA(cudaEventCreate(&e1));
+    auto done = [&](int rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; };
+    if (cudaEventRecord(e0, s->stream) != cudaSuccess) return done(fail(RF_ERR_CUDA, "event record"));
+    // fuse_passes counts every discarded pass, the first-run pass included
+    if (int rc = rf_warmup(s, f, d->fuse_passes ? d->fuse_passes - 1 : 0, d->tss_width)) return done(rc);
+    const uint64_t passes = (d->points + s->N - 1) / s->N;
+    if (passes > 0xffffffffull) return done(fail(RF_ERR_CAPACITY, "rf_render: too many passes"));
+    cudaError_t e = cudaMemsetAsync(s->r_bins, 0, nb * sizeof(float4), s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->r_hits, 0, nb * sizeof(uint32_t), s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->counters, 0, 2 * sizeof(unsigned long long), s->stream);
+    if (e != cudaSuccess) return done(cuda_fail(e, "rf_render clear"));
+    if (int rc = launch_passes(s, (uint32_t)passes, false, true, s->r_bins, s->r_hits, W, H, ssa)) return done(rc);
+    const float4* src = s->r_bins;
+    if (d->density_estimation && (f->g.est_radius > 0 || f->g.est_min > 0)) {
+        const int R = std::min(100, f->g.est_radius), mn = std::min(100, f->g.est_min);
+        e = launch_density(s->r_bins, W, H, R, mn, f->g.est_curve, s->r_de, s->stream);
+        if (e != cudaSuccess) return done(cuda_fail(e, "density estimation"));
+        src = s->r_de;
+    }
+    const double* st = nullptr;
+    if (!(d->k2 > 0.0f)) {
+        e = launch_stats(src, W, H, s->r_stats, s->stream);
+        if (e != cudaSuccess) return done(cuda_fail(e, "stats"));
+        st = s->r_stats;
+    }
+    e = launch_tonemap(src, W, H, ss, f->g.gamma, f->g.brightness, f->g.vibrancy, d->k2, st, nullptr, s->r_img,
+                       s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, s->r_img, ni * sizeof(uchar4), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return done(cuda_fail(e, "rf_render"));
+    if (stats) {
+        unsigned long long c[2];
+        float ms = 0;
+        cudaMemcpy(c, s->counters, sizeof c, cudaMemcpyDeviceToHost);
+        cudaEventElapsedTime(&ms, e0, e1);
+        stats[0] = (double)passes * (double)s->N;
+        stats[1] = (double)c[0];
+        stats[2] = ms;
+    }
+    return done(RF_OK);
+}
+
+// ---------------------------------------------------------------------------------------------
+// PNG output (stored deflate blocks; no compression library needed)
+// ---------------------------------------------------------------------------------------------
+namespace {
+uint32_t crc32_update(uint32_t c, const uint8_t* p, size_t n) {
+    static uint32_t table[256];
+    static bool init = false;
+    if (!init) {
+        for (uint32_t i = 0; i < 256; i++) {
+            uint32_t v = i;
+            for (int k = 0; k < 8; k++) v = (v & 1) ? 0xedb88320u ^ (v >> 1) : v >> 1;
+            table[i] = v;
+        }
+        init = true;
+    }
+    c ^= 0xffffffffu;
+    for (size_t i = 0; i < n; i++) c = table[(c ^ p[i]) & 0xff] ^ (c >> 8);
+    return c ^ 0xffffffffu;
+}
+void put_be32(std::string& s, uint32_t v) {
+    s += (char)(v >> 24); s += (char)(v >> 16); s += (char)(v >> 8); s += (char)v;
+}
+void chunk(std::string& out, const char* type, const std::string& data) {
+    put_be32(out, (uint32_t)data.size());
+    std::string td = std::string(type, 4) + data;
+    out += td;
+    put_be32(out, crc32_update(0, (const uint8_t*)td.data(), td.size()));
+}
+}  // namespace
+
+int rf_write_png(const char* path, const uint8_t* rgba8, uint32_t w, uint32_t h) {
+    if (!path || !rgba8 || w == 0 || h == 0) return fail(RF_ERR_INVALID_ARG, "rf_write_png: bad arguments");
+    std::string raw;
+    raw.reserve((size_t)(w * 4 + 1) * h);
+    for (uint32_t y = 0; y < h; y++) {
+        raw += '\0';  // filter type 0
+        raw.append((const char*)rgba8 + (size_t)y * w * 4, (size_t)w * 4);
+    }
+    std::string z = "\x78\x01";
+    uint32_t a = 1, b = 0;
+    for (unsigned char ch : raw) { a = (a + ch) % 65521; b = (b + a) % 65521; }
+    for (size_t p = 0; p < raw.size() || p == 0; p += 65535) {
+        size_t n = std::min<size_t>(65535, raw.size() - p);
+        bool last = p + n >= raw.size();
+        z += (char)(last ? 1 : 0);
+        z += (char)(n & 0xff); z += (char)(n >> 8);
+        z += (char)(~n & 0xff); z += (char)((~n >> 8) & 0xff);
+        z.append(raw, p, n);
+        if (last) break;
+    }
+    put_be32(z, (b << 16) | a);
+    std::string png = "\x89PNG\r\n\x1a\n";
+    std::string ihdr;
+    put_be32(ihdr, w); put_be32(ihdr, h);
+    ihdr += (char)8; ihdr += (char)6; ihdr += (char)0; ihdr += (char)0; ihdr += (char)0;
+    chunk(png, "IHDR", ihdr);
+    chunk(png, "IDAT", z);
+    chunk(png, "IEND", "");
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return fail(RF_ERR_IO, std::string("cannot write ") + path);
+    f.write(png.data(), (std::streamsize)png.size());
+    return f ? RF_OK : fail(RF_ERR_IO, std::string("write failed: ") + path);
+}
+
+}  // extern "C"

@@ -1,0 +1,305 @@
+// Image passes after the chaos game: adaptive density estimation, FP64 histogram statistics
+// and the log-density tonemap with a supersample box filter.
+//
+// The reference does density estimation as a GL point-sprite raster pass with additive
+// blending (src/main.cpp:490-515, shaders/density_vert.glsl:26-63, density_frag.glsl:9-18):
+// every non-empty bin becomes a sprite of radius r = max(min, min(R, int(R / a^curve))) whose
+// fragments add color * (1 - d^2) * (2/pi) / r^2.  Here the same sum is a gather: each output
+// bin reads the bins within the largest radius present near it and keeps those whose disc
+// covers it.  The disc is the symmetric restatement 4 (dx^2 + dy^2) <= (2r + 1)^2 with
+// d^2 = (dx^2 + dy^2) / (r + 0.5)^2 (the GL sprite's sub-pixel centring depends on point
+// rasterisation rules).  Radii come from thresholds on a, computed on the host in FP64, and
+// the kernel weights from a per-radius table, so every radius and weight is exactly defined.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "kernels.h"
+
+namespace rfk {
+
+constexpr int kDeTileX = 32, kDeTileY = 8;
+constexpr int kDeMaxSmemR = 12;  // radius handled through shared-memory tiles
+
+struct DeTables {
+    float thr[101];      // thr[k-1]: bin radius >= k  <=>  a <= thr (curve > 0) or a >= thr (curve < 0)
+    int R, min_r, mode;  // mode 0: curve > 0, 1: curve < 0, 2: curve == 0 (radius R)
+    int wbase[102];      // offset of radius r's (r+1)^2 weights
+};
+
+__device__ __forceinline__ int de_radius(float a, const DeTables& T) {
+    int r;
+    if (T.mode == 2) r = T.R;
+    else {
+        // thresholds are monotone: binary search for the largest k with the condition true
+        int lo = 0, hi = T.R;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            const bool ok = (T.mode == 0) ? (a <= T.thr[mid - 1]) : (a >= T.thr[mid - 1]);
+            if (ok) lo = mid; else hi = mid - 1;
+        }
+        r = lo;
+    }
+    return r > T.min_r ? r : T.min_r;  // max(min, min(R, int(R / a^curve))), density_vert.glsl:35-44
+}
+
+// pass 1: radius per bin (255 = empty)
+__global__ void de_radius_kernel(const float4* __restrict__ in, size_t n, const DeTables T, uint8_t* __restrict__ rad) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float a = in[i].w;
+        rad[i] = (a == 0.0f || a != a) ? (uint8_t)255 : (uint8_t)de_radius(a, T);
+    }
+}
+
+// pass 2: gather through a shared-memory tile with a halo of R bins
+template <int R>
+__global__ void __launch_bounds__(kDeTileX * kDeTileY) de_gather_kernel(
+    const float4* __restrict__ in, const uint8_t* __restrict__ rad, uint32_t w, uint32_t h,
+    const float* __restrict__ weights, const DeTables T, float4* __restrict__ out) {
+    constexpr int SW = kDeTileX + 2 * R, SH = kDeTileY + 2 * R;
+    __shared__ float4 s_c[SH][SW];
+    __shared__ uint8_t s_r[SH][SW];
+    __shared__ int s_max;
+    const int tx = threadIdx.x % kDeTileX, ty = threadIdx.x / kDeTileX;
+    const int x0 = blockIdx.x * kDeTileX - R, y0 = blockIdx.y * kDeTileY - R;
+    if (threadIdx.x == 0) s_max = 0;
+    __syncthreads();
+    int lmax = 0;
+    for (int i = threadIdx.x; i < SW * SH; i += blockDim.x) {
+        const int sx = i % SW, sy = i / SW;
+        const int gx = x0 + sx, gy = y0 + sy;
+        float4 v = make_float4(0, 0, 0, 0);
+        uint8_t r = 255;
+        if (gx >= 0 && gy >= 0 && gx < (int)w && gy < (int)h) {
+            const size_t gi = (size_t)gy * w + gx;
+            r = rad[gi];
+            if (r != 255) v = in[gi];
+        }
+        s_c[sy][sx] = v;
+        s_r[sy][sx] = r;
+        if (r != 255 && r > lmax) lmax = r;
+    }
+    atomicMax(&s_max, lmax);
+    __syncthreads();
+    const int ox = blockIdx.x * kDeTileX + tx, oy = blockIdx.y * kDeTileY + ty;
+    if (ox >= (int)w || oy >= (int)h) return;
+    const int rm = s_max;
+    float4 acc = make_float4(0, 0, 0, 0);
+    for (int dy = -rm; dy <= rm; dy++) {
+        for (int dx = -rm; dx <= rm; dx++) {
+            const int sx = tx + R + dx, sy = ty + R + dy;
+            const int r = s_r[sy][sx];
+            if (r == 255) continue;
+            const int ax = dx < 0 ? -dx : dx, ay = dy < 0 ? -dy : dy;
+            if (ax > r || ay > r) continue;
+            float wt;
+            if (r == 0) wt = 1.0f;
+            else {
+                if (4 * (ax * ax + ay * ay) > (2 * r + 1) * (2 * r + 1)) continue;
+                wt = weights[T.wbase[r] + ay * (r + 1) + ax];
+            }
+            const float4 v = s_c[sy][sx];
+            acc.x = fmaf(v.x, wt, acc.x);
+            acc.y = fmaf(v.y, wt, acc.y);
+            acc.z = fmaf(v.z, wt, acc.z);
+            acc.w = fmaf(v.w, wt, acc.w);
+        }
+    }
+    out[(size_t)oy * w + ox] = acc;
+}
+
+// large radii: the same gather straight from global memory
+__global__ void de_gather_global_kernel(const float4* __restrict__ in, const uint8_t* __restrict__ rad,
+                                        uint32_t w, uint32_t h, const float* __restrict__ weights,
+                                        const DeTables T, float4* __restrict__ out) {
+    const int ox = blockIdx.x * blockDim.x + threadIdx.x, oy = blockIdx.y;
+    if (ox >= (int)w) return;
+    const int Rm = T.R > T.min_r ? T.R : T.min_r;
+    float4 acc = make_float4(0, 0, 0, 0);
+    for (int dy = -Rm; dy <= Rm; dy++) {
+        const int gy = oy + dy;
+        if (gy < 0 || gy >= (int)h) continue;
+        for (int dx = -Rm; dx <= Rm; dx++) {
+            const int gx = ox + dx;
+            if (gx < 0 || gx >= (int)w) continue;
+            const size_t gi = (size_t)gy * w + gx;
+            const int r = rad[gi];
+            if (r == 255) continue;
+            const int ax = dx < 0 ? -dx : dx, ay = dy < 0 ? -dy : dy;
+            if (ax > r || ay > r) continue;
+            float wt;
+            if (r == 0) wt = 1.0f;
+            else {
+                if (4 * (ax * ax + ay * ay) > (2 * r + 1) * (2 * r + 1)) continue;
+                wt = weights[T.wbase[r] + ay * (r + 1) + ax];
+            }
+            const float4 v = in[gi];
+            acc.x = fmaf(v.x, wt, acc.x);
+            acc.y = fmaf(v.y, wt, acc.y);
+            acc.z = fmaf(v.z, wt, acc.z);
+            acc.w = fmaf(v.w, wt, acc.w);
+        }
+    }
+    out[(size_t)oy * w + ox] = acc;
+}
+
+// FP64 sum and max of the density channel, count of non-empty bins
+__global__ void stats_kernel(const float4* __restrict__ in, size_t n, double* out) {
+    double s = 0.0, m = 0.0;
+    unsigned long long nz = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double a = (double)in[i].w;
+        s += a;
+        m = a > m ? a : m;
+        nz += (a > 0.0) ? 1 : 0;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, o);
+        m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+        nz += __shfl_down_sync(0xffffffffu, nz, o);
+    }
+    __shared__ double ss[32], sm[32];
+    __shared__ unsigned long long sn[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { ss[wid] = s; sm[wid] = m; sn[wid] = nz; }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        s = lane < nw ? ss[lane] : 0.0;
+        m = lane < nw ? sm[lane] : 0.0;
+        nz = lane < nw ? sn[lane] : 0ull;
+        for (int o = 16; o > 0; o >>= 1) {
+            s += __shfl_down_sync(0xffffffffu, s, o);
+            m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+            nz += __shfl_down_sync(0xffffffffu, nz, o);
+        }
+        if (lane == 0) {
+            atomicAdd(out, s);
+            // a >= 0: the IEEE bit pattern orders like the value
+            atomicMax(reinterpret_cast<unsigned long long*>(out + 1), (unsigned long long)__double_as_longlong(m));
+            atomicAdd(reinterpret_cast<unsigned long long*>(out + 2), nz);
+        }
+    }
+}
+
+// tonemap.glsl:18-38 with an ss x ss box filter: per bin c *= 0.5*brightness*log10(1 + a*k2)/a,
+// mean over the block, then z = a^(1/gamma), rgb = clamp(mix(rgb^(1/gamma), (z/a)*rgb, vibrancy)).
+// A block with no density (where the shader would divide 0 by 0) is opaque black.
+__global__ void tonemap_kernel(const float4* __restrict__ in, uint32_t w, uint32_t h, uint32_t ss, float gamma,
+                               float brightness, float vibrancy, float k2, const double* __restrict__ stats,
+                               float4* __restrict__ out_f32, uchar4* __restrict__ out8) {
+    const uint32_t ow = w / ss, oh = h / ss;
+    const uint32_t ox = blockIdx.x * blockDim.x + threadIdx.x, oy = blockIdx.y;
+    if (ox >= ow || oy >= oh) return;
+    float k = k2;
+    if (!(k > 0.0f)) {
+        const double sum = stats ? stats[0] : 0.0;
+        k = sum > 0.0 ? (float)((double)w * (double)h / sum) : 1.0f;
+    }
+    float4 acc = make_float4(0, 0, 0, 0);
+    for (uint32_t j = 0; j < ss; j++) {
+        const float4* row = in + (size_t)(oy * ss + j) * w + (size_t)ox * ss;
+        for (uint32_t i = 0; i < ss; i++) {
+            const float4 c = row[i];
+            if (c.w > 0.0f) {
+                const float ls = 0.5f * brightness * log1pf(c.w * k) * 0.434294481903251827651128918916f / c.w;
+                acc.x = fmaf(c.x, ls, acc.x);
+                acc.y = fmaf(c.y, ls, acc.y);
+                acc.z = fmaf(c.z, ls, acc.z);
+                acc.w = fmaf(c.w, ls, acc.w);
+            }
+        }
+    }
+    const float inv = 1.0f / (float)(ss * ss);
+    float4 o = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    const float a = acc.w * inv;
+    if (a > 0.0f) {
+        const float ig = 1.0f / gamma;
+        const float gf = powf(a, ig) / a;
+        const float rgb[3] = {acc.x * inv, acc.y * inv, acc.z * inv};
+        float res[3];
+        for (int q = 0; q < 3; q++) {
+            const float v = powf(rgb[q], ig) * (1.0f - vibrancy) + gf * rgb[q] * vibrancy;
+            res[q] = fminf(fmaxf(v, 0.0f), 1.0f);
+        }
+        o = make_float4(res[0], res[1], res[2], 1.0f);
+    }
+    const size_t oi = (size_t)oy * ow + ox;
+    if (out_f32) out_f32[oi] = o;
+    if (out8) out8[oi] = make_uchar4((unsigned char)lrintf(o.x * 255.0f), (unsigned char)lrintf(o.y * 255.0f),
+                                     (unsigned char)lrintf(o.z * 255.0f), 255);
+}
+
+// ---------------------------------------------------------------------------------------------
+static void de_tables(int R, int min_r, float curve, DeTables& T, std::vector<float>& wts) {
+    T.R = R;
+    T.min_r = min_r;
+    T.mode = (curve > 0.0f) ? 0 : (curve < 0.0f ? 1 : 2);
+    for (int k = 1; k <= R; k++) {
+        // int(R / a^curve) >= k  <=>  a^curve <= R / k
+        const double t = std::pow((double)R / (double)k, 1.0 / (double)curve);
+        float f = (float)t;
+        if (T.mode == 0 && (double)f > t) f = std::nextafter(f, -INFINITY);  // a <= f  <=>  a <= t
+        if (T.mode == 1 && (double)f < t) f = std::nextafter(f, INFINITY);   // a >= f  <=>  a >= t
+        T.thr[k - 1] = f;
+    }
+    wts.clear();
+    const int rmax = R > min_r ? R : min_r;
+    for (int r = 0; r <= rmax && r <= 100; r++) {
+        T.wbase[r] = (int)wts.size();
+        const double nf = 0.63661977236 / (double)(r * r ? r * r : 1);
+        const double den = (r + 0.5) * (r + 0.5);
+        for (int ay = 0; ay <= r; ay++)
+            for (int ax = 0; ax <= r; ax++) {
+                const int d2 = ax * ax + ay * ay;
+                wts.push_back(r == 0 ? 1.0f : (float)((1.0 - (double)d2 / den) * nf));
+            }
+    }
+}
+
+cudaError_t launch_density(const float4* in, uint32_t w, uint32_t h, int R, int min_r, float curve, float4* out,
+                           cudaStream_t st) {
+    DeTables T;
+    std::vector<float> wts;
+    de_tables(R, min_r, curve, T, wts);
+    const size_t n = (size_t)w * h;
+    uint8_t* rad = nullptr;
+    float* dw = nullptr;
+    cudaError_t e = cudaMallocAsync(&rad, n, st);
+    if (e != cudaSuccess) return e;
+    e = cudaMallocAsync(&dw, wts.size() * sizeof(float), st);
+    if (e != cudaSuccess) { cudaFreeAsync(rad, st); return e; }
+    cudaMemcpyAsync(dw, wts.data(), wts.size() * sizeof(float), cudaMemcpyHostToDevice, st);
+    de_radius_kernel<<<1024, 256, 0, st>>>(in, n, T, rad);
+    const int rmax = R > min_r ? R : min_r;
+    const dim3 grid((w + kDeTileX - 1) / kDeTileX, (h + kDeTileY - 1) / kDeTileY);
+    const int threads = kDeTileX * kDeTileY;
+    if (rmax <= 3) de_gather_kernel<3><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
+    else if (rmax <= 6) de_gather_kernel<6><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
+    else if (rmax <= 9) de_gather_kernel<9><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
+    else if (rmax <= kDeMaxSmemR) de_gather_kernel<kDeMaxSmemR><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
+    else de_gather_global_kernel<<<dim3((w + 127) / 128, h), 128, 0, st>>>(in, rad, w, h, dw, T, out);
+    e = cudaGetLastError();
+    cudaFreeAsync(rad, st);
+    cudaFreeAsync(dw, st);
+    return e;
+}
+
+cudaError_t launch_stats(const float4* in, uint32_t w, uint32_t h, double* out3, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(out3, 0, 3 * sizeof(double), st);
+    if (e != cudaSuccess) return e;
+    stats_kernel<<<1024, 256, 0, st>>>(in, (size_t)w * h, out3);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tonemap(const float4* in, uint32_t w, uint32_t h, uint32_t ss, float gamma, float brightness,
+                           float vibrancy, float k2, const double* stats, float4* out_f32, uchar4* out8,
+                           cudaStream_t st) {
+    const uint32_t ow = w / ss, oh = h / ss;
+    tonemap_kernel<<<dim3((ow + 127) / 128, oh), 128, 0, st>>>(in, w, h, ss, gamma, brightness, vibrancy, k2, stats,
+                                                               out_f32, out8);
+    return cudaGetLastError();
+}
+
+}  // namespace rfk

@@ -1,0 +1,54 @@
+// Launch interface of the device kernels (kernels.cu, image.cu), shared with the host runtime.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+namespace rfk {
+
+struct ChaosArgs {
+    const uint32_t* progs;   // one compiled genome per temporal sample
+    uint32_t prog_stride;    // words between copies
+    uint32_t prog_words;     // words staged per CTA
+    const float4* walk_in;   // N walkers (x, y, colour, unused)
+    float4* walk_out;
+    uint4* rng;              // N JSF32 states
+    const uint16_t* table;   // table_size permutations of the CTA's slots
+    uint32_t table_size;
+    uint32_t ppts;           // walkers per temporal sample
+    uint32_t chunks_per_ts;  // mixing domains (CTA x cluster slots) per temporal sample
+    uint32_t pass0;          // pass index of this launch's first pass
+    uint32_t steps;          // passes in this launch
+    uint64_t seed;
+    int first_run;           // pass 0 reads the start points, jitters, draws colours
+    int draw;
+    float ss[6];             // screen affine
+    uint32_t W, H;
+    float4* bins;            // RGBA sums
+    uint32_t* hits;          // counts (may be null)
+    const float4* palette;   // 256 entries
+    unsigned long long* counters;  // [0] drawn [1] emitted [2] walker-steps
+    uint8_t* trace;          // xform id per (pass, 256-group), may be null
+    uint32_t trace_passes;
+    uint32_t n_groups;
+};
+
+size_t chaos_smem(int cta, uint32_t prog_words, uint32_t steps);
+cudaError_t launch_chaos(int cta, int cluster, const ChaosArgs& a, uint32_t grid, cudaStream_t st);
+cudaError_t launch_init_rng(uint4* rng, uint64_t n, uint64_t seed, cudaStream_t st);
+cudaError_t launch_shuffle_table(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed, cudaStream_t st);
+cudaError_t launch_animate(const uint32_t* base, uint32_t words, uint32_t T, float tss, uint32_t* out,
+                           uint32_t stride, cudaStream_t st);
+cudaError_t launch_probe(const uint32_t* prog, int xform, uint32_t n, const float* in, uint32_t* rng,
+                         int first_run, float* out, cudaStream_t st);
+
+// image passes (image.cu)
+cudaError_t launch_density(const float4* in, uint32_t w, uint32_t h, int radius, int min_radius, float curve,
+                           float4* out, cudaStream_t st);
+cudaError_t launch_stats(const float4* in, uint32_t w, uint32_t h, double* out3, cudaStream_t st);
+cudaError_t launch_tonemap(const float4* in, uint32_t w, uint32_t h, uint32_t ss, float gamma, float brightness,
+                           float vibrancy, float k2, const double* stats, float4* out_f32, uchar4* out8,
+                           cudaStream_t st);
+
+}  // namespace rfk

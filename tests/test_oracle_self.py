@@ -1,0 +1,119 @@
+"""Internal consistency of the oracle (CPU): the xform-id stream predicted from RNG draw counts
+equals the one the full chaos game draws; the CUDA kernel's walker-shuffle schedule gives the
+same histogram statistics as the reference's fresh-permutation-per-pass scheme; FP32 and FP64
+agree statistically; the keyed permutations are bijections; DE and tonemap identities."""
+import numpy as np
+import pytest
+
+
+def _l1(a, b):
+    a = a / a.sum()
+    b = b / b.sum()
+    return float(np.abs(a - b).sum())
+
+
+@pytest.fixture(scope="module")
+def small_genome(rk, orc, compiler):
+    f = rk.Flame.synthesize(compiler, rk.SYNTH_SMALL, 0, 128, 128)
+    return orc.Genome(f.to_xml())
+
+
+@pytest.fixture(scope="module")
+def rich_genome(rk, orc, compiler):
+    f = rk.Flame.synthesize(compiler, rk.SYNTH_RANDOM, 7, 128, 128, n_xforms=6, final_xform=True, force_parametric=True)
+    return orc.Genome(f.to_xml())
+
+
+@pytest.mark.parametrize("T", [1, 2])
+def test_xid_stream_predicted_from_draw_counts(rich_genome, T):
+    g = rich_genome
+    r = g.chaos(4096, 64, 64, fuse=6, draw=10, seed=5, temporal_samples=T, trace=True, want_rgba=False)
+    seq = g.xid_sequence(4096, 6, 10, seed=5, temporal_samples=T)
+    assert np.array_equal(r["trace"], seq)
+    assert len(np.unique(seq)) > 1
+
+
+def test_emitted_counts_follow_xids(orc, compiler, rk):
+    # xform 1 has opacity 0: points it produces are never emitted (flame.glsl:81)
+    xml = ('<flame size="64 64" scale="16"><xform weight="0.5" color="0" color_speed="0.5" opacity="1" coefs="0.5 0 0 0.5 0.2 0" linear="1"/>'
+           '<xform weight="0.5" color="1" color_speed="0.5" opacity="0" coefs="0.5 0 0 0.5 -0.2 0" linear="1"/></flame>')
+    g = orc.Genome(xml)
+    r = g.chaos(2048, 64, 64, fuse=4, draw=12, seed=1, want_rgba=False)
+    seq = g.xid_sequence(2048, 4, 12, seed=1)
+    assert r["emitted"] == int((seq[4:] == 0).sum()) * 256
+    assert r["drawn"] <= r["emitted"] and r["drawn"] == int(r["hits"].sum())
+
+
+def _noise(runs):
+    """Mean L1 of each run to the pooled mean of the others (leave-one-out)."""
+    out = []
+    for i in range(len(runs)):
+        others = np.mean([r for j, r in enumerate(runs) if j != i], 0)
+        out.append(_l1(runs[i], others))
+    return float(np.mean(out))
+
+
+@pytest.mark.parametrize("which", ["small", "rich"])
+def test_kernel_shuffle_schedule_matches_reference_scheme(small_genome, rich_genome, which):
+    """The kernel's walker shuffle (a keyed permutation of each mixing domain every pass, a keyed
+    global gather every L passes) against the reference's fresh global permutation per pass
+    (flame.cpp:317-325): a 4096-slot domain (a 4-CTA cluster) is as noisy as the reference's
+    scheme; a single 1024-slot CTA stays within 1.5x."""
+    g = small_genome if which == "small" else rich_genome
+    kw = dict(walkers=8192, width=96, height=96, fuse=20, draw=48, want_rgba=False)
+    seeds = range(16)
+    ref = _noise([g.chaos(seed=100 + s, shuffle_mode=0, **kw)["hits"].astype(np.float64) for s in seeds])
+    d4096 = _noise([g.chaos(seed=300 + s, shuffle_mode=1, cta_slots=4096, steps_per_launch=32, table_size=256,
+                            **kw)["hits"].astype(np.float64) for s in seeds])
+    d1024 = _noise([g.chaos(seed=500 + s, shuffle_mode=1, cta_slots=1024, steps_per_launch=32, table_size=256,
+                            **kw)["hits"].astype(np.float64) for s in seeds])
+    assert d4096 <= 1.1 * ref, (d4096, ref)
+    assert d1024 <= 1.5 * ref, (d1024, ref)
+
+
+def test_fp32_matches_fp64_statistically(small_genome):
+    g = small_genome
+    kw = dict(walkers=4096, width=64, height=64, fuse=20, draw=40, want_rgba=False)
+    a = g.chaos(seed=1, fp64=True, **kw)["hits"].astype(np.float64)
+    b = g.chaos(seed=2, fp64=True, **kw)["hits"].astype(np.float64)
+    c = g.chaos(seed=3, fp64=False, **kw)["hits"].astype(np.float64)
+    assert _l1(a, c) <= 1.5 * _l1(a, b)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 256, 1000, 1024, 4097, 65536])
+def test_feistel_is_a_bijection(orc, n):
+    key = orc.derive_key(42, n, 7, 1)
+    vals = [orc.feistel(i, n, key) for i in range(n)]
+    assert sorted(vals) == list(range(n))
+
+
+def test_density_estimation_identities(orc):
+    rng = np.random.default_rng(0)
+    img = np.zeros((40, 40, 4))
+    img[10:30, 10:30] = rng.uniform(0, 50, (20, 20, 4))
+    img[..., 3] = np.where(img[..., 3] > 0, np.round(img[..., 3]) + 1, 0)
+    # radius 0 everywhere (R = 0) copies the histogram
+    assert np.array_equal(orc.density_estimate(img, 0, 0, 0.4), img)
+    # one bin of density 1 spreads over the disc with the sprite kernel of density_frag.glsl
+    for R in (1, 4, 9):
+        one = np.zeros((31, 31, 4))
+        one[15, 15] = [0.5, 0.25, 1.0, 1.0]
+        out = orc.density_estimate(one, R, 0, 0.4)
+        want = np.zeros((31, 31))
+        for dy in range(-R, R + 1):
+            for dx in range(-R, R + 1):
+                if 4 * (dx * dx + dy * dy) <= (2 * R + 1) ** 2:
+                    want[15 + dy, 15 + dx] = (1 - (dx * dx + dy * dy) / (R + 0.5) ** 2) * 0.63661977236 / R ** 2
+        assert np.allclose(out[..., 3], want, rtol=1e-12, atol=0)
+        assert np.allclose(out[..., 0], 0.5 * want, rtol=1e-12, atol=0)
+
+
+def test_tonemap_supersample_box(orc):
+    rng = np.random.default_rng(1)
+    img = rng.uniform(0, 20, (8, 8, 4))
+    img[0, 0] = 0
+    one = orc.tonemap(img, 2.2, 4.0, 1.0, 1e-2, ss=1)
+    assert np.all(one[0, 0] == [0, 0, 0, 1])
+    two = orc.tonemap(img, 2.2, 4.0, 1.0, 1e-2, ss=2)
+    assert two.shape == (4, 4, 4)
+    assert np.all((two[..., :3] >= 0) & (two[..., :3] <= 1)) and np.all(two[..., 3] == 1)
