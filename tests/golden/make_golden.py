@@ -17,6 +17,7 @@ Usage: python tests/golden/make_golden.py [reference_dir]
 import ctypes
 import json
 import os
+import re
 import sys
 
 import numpy as np
@@ -79,6 +80,17 @@ def main():
         reg.append({"name": name, "params": list((d.get("param") or {}).keys()),
                     "flags": list(d.get("flags") or [])})
     out["registry"] = reg
+    # FP32 library calls (sin, cos, pow, exp, log, atan, sqrt, ...) on each variation's path,
+    # precalcs included: the error budget of a single step is counted in these
+    common_calls = {"r": 1, "a": 1, "phi": 1, "sinr": 1, "cosr": 1}
+    pat = re.compile(r"\b(sin|cos|tan|sincos|sinhcosh|sinh|cosh|pow|exp|log|log10|atan|sqrt|length)\s*\(")
+    calls = {}
+    for name, d in lib["variations"].items():
+        d = d or {}
+        text = (d.get("src") or "") + "\n" + (d.get("result") or "")
+        used = set(re.findall(r"\$([a-z0-9_]+)", text))
+        calls[name] = len(pat.findall(text)) + sum(common_calls.get(u, 0) for u in used)
+    out["libm_calls"] = calls
     out["common"] = list(lib["common"].keys())
     with open(os.path.join(O.HERE, "_ref", "broken.txt")) as f:
         out["does_not_compile"] = [ln.strip() for ln in f if ln.strip()]
