@@ -190,6 +190,15 @@ RF_API int  rf_sim_counters(rf_sim* s, uint64_t out[3]);
    d = |offset| / (r + 0.5); r = 0 copies the bin.  R <= 100 (main.cpp:502). */
 RF_API int rf_density_estimate(const float* bins_rgba, uint32_t width, uint32_t height, int radius,
                         int min_radius, float curve, float* out_rgba, void* stream);
+/* rf_density_estimate without any device allocation (no counterpart in the reference).
+   For callers that cannot call cudaMalloc — e.g. a plug-in inside a host application that owns
+   the device memory pool, or a frame loop with a fixed memory budget that must not enter the
+   allocator.  Its scratch (bin radii, kernel weights) lives in static device arrays of the
+   library: at most 8,388,608 bins (one 3840x2160 grid); larger grids return RF_ERR_CAPACITY.
+   The first call on a device looks the arrays up (make it before any stream capture); calls
+   share the scratch, so calls that overlap on the GPU race and must be serialised. */
+RF_API int rf_density_estimate_static(const float* bins_rgba, uint32_t width, uint32_t height, int radius,
+                                      int min_radius, float curve, float* out_rgba, void* stream);
 /* FP64 statistics of the density channel: out[0] = sum of a, out[1] = max a, out[2] = bins with a > 0. */
 RF_API int rf_hist_stats(const float* rgba, uint32_t width, uint32_t height, double* out3, void* stream);
 /* Log-density tonemap (tonemap.glsl:18-38) with a box supersample filter of ss x ss bins:

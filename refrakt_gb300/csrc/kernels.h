@@ -46,6 +46,10 @@ cudaError_t launch_probe(const uint32_t* prog, int xform, uint32_t n, const floa
 // image passes (image.cu)
 cudaError_t launch_density(const float4* in, uint32_t w, uint32_t h, int radius, int min_radius, float curve,
                            float4* out, cudaStream_t st);
+size_t density_weight_count(int radius, int min_radius);
+cudaError_t launch_density_scratch(const float4* in, uint32_t w, uint32_t h, int radius, int min_radius, float curve,
+                                   float4* out, uint8_t* radius_scratch, float* weight_scratch,
+                                   size_t weight_capacity, cudaStream_t st);
 cudaError_t launch_stats(const float4* in, uint32_t w, uint32_t h, double* out3, cudaStream_t st);
 cudaError_t launch_tonemap(const float4* in, uint32_t w, uint32_t h, uint32_t ss, float gamma, float brightness,
                            float vibrancy, float k2, const double* stats, float4* out_f32, uchar4* out8,
