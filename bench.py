@@ -26,13 +26,44 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-W_OUT, H_OUT, SS = 1920, 1080, 2
-W, H = W_OUT * SS, H_OUT * SS
-POINTS = 1000 * W * H  # 8,294,400,000
+# Workloads.  The default (`frame1080`) is the headline: the full-quality 1080p frame.  The
+# others are the small CPU-runnable genome and the two atomic-contention / histogram-size stress
+# genomes, measured the same way (chaos game only where no image is asked for).
+WORKLOADS = {
+    "frame1080": dict(name="plain 1080p frame, supersample 2 (3840x2160 bins), 1000 points/bin, DE r9 c0.4",
+                      genome=dict(kind=1, seed=1, n_xforms=8, final_xform=True, force_parametric=True),
+                      out=(1920, 1080), ss=2, points=1000 * 3840 * 2160, de=(9, 0, 0.4), image=True),
+    "small": dict(name="small genome (seed 0, 3 xforms), 512x512 bins, 65,536 walkers x 256 passes",
+                  genome=dict(kind=0, seed=0, n_xforms=0, final_xform=False, force_parametric=False),
+                  out=(512, 512), ss=1, points=65536 * 256, de=None, image=True, walkers=65536),
+    "contract": dict(name="contracting genome (seed 4, 6 xforms), 1920x1080 bins, 2^34 points",
+                     genome=dict(kind=2, seed=4, n_xforms=0, final_xform=False, force_parametric=False),
+                     out=(1920, 1080), ss=1, points=2 ** 34, de=None, image=False),
+    "spacefill": dict(name="space-filling genome (seed 5, 16 xforms), 8192x8192 bins, 2^34 points",
+                      genome=dict(kind=3, seed=5, n_xforms=0, final_xform=False, force_parametric=False),
+                      out=(4096, 4096), ss=2, points=2 ** 34, de=None, image=False),
+}
 FUSE = 20
-DE = (9, 0, 0.4)
-GENOME = dict(kind=1, seed=1, n_xforms=8, final_xform=True, force_parametric=True)
-CONFIG_NAME = "plain 1080p frame, supersample 2 (3840x2160 bins), 1000 points/bin, DE r9 c0.4"
+WL = WORKLOADS["frame1080"]
+W_OUT, H_OUT = WL["out"]
+SS = WL["ss"]
+W, H = W_OUT * SS, H_OUT * SS
+POINTS = WL["points"]
+DE = WL["de"]
+GENOME = WL["genome"]
+CONFIG_NAME = WL["name"]
+
+
+def select_workload(key):
+    global WL, W_OUT, H_OUT, SS, W, H, POINTS, DE, GENOME, CONFIG_NAME
+    WL = WORKLOADS[key]
+    W_OUT, H_OUT = WL["out"]
+    SS = WL["ss"]
+    W, H = W_OUT * SS, H_OUT * SS
+    POINTS = WL["points"]
+    DE = WL["de"]
+    GENOME = WL["genome"]
+    CONFIG_NAME = WL["name"]
 
 
 def _dist():
@@ -94,6 +125,25 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def slowest_rank_ms(ms):
+    """Max of a per-rank duration over all ranks (identity without torch.distributed)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(ms)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(points_per_rank, ms_per_step):
+    """Whole-job Gpoints/s of independent replicas: every rank's points over the slowest rank's time."""
+    import torch.distributed as dist
+    ws = dist.get_world_size() if (dist.is_available() and dist.is_initialized()) else 1
+    return points_per_rank * ws / (slowest_rank_ms(ms_per_step) * 1e-3) / 1e9
 
 
 def _peaks():
@@ -179,19 +229,25 @@ def run_native(args):
     xml = flame.to_xml()
     info = flame.info()
     sms = torch.cuda.get_device_properties(local).multi_processor_count
-    cta = args.cta
-    walkers = sms * args.ctas_per_sm * cta
-    sim = R.Sim(walkers, cta_slots=cta, steps_per_launch=args.steps_per_launch, seed=1000 + rank, device=local)
+    cta = args.cta_slots
+    walkers = WL.get("walkers") or sms * args.ctas_per_sm * cta
+    sim = R.Sim(walkers, cta_slots=cta, cta_threads=args.cta_threads, steps_per_launch=args.steps_per_launch,
+                seed=1000 + rank, device=local)
     passes = (POINTS + walkers - 1) // walkers
     launches = (passes + args.steps_per_launch - 1) // args.steps_per_launch
     bins = torch.zeros(H, W, 4, device="cuda")
     hits = torch.zeros(H, W, dtype=torch.int32, device="cuda")
-    de = torch.zeros_like(bins)
+    de = torch.zeros_like(bins) if DE else None
     img = torch.zeros(H_OUT, W_OUT, 4, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
     sim.set_stream(stream)
 
+    # bins smaller than the 129 MB L2: write a 256 MB buffer before every frame
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda") if W * H * 20 <= 129e6 else None
+
     def frame(ev=None):
+        if flush is not None:
+            flush.zero_()
         sim.warmup(flame, FUSE - 1)
         bins.zero_()
         hits.zero_()
@@ -200,8 +256,13 @@ def run_native(args):
         sim.draw_to_bins(flame, bins, hits, W, H, passes, sync=False)
         if ev:
             ev[1].record(stream)
-        R.density_estimate(bins, W, H, DE[0], DE[1], DE[2], de, stream=stream)
-        R.tonemap(de, W, H, SS, info["gamma"], info["brightness"], info["vibrancy"], 0.0, None, img, stream=stream)
+        if not WL["image"]:
+            return
+        src = bins
+        if DE:
+            R.density_estimate(bins, W, H, DE[0], DE[1], DE[2], de, stream=stream)
+            src = de
+        R.tonemap(src, W, H, SS, info["gamma"], info["brightness"], info["vibrancy"], 0.0, None, img, stream=stream)
 
     def barrier():
         if ws > 1:
@@ -223,12 +284,8 @@ def run_native(args):
         barrier()
     ms = t0.elapsed_time(t1)
     draw_ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_step = ms / args.steps
-    value = POINTS * ws / (ms_step * 1e-3) / 1e9
+    ms_step = slowest_rank_ms(ms / args.steps)
+    value = replica_throughput(POINTS, ms / args.steps)
 
     # end to end through the C ABI: host genome in, pinned host image out
     out = torch.empty(H_OUT, W_OUT, 4, dtype=torch.uint8, pin_memory=True)
@@ -238,16 +295,13 @@ def run_native(args):
         barrier()
         t_a = time.perf_counter()
         f2 = R.Flame.from_xml(xml, comp)
-        _, st = sim.render(f2, W_OUT, H_OUT, POINTS, supersample=SS, fuse_passes=FUSE, out=out_np)
+        _, st = sim.render(f2, W_OUT, H_OUT, POINTS, supersample=SS, fuse_passes=FUSE, out=out_np,
+                           density_estimation=DE is not None)
         barrier()
         if i >= args.warmup:
             e2e_ms.append((time.perf_counter() - t_a) * 1e3)
-    e2e_step = statistics.median(e2e_ms)
-    if ws > 1:
-        t = torch.tensor([e2e_step], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_step = float(t.item())
-    e2e_value = POINTS * ws / (e2e_step * 1e-3) / 1e9
+    e2e_step = slowest_rank_ms(statistics.median(e2e_ms))
+    e2e_value = replica_throughput(POINTS, statistics.median(e2e_ms))
     prog_bytes = info["total_params"] * 4  # order of the uploaded genome
     h2d = prog_bytes + 256 * 16
     d2h = W_OUT * H_OUT * 4
@@ -264,8 +318,10 @@ def run_native(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic genome (seed 1); no dataset",
         "config": {"workload": CONFIG_NAME, "points_per_frame": POINTS, "bins": [W, H], "output": [W_OUT, H_OUT],
                    "genome": GENOME, "walkers": walkers, "cta_slots": cta, "steps_per_launch": args.steps_per_launch,
-                   "passes_per_frame": passes, "fuse_passes": FUSE, "density_estimation": list(DE),
-                   "l2": "bins (3840x2160x20 B = 166 MB) exceed the 129 MB L2", "parallelism": "replicas" if ws > 1 else "single"},
+                   "passes_per_frame": passes, "fuse_passes": FUSE, "density_estimation": list(DE) if DE else None,
+                   "l2": "bins %dx%d x 20 B = %.0f MB (L2 129 MB)%s" % (W, H, W * H * 20 / 1e6,
+                         "; exceed L2" if W * H * 20 > 129e6 else "; an L2 flush separates frames"),
+                   "parallelism": "replicas" if ws > 1 else "single"},
         "s_per_frame": ms_step / 1e3,
         "draw_ms_per_frame": draw_ms,
         "gpu_launches": (launches + (FUSE + args.steps_per_launch - 1) // args.steps_per_launch + 4) * args.steps,
@@ -280,7 +336,7 @@ def run_native(args):
         "clocks": clk.summary(),
     }
     if rank == 0:
-        if ws == 1 and not args.no_cpu_baseline:
+        if ws == 1 and not args.no_cpu_baseline and args.workload == "frame1080":
             v, thr, sample, _ = cpu_baseline(xml)
             line["cpu_baseline"] = {"value": v, "unit": "Gpoints/s", "cores": thr, "kind": "port", "sample": sample}
         print(json.dumps(line))
@@ -296,11 +352,14 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--cta", type=int, default=1024)
-    ap.add_argument("--ctas-per-sm", type=int, default=16)
+    ap.add_argument("--cta-slots", type=int, default=4096)
+    ap.add_argument("--cta-threads", type=int, default=0)
+    ap.add_argument("--ctas-per-sm", type=int, default=4)
     ap.add_argument("--steps-per-launch", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="frame1080", choices=sorted(WORKLOADS))
     args = ap.parse_args()
+    select_workload(args.workload)
     if args.impl == "reference":
         return run_reference(args)
     return run_native(args)

@@ -140,14 +140,14 @@ RF_API int  rf_flame_xform_draws(const rf_flame* f, int xform);
  * ---------------------------------------------------------------------------------------- */
 
 typedef struct {
-    uint64_t walkers;           /* total walker slots N (multiple of the shuffle domain * temporal_samples) */
+    uint64_t walkers;           /* total walker slots N (multiple of cta_slots * temporal_samples) */
     uint32_t temporal_samples;  /* T (flame.cpp:109) */
     uint32_t shuffle_count;     /* permutations in the walker-shuffle table (flame.cpp:110) */
     uint64_t seed;              /* slot i's JSF32 state = warmup_ctx(i + seed * N) */
-    uint32_t cta_slots;         /* walkers per CTA: 256, 512 or 1024 (0 = 1024) */
-    uint32_t cluster_ctas;      /* CTAs per thread-block cluster sharing one walker shuffle
-                                   through distributed shared memory: 1, 2, 4 (or 8 with 512-slot
-                                   CTAs); 0 = 1.  The shuffle domain is cta_slots * cluster_ctas. */
+    uint32_t cta_slots;         /* walker slots per CTA — the walker shuffle's mixing domain:
+                                   256, 512, 1024, 2048 or 4096 (0 = 4096) */
+    uint32_t cta_threads;       /* threads per CTA: 256, 512 or 1024, dividing cta_slots
+                                   (0 = min(cta_slots, 1024)) */
     uint32_t steps_per_launch;  /* passes per persistent launch L (0 = 32; 1 = the reference's
                                    per-pass global gather) */
     int32_t  device;            /* CUDA device ordinal */

@@ -53,7 +53,7 @@ class FlameInfo(ctypes.Structure):
 class SimDesc(ctypes.Structure):
     _fields_ = [("walkers", ctypes.c_uint64), ("temporal_samples", ctypes.c_uint32),
                 ("shuffle_count", ctypes.c_uint32), ("seed", ctypes.c_uint64), ("cta_slots", ctypes.c_uint32),
-                ("cluster_ctas", ctypes.c_uint32), ("steps_per_launch", ctypes.c_uint32), ("device", ctypes.c_int32)]
+                ("cta_threads", ctypes.c_uint32), ("steps_per_launch", ctypes.c_uint32), ("device", ctypes.c_int32)]
 
 
 class RenderDesc(ctypes.Structure):
@@ -303,9 +303,9 @@ class Sim:
     """Walker slots, RNG states and the shuffle table — ``flame::set_sim_parameters`` plus the
     per-flame ``warmup`` / ``draw_to_bins`` (src/flame.cpp:105-330)."""
 
-    def __init__(self, walkers, temporal_samples=1, shuffle_count=1024, seed=0, cta_slots=1024, cluster_ctas=1,
+    def __init__(self, walkers, temporal_samples=1, shuffle_count=1024, seed=0, cta_slots=4096, cta_threads=0,
                  steps_per_launch=32, device=0):
-        d = SimDesc(walkers, temporal_samples, shuffle_count, seed, cta_slots, cluster_ctas, steps_per_launch, device)
+        d = SimDesc(walkers, temporal_samples, shuffle_count, seed, cta_slots, cta_threads, steps_per_launch, device)
         h = ctypes.c_void_p()
         _check(library().rf_sim_create(ctypes.byref(d), ctypes.byref(h)))
         self._h = h

@@ -55,7 +55,7 @@ struct rf_sim {
     int device = 0;
     cudaStream_t stream = nullptr;
     uint64_t N = 0;
-    uint32_t T = 1, ppts = 0, cta = 1024, cluster = 1, L = 32, table_size = 1024;
+    uint32_t T = 1, ppts = 0, slots = 4096, threads = 1024, L = 32, table_size = 1024;
     float4* walk[2] = {nullptr, nullptr};
     int cur = 0;
     uint4* rng = nullptr;
@@ -112,7 +112,7 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.table = s->table;
         a.table_size = s->table_size;
         a.ppts = s->ppts;
-        a.chunks_per_ts = s->ppts / (s->cta * s->cluster);
+        a.chunks_per_ts = s->ppts / s->slots;
         a.pass0 = s->pass;
         a.steps = steps;
         a.seed = s->d.seed;
@@ -128,8 +128,8 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.trace = s->trace;
         a.trace_passes = s->trace_passes;
         a.n_groups = (uint32_t)(s->N / kGroup);
-        const uint32_t grid = (uint32_t)(s->N / s->cta);
-        cudaError_t e = launch_chaos((int)s->cta, (int)s->cluster, a, grid, s->stream);
+        const uint32_t grid = (uint32_t)(s->N / s->slots);
+        cudaError_t e = launch_chaos((int)s->threads, (int)s->slots, a, grid, s->stream);
         if (e != cudaSuccess) return cuda_fail(e, "chaos kernel launch");
         s->cur ^= 1;
         s->pass += steps;
@@ -339,17 +339,15 @@ int rf_flame_xform_draws(const rf_flame* f, int xi) {
 int rf_sim_create(const rf_sim_desc* d, rf_sim** out) {
     if (!d || !out) return fail(RF_ERR_INVALID_ARG, "rf_sim_create: null argument");
     *out = nullptr;
-    const uint32_t cta = d->cta_slots ? d->cta_slots : 1024;
+    const uint32_t slots = d->cta_slots ? d->cta_slots : 4096;
+    const uint32_t threads = d->cta_threads ? d->cta_threads : std::min<uint32_t>(slots, 1024);
     const uint32_t T = d->temporal_samples ? d->temporal_samples : 1;
-    const uint32_t cluster = d->cluster_ctas ? d->cluster_ctas : 1;
-    if (cta != 256 && cta != 512 && cta != 1024) return fail(RF_ERR_INVALID_ARG, "cta_slots must be 256, 512 or 1024");
-    const bool ok_cluster = cluster == 1 || (cluster == 2 && cta >= 512) || (cluster == 4 && cta >= 512) ||
-                            (cluster == 8 && cta == 512);
-    if (!ok_cluster) return fail(RF_ERR_INVALID_ARG, "cluster_ctas must be 1, 2 or 4 (8 with 512-slot CTAs)");
-    const uint32_t domain = cta * cluster;
+    if (!chaos_shape_supported((int)threads, (int)slots))
+        return fail(RF_ERR_INVALID_ARG, "cta_slots / cta_threads: 256x256, 512x512, 1024 or 2048 slots on 512 threads, "
+                                        "1024, 2048 or 4096 slots on 1024 threads");
     if (d->walkers == 0 || d->walkers % T) return fail(RF_ERR_INVALID_ARG, "walkers must be a positive multiple of temporal_samples");
     const uint64_t ppts = d->walkers / T;
-    if (ppts % domain) return fail(RF_ERR_INVALID_ARG, "walkers per temporal sample must be a multiple of cta_slots * cluster_ctas");
+    if (ppts % slots) return fail(RF_ERR_INVALID_ARG, "walkers per temporal sample must be a multiple of cta_slots");
     if (ppts > 0x7fffffffull) return fail(RF_ERR_CAPACITY, "too many walkers per temporal sample");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(RF_ERR_NO_DEVICE, "no CUDA device");
@@ -360,8 +358,8 @@ int rf_sim_create(const rf_sim_desc* d, rf_sim** out) {
     s->N = d->walkers;
     s->T = T;
     s->ppts = (uint32_t)ppts;
-    s->cta = cta;
-    s->cluster = cluster;
+    s->slots = slots;
+    s->threads = threads;
     s->L = d->steps_per_launch ? std::min<uint32_t>(d->steps_per_launch, 256) : 32;
     s->table_size = d->shuffle_count ? d->shuffle_count : 1024;
     auto cleanup = [&](int rc) { rf_sim_destroy(s); return rc; };
@@ -372,7 +370,7 @@ int rf_sim_create(const rf_sim_desc* d, rf_sim** out) {
     ALLOC(s->walk[0], s->N * sizeof(float4));
     ALLOC(s->walk[1], s->N * sizeof(float4));
     ALLOC(s->rng, s->N * sizeof(uint4));
-    ALLOC(s->table, (size_t)s->table_size * domain * sizeof(uint16_t));
+    ALLOC(s->table, (size_t)s->table_size * slots * sizeof(uint16_t));
     ALLOC(s->base_prog, kProgMaxWords * sizeof(uint32_t));
     s->prog_stride = kProgMaxWords;
     ALLOC(s->progs, (size_t)T * s->prog_stride * sizeof(uint32_t));
@@ -380,7 +378,7 @@ int rf_sim_create(const rf_sim_desc* d, rf_sim** out) {
     ALLOC(s->counters, 8 * sizeof(unsigned long long));
 #undef ALLOC
     if ((e = launch_init_rng(s->rng, s->N, d->seed, s->stream)) != cudaSuccess) return cleanup(cuda_fail(e, "rng init"));
-    if ((e = launch_shuffle_table(s->table, domain, s->table_size, d->seed, s->stream)) != cudaSuccess)
+    if ((e = launch_shuffle_table(s->table, slots, s->table_size, d->seed, s->stream)) != cudaSuccess)
         return cleanup(cuda_fail(e, "shuffle table"));
     if ((e = cudaMemsetAsync(s->counters, 0, 8 * sizeof(unsigned long long), s->stream)) != cudaSuccess)
         return cleanup(cuda_fail(e, "memset"));

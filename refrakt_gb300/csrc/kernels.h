@@ -14,10 +14,10 @@ struct ChaosArgs {
     const float4* walk_in;   // N walkers (x, y, colour, unused)
     float4* walk_out;
     uint4* rng;              // N JSF32 states
-    const uint16_t* table;   // table_size permutations of the CTA's slots
+    const uint16_t* table;   // table_size permutations of a CTA's slots (the mixing domain)
     uint32_t table_size;
     uint32_t ppts;           // walkers per temporal sample
-    uint32_t chunks_per_ts;  // mixing domains (CTA x cluster slots) per temporal sample
+    uint32_t chunks_per_ts;  // CTAs (mixing domains) per temporal sample
     uint32_t pass0;          // pass index of this launch's first pass
     uint32_t steps;          // passes in this launch
     uint64_t seed;
@@ -34,8 +34,9 @@ struct ChaosArgs {
     uint32_t n_groups;
 };
 
-size_t chaos_smem(int cta, uint32_t prog_words, uint32_t steps);
-cudaError_t launch_chaos(int cta, int cluster, const ChaosArgs& a, uint32_t grid, cudaStream_t st);
+size_t chaos_smem(int slots, uint32_t prog_words, uint32_t steps);
+bool chaos_shape_supported(int threads, int slots);
+cudaError_t launch_chaos(int threads, int slots, const ChaosArgs& a, uint32_t grid, cudaStream_t st);
 cudaError_t launch_init_rng(uint4* rng, uint64_t n, uint64_t seed, cudaStream_t st);
 cudaError_t launch_shuffle_table(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed, cudaStream_t st);
 cudaError_t launch_animate(const uint32_t* base, uint32_t words, uint32_t T, float tss, uint32_t* out,

@@ -79,7 +79,7 @@ LINEAR = ('<flame size="256 256" scale="64" center="0 0"><xform weight="0.5" col
           + "</flame>")
 
 
-@pytest.mark.parametrize("cta,L", [(1024, 16), (512, 5), (1024, 1)])
+@pytest.mark.parametrize("cta,L", [(4096, 32), (2048, 7), (1024, 16), (512, 5), (1024, 1)])
 def test_linear_genome_histogram_bit_exact(rk, orc, compiler, cta, L):
     """Affine-only genome: every operation is an explicit FP32 fma/mul/add, so the CUDA kernel and
     the FP32 oracle on the same shuffle schedule produce the same walkers and the same counts."""
