@@ -42,6 +42,10 @@ WORKLOADS = {
     "spacefill": dict(name="space-filling genome (seed 5, 16 xforms), 8192x8192 bins, 2^34 points",
                       genome=dict(kind=3, seed=5, n_xforms=0, final_xform=False, force_parametric=False),
                       out=(4096, 4096), ss=2, points=2 ** 34, de=None, image=False),
+    "batch": dict(name="batched animation: 120 frames interpolated seed 2 (4 xforms) -> seed 3 (10 xforms) at "
+                       "1024x768 + 64 random genomes (2-16 xforms) at 512x512 / 1024x768 / 1920x1080, 200 spp, "
+                       "one persistent graph-captured launch",
+                  genome=None, out=(1024, 768), ss=1, points=None, de=(9, 0, 0.4), image=True),
 }
 FUSE = 20
 WL = WORKLOADS["frame1080"]
@@ -191,8 +195,13 @@ def run_reference(args):
     import refrakt_gb300 as R
     R.build()
     comp = R.FlameCompiler()
-    xml = R.Flame.synthesize(comp, GENOME["kind"], GENOME["seed"], W, H, n_xforms=GENOME["n_xforms"],
-                             final_xform=GENOME["final_xform"], force_parametric=GENOME["force_parametric"]).to_xml()
+    if GENOME is None:  # batched workload: the first animation frame stands for the batch
+        xml = batch_items(R, comp)[0][0].to_xml()
+    else:
+        xml = R.Flame.synthesize(comp, GENOME["kind"], GENOME["seed"], W, H, n_xforms=GENOME["n_xforms"],
+                                 final_xform=GENOME["final_xform"],
+                                 force_parametric=GENOME["force_parametric"]).to_xml()
+    points = POINTS or 200 * 1024 * 768
     vals = []
     last = None
     for i in range(args.warmup + args.steps):
@@ -202,10 +211,10 @@ def run_reference(args):
         last = (thr, sample)
     v = statistics.median(vals)
     line = {"metric": "Gpoints/s histogrammed", "value": v, "unit": "Gpoints/s", "impl": "reference",
-            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": POINTS / (v * 1e9) * 1e3,
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": points / (v * 1e9) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic genome (seed 1), no dataset",
-            "config": {"workload": CONFIG_NAME, "points_per_frame": POINTS, "bins": [W, H], "genome": GENOME},
+            "config": {"workload": CONFIG_NAME, "points_per_frame": points, "bins": [W, H], "genome": GENOME},
             "cpu_baseline": {"value": v, "unit": "Gpoints/s", "cores": last[0], "kind": "port", "sample": last[1]},
             "e2e": {"value": v, "unit": "Gpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -346,6 +355,110 @@ def run_native(args):
     return 0
 
 
+def batch_items(R, comp):
+    """The batched-animation workload: (flame, width, height, points, seed) tuples."""
+    a = R.Flame.synthesize(comp, R.SYNTH_RANDOM, 2, 1024, 768, n_xforms=4)
+    b = R.Flame.synthesize(comp, R.SYNTH_RANDOM, 3, 1024, 768, n_xforms=10)
+    items = []
+    for k in range(120):
+        f = a.interpolate(b, k / 119.0)
+        items.append((f, 1024, 768, 200 * 1024 * 768, 7))  # one seed: coherent frames
+    sizes = [(512, 512), (1024, 768), (1920, 1080)]
+    for k in range(64):
+        w, h = sizes[k % 3]
+        f = R.Flame.synthesize(comp, R.SYNTH_RANDOM, 100 + k, w, h, n_xforms=2 + k % 15)
+        items.append((f, w, h, 200 * w * h, 100 + k))
+    return items
+
+
+def run_batch(args):
+    import torch
+    import refrakt_gb300 as R
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    R.build()
+    comp = R.FlameCompiler()
+    items = batch_items(R, comp)
+    for f, *_ in items:
+        f.set_estimator(*DE)
+    points = sum(it[3] for it in items)
+    n_img = len(items)
+    b = R.Batch(items, fuse_passes=FUSE, density_estimation=True, device=local)
+    info = b.info()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        b.run()
+        b.sync()
+    barrier()
+    dev_ms = []
+    with ClockSampler(local) as clk:
+        barrier()
+        t_a = time.perf_counter()
+        for _ in range(args.steps):
+            b.run()
+            dev_ms.append(b.sync()["ms"])  # events around the graph launch on the batch's stream
+        barrier()
+        wall = (time.perf_counter() - t_a) * 1e3
+    st = b.sync()
+    ms = sum(dev_ms) / args.steps
+    ms_step = slowest_rank_ms(ms)
+    value = replica_throughput(st["points"], ms)
+
+    # end to end through the public API: genomes from host XML, create (compile, upload, autotune,
+    # capture), run, every image back to pinned host memory, destroy
+    xmls = [(it[0].to_xml(),) + tuple(it[1:]) for it in items]
+    outs = [torch.empty(h, w, 4, dtype=torch.uint8, pin_memory=True).numpy() for _, w, h, *_ in xmls]
+    e2e_ms = []
+    for i in range(max(1, args.warmup // 3) + args.steps):
+        barrier()
+        t_a = time.perf_counter()
+        fl = [(R.Flame.from_xml(x, comp), w, h, p, s) for x, w, h, p, s in xmls]
+        bb = R.Batch(fl, fuse_passes=FUSE, density_estimation=True, device=local)
+        bb.run()
+        for k in range(n_img):
+            bb.image(k, outs[k])
+        bb.close()
+        barrier()
+        if i >= max(1, args.warmup // 3):
+            e2e_ms.append((time.perf_counter() - t_a) * 1e3)
+    e2e_step = slowest_rank_ms(statistics.median(e2e_ms))
+    d2h = sum(w * h * 4 for _, w, h, *_ in xmls)
+    h2d = sum(it[0].info()["total_params"] * 4 + 256 * 16 for it in items)
+    line = {
+        "metric": "Gpoints/s histogrammed", "value": value, "unit": "Gpoints/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic genomes (seeds 2, 3, 100-163); no dataset",
+        "config": {"workload": CONFIG_NAME, "images": n_img, "points_per_batch": st["points"],
+                   "requested_points": points, "density_estimation": list(DE), "fuse_passes": FUSE,
+                   "autotuned": info, "l2": "%.1f GB of bins per batch (L2 129 MB)" %
+                   (sum(w * h * 20 for _, w, h, *_ in items) / 1e9),
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "frames_per_s": n_img / (ms_step * 1e-3),
+        "binned_fraction": st["binned"] / st["points"],
+        "wall_ms_per_step": wall / args.steps,
+        "gpu_launches": (1 + sum(5 for _ in items)) * args.steps,
+        "e2e": {"value": replica_throughput(st["points"], statistics.median(e2e_ms)), "unit": "Gpoints/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "frames_per_s": n_img / (e2e_step * 1e-3),
+                "includes": "genome parse + compile + upload + autotune + graph capture + run + image readback"},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    b.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -362,6 +475,8 @@ def main():
     select_workload(args.workload)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
     return run_native(args)
 
 

@@ -107,6 +107,12 @@ typedef struct {
 } rf_synth_desc;
 RF_API int  rf_flame_synthesize(const rf_synth_desc* d, const rf_compiler* c, rf_flame** out);
 
+/* Genome at t in [0, 1] between a and b (animation frames; the reference only rotates affines
+   over time, main.cpp:383-395).  The shorter genome's missing xforms are padded with zero
+   selection weight; affines, post, weights, colours, variation weights (0 where absent) and shared
+   parameters are lerped. */
+RF_API int  rf_flame_interpolate(const rf_flame* a, const rf_flame* b, float t, rf_flame** out);
+
 typedef struct {
     uint32_t size[2];           /* flame.hpp:47 */
     float    center[2];
@@ -237,6 +243,55 @@ typedef struct {
 /* Renders `f` into out_rgba8 (host memory, width*height*4 bytes).  stats (may be NULL):
    [0] points computed, [1] points binned, [2] milliseconds on the device. */
 RF_API int rf_render(rf_sim* s, rf_flame* f, const rf_render_desc* d, uint8_t* out_rgba8, double* stats);
+
+/* ------------------------------------------------------------------------------------------
+ * Batched rendering.  No counterpart in the reference, which renders one genome per call
+ * (flame.cpp:146 draw_to_bins); this draws many genomes — animation frames, independent
+ * genomes with different xform counts and bin grids — in one persistent launch pulling work
+ * units from a queue, then runs each genome's density estimation and tonemap.  A work unit is a
+ * self-contained chaos game of `cta_slots` walkers of one genome (own seeds, start points,
+ * fuse passes, walker shuffle) run inside one CTA.  The sequence is captured once in a CUDA
+ * graph (use_graph) and replayed by rf_batch_run.
+ *
+ * Unit u of an item is the reference's chaos game of one temporal sample of cta_slots walkers
+ * seeded with s = item.seed + u * 0x9E3779B97F4A7C15 (slot i: warmup_ctx(i + s * cta_slots),
+ * flame.cpp:138-141), fuse_passes discarded passes then its drawing passes; after the first pass
+ * walkers are exchanged through one of 1024 shared permutations of the unit (keyed by
+ * 0x5EED + cta_slots) and, at the first drawing pass, through a keyed permutation of the unit.
+ * Items with equal seeds share their walkers' random streams (coherent animation frames).
+ * ---------------------------------------------------------------------------------------- */
+typedef struct rf_batch rf_batch;
+typedef struct {
+    const rf_flame* flame;      /* compiled genome; read at rf_batch_create only */
+    uint32_t width, height;     /* output image size */
+    uint32_t supersample;       /* bins = (width*ss) x (height*ss); 0 = 1 */
+    uint64_t points;            /* points to draw (rounded up to whole unit passes) */
+    uint64_t seed;              /* seeds of the genome's walkers and shuffles */
+} rf_batch_item;
+typedef struct {
+    uint32_t fuse_passes;       /* discarded passes at the start of every unit; 0 = 20 */
+    uint32_t cta_slots;         /* walkers per unit (1024, 2048, 4096); 0 = autotune */
+    uint32_t unit_passes;       /* drawing passes per unit; 0 = autotune */
+    int32_t  density_estimation;/* 1: adaptive DE with each genome's estimator fields */
+    float    k2;                /* tonemap k2 (<= 0: automatic per genome) */
+    int32_t  use_graph;         /* 1: capture the whole batch in a CUDA graph */
+    int32_t  device;
+} rf_batch_desc;
+RF_API int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc* d, rf_batch** out);
+/* Enqueues one whole batch (clear, draw, DE, tonemap) on the batch's own stream. */
+RF_API int rf_batch_run(rf_batch* b);
+/* Waits for the last run.  stats (may be NULL, 4 doubles): [0] points computed, [1] points
+   binned, [2] milliseconds on the device, [3] walker-steps including fuse passes. */
+RF_API int rf_batch_sync(rf_batch* b, double* stats);
+/* Copies item i's image (width*height*4 bytes) to host memory. */
+RF_API int rf_batch_image(rf_batch* b, uint32_t i, uint8_t* out_rgba8);
+/* Device pointers of item i's bins (float4 RGBA sums, u32 hits) and the bin grid size. */
+RF_API int rf_batch_bins(rf_batch* b, uint32_t i, float** rgba, uint32_t** hits, uint32_t* width, uint32_t* height);
+/* Copies item i's bins to host memory (either pointer may be NULL). */
+RF_API int rf_batch_read_bins(rf_batch* b, uint32_t i, float* host_rgba, uint32_t* host_hits);
+/* The autotuned shape: walkers per unit, number of units, drawing passes per unit. */
+RF_API int rf_batch_info(const rf_batch* b, uint32_t* cta_slots, uint32_t* units, uint32_t* unit_passes);
+RF_API int rf_batch_destroy(rf_batch* b);
 
 /* Writes an RGBA8 image as an uncompressed PNG. */
 RF_API int rf_write_png(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height);

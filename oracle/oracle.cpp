@@ -838,7 +838,7 @@ int chaos(const orc_genome* g, const orc_chaos_cfg* cfg, double* rgba, uint64_t*
     if (cfg->shuffle_mode == 1) {
         table.assign(cfg->table_size, std::vector<uint32_t>(cs_));
         for (uint32_t k = 0; k < cfg->table_size; k++) {
-            uint64_t key = derive_key(cfg->seed, k, 0, TAG_TABLE);
+            uint64_t key = derive_key(cfg->table_seed_set ? cfg->table_seed : cfg->seed, k, 0, TAG_TABLE);
             for (uint32_t j = 0; j < cs_; j++) table[k][j] = feistel(j, cs_, key);
         }
     }

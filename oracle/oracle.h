@@ -74,6 +74,8 @@ typedef struct {
     uint32_t table_size;       /* shuffle_mode 1: permutations in the local table */
     float    tss_width;        /* temporal sample width (animate.tpl.glsl) */
     int      threads;          /* worker threads (>=1) */
+    int      table_seed_set;   /* shuffle_mode 1: 1 = the local table is keyed by table_seed, */
+    uint64_t table_seed;       /*   0 = by seed (the batched launch shares one table) */
 } orc_chaos_cfg;
 
 /* rgba: W*H*4 doubles (may be NULL), hits: W*H u64 (may be NULL),

@@ -44,7 +44,7 @@ class ChaosCfg(ctypes.Structure):
                 ("height", ctypes.c_uint32), ("fp64", ctypes.c_int), ("shuffle_mode", ctypes.c_int),
                 ("cta_slots", ctypes.c_uint32), ("steps_per_launch", ctypes.c_uint32),
                 ("table_size", ctypes.c_uint32), ("tss_width", ctypes.c_float),
-                ("threads", ctypes.c_int)]
+                ("threads", ctypes.c_int), ("table_seed_set", ctypes.c_int), ("table_seed", ctypes.c_uint64)]
 
 
 def lib():
@@ -206,9 +206,10 @@ class Genome:
 
     def chaos(self, walkers, width, height, fuse=20, draw=16, seed=0, temporal_samples=1, fp64=True,
               shuffle_mode=0, cta_slots=1024, steps_per_launch=32, table_size=1024, tss_width=0.02,
-              trace=False, want_rgba=True):
+              trace=False, want_rgba=True, table_seed=None):
         cfg = ChaosCfg(walkers, temporal_samples, seed, fuse, draw, width, height, int(fp64), shuffle_mode,
-                       cta_slots, steps_per_launch, table_size, tss_width, 1)
+                       cta_slots, steps_per_launch, table_size, tss_width, 1, int(table_seed is not None),
+                       table_seed or 0)
         rgba = np.zeros((height, width, 4), np.float64) if want_rgba else None
         hits = np.zeros((height, width), np.uint64)
         tr = np.zeros((fuse + draw, walkers // 256), np.uint8) if trace else None

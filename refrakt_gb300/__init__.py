@@ -62,6 +62,17 @@ class RenderDesc(ctypes.Structure):
                 ("k2", ctypes.c_float), ("density_estimation", ctypes.c_int32)]
 
 
+class BatchItem(ctypes.Structure):
+    _fields_ = [("flame", ctypes.c_void_p), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("supersample", ctypes.c_uint32), ("points", ctypes.c_uint64), ("seed", ctypes.c_uint64)]
+
+
+class BatchDesc(ctypes.Structure):
+    _fields_ = [("fuse_passes", ctypes.c_uint32), ("cta_slots", ctypes.c_uint32), ("unit_passes", ctypes.c_uint32),
+                ("density_estimation", ctypes.c_int32), ("k2", ctypes.c_float), ("use_graph", ctypes.c_int32),
+                ("device", ctypes.c_int32)]
+
+
 _lib = None
 
 _SIGS = {
@@ -83,6 +94,7 @@ _SIGS = {
     "rf_flame_to_xml": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "rf_flame_synthesize": ([ctypes.POINTER(SynthDesc), ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "rf_flame_get_info": ([ctypes.c_void_p, ctypes.POINTER(FlameInfo)], ctypes.c_int),
+    "rf_flame_interpolate": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "rf_flame_set_view": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_float, ctypes.c_float], ctypes.c_int),
     "rf_flame_set_tonemap": ([ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_float], ctypes.c_int),
     "rf_flame_set_estimator": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float], ctypes.c_int),
@@ -112,6 +124,17 @@ _SIGS = {
                         ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rf_render": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(RenderDesc), ctypes.c_void_p,
                    ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    "rf_batch_create": ([ctypes.POINTER(BatchItem), ctypes.c_uint32, ctypes.POINTER(BatchDesc),
+                         ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rf_batch_run": ([ctypes.c_void_p], ctypes.c_int),
+    "rf_batch_sync": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    "rf_batch_image": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),
+    "rf_batch_bins": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                       ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
+    "rf_batch_read_bins": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rf_batch_info": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
+                       ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
+    "rf_batch_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "rf_write_png": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
 }
 
@@ -257,6 +280,12 @@ class Flame:
     def to_xml(self):
         return _string_out(library().rf_flame_to_xml, self._h)
 
+    def interpolate(self, other, t):
+        """Genome at t between self (t = 0) and other (t = 1)."""
+        h = ctypes.c_void_p()
+        _check(library().rf_flame_interpolate(self._h, other._h, t, ctypes.byref(h)))
+        return Flame(h, self._compiler)
+
     def info(self):
         i = FlameInfo()
         _check(library().rf_flame_get_info(self._h, ctypes.byref(i)))
@@ -362,6 +391,65 @@ class Sim:
         st = (ctypes.c_double * 3)()
         _check(library().rf_render(self._h, flame._h, ctypes.byref(d), img.ctypes.data_as(ctypes.c_void_p), st))
         return img, {"points": st[0], "binned": st[1], "ms": st[2]}
+
+
+class Batch:
+    """Many genomes drawn by one persistent launch, then density-estimated and tonemapped each
+    (rf_batch_*).  `items` holds (flame, width, height, points, seed) or
+    (flame, width, height, points, seed, supersample) tuples."""
+
+    def __init__(self, items, fuse_passes=20, cta_slots=0, unit_passes=0, density_estimation=True, k2=0.0,
+                 use_graph=True, device=0):
+        arr = (BatchItem * len(items))()
+        self.sizes = []
+        self._flames = [it[0] for it in items]  # keep the genomes alive as long as the batch
+        for i, it in enumerate(items):
+            flame, w, h, points, seed = it[:5]
+            ss = it[5] if len(it) > 5 else 1
+            arr[i] = BatchItem(flame._h, w, h, ss, points, seed)
+            self.sizes.append((w, h, ss))
+        d = BatchDesc(fuse_passes, cta_slots, unit_passes, int(density_estimation), k2, int(use_graph), device)
+        h = ctypes.c_void_p()
+        _check(library().rf_batch_create(arr, len(items), ctypes.byref(d), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            library().rf_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def run(self):
+        _check(library().rf_batch_run(self._h))
+
+    def sync(self):
+        st = (ctypes.c_double * 4)()
+        _check(library().rf_batch_sync(self._h, st))
+        return {"points": st[0], "binned": st[1], "ms": st[2], "steps": st[3]}
+
+    def image(self, i, out=None):
+        import numpy as np
+        w, h, _ = self.sizes[i]
+        img = out if out is not None else np.zeros((h, w, 4), np.uint8)
+        _check(library().rf_batch_image(self._h, i, img.ctypes.data_as(ctypes.c_void_p)))
+        return img
+
+    def bins(self, i):
+        """Host copies of item i's RGBA sums (H, W, 4 float32) and hit counts (H, W uint32)."""
+        import numpy as np
+        w, h, ss = self.sizes[i]
+        rgba = np.zeros((h * ss, w * ss, 4), np.float32)
+        hits = np.zeros((h * ss, w * ss), np.uint32)
+        _check(library().rf_batch_read_bins(self._h, i, rgba.ctypes.data_as(ctypes.c_void_p),
+                                            hits.ctypes.data_as(ctypes.c_void_p)))
+        return rgba, hits
+
+    def info(self):
+        a, b, c = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        _check(library().rf_batch_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"cta_slots": a.value, "units": b.value, "unit_passes": c.value}
 
 
 def render(sim, flame, *a, **k):

@@ -560,4 +560,70 @@ int genome_synthesize(int kind, uint64_t seed, uint32_t n_xforms, int final_xfor
     return genome_validate(g, reg);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Interpolation between two genomes (animation frames; the reference only rotates affines over
+// time, main.cpp:383-395).  Xform i of the shorter genome is padded with a copy of the longer
+// genome's xform i at selection weight 0; every numeric field is lerped, variation weights of
+// variations present on one side only lerp from 0; parameters present on one side are taken
+// as they are.
+// ---------------------------------------------------------------------------------------------
+namespace {
+inline float lerpf(float a, float b, float t) { return a + (b - a) * t; }
+
+Xform lerp_xform(const Xform& a, const Xform& b, float t) {
+    Xform o;
+    for (int i = 0; i < 6; i++) o.affine[i] = lerpf(a.affine[i], b.affine[i], t);
+    o.has_post = a.has_post || b.has_post;
+    if (o.has_post) {
+        const float id[6] = {1, 0, 0, 1, 0, 0};
+        for (int i = 0; i < 6; i++)
+            o.post[i] = lerpf(a.has_post ? a.post[i] : id[i], b.has_post ? b.post[i] : id[i], t);
+    }
+    o.weight = lerpf(a.weight, b.weight, t);
+    o.color = lerpf(a.color, b.color, t);
+    o.color_speed = lerpf(a.color_speed, b.color_speed, t);
+    o.opacity = lerpf(a.opacity, b.opacity, t);
+    o.rotation_frequency = t < 0.5f ? a.rotation_frequency : b.rotation_frequency;
+    for (const auto& [n, w] : a.vars) o.vars[n] = lerpf(w, b.vars.count(n) ? b.vars.at(n) : 0.0f, t);
+    for (const auto& [n, w] : b.vars)
+        if (!a.vars.count(n)) o.vars[n] = lerpf(0.0f, w, t);
+    for (const auto& [n, v] : a.params) o.params[n] = b.params.count(n) ? lerpf(v, b.params.at(n), t) : v;
+    for (const auto& [n, v] : b.params)
+        if (!a.params.count(n)) o.params[n] = v;
+    return o;
+}
+}  // namespace
+
+int genome_interpolate(const Genome& a, const Genome& b, float t, const Registry& reg, Genome& out) {
+    out = a;
+    const size_t n = std::max(a.xforms.size(), b.xforms.size());
+    out.xforms.clear();
+    for (size_t i = 0; i < n; i++) {
+        Xform xa, xb;
+        if (i < a.xforms.size()) xa = a.xforms[i]; else { xa = b.xforms[i]; xa.weight = 0.0f; }
+        if (i < b.xforms.size()) xb = b.xforms[i]; else { xb = a.xforms[i]; xb.weight = 0.0f; }
+        out.xforms.push_back(lerp_xform(xa, xb, t));
+    }
+    if (a.has_final || b.has_final) {
+        Xform ident;
+        ident.affine[0] = ident.affine[3] = 1.0f;
+        ident.vars["linear"] = 1.0f;
+        ident.opacity = 1.0f;
+        out.final_xf = lerp_xform(a.has_final ? a.final_xf : ident, b.has_final ? b.final_xf : ident, t);
+        out.has_final = true;
+    }
+    for (int k = 0; k < 256; k++)
+        for (int q = 0; q < 4; q++) out.palette[k][q] = lerpf(a.palette[k][q], b.palette[k][q], t);
+    for (int q = 0; q < 2; q++) out.center[q] = lerpf(a.center[q], b.center[q], t);
+    out.scale = lerpf(a.scale, b.scale, t);
+    out.rotate = lerpf(a.rotate, b.rotate, t);
+    out.gamma = lerpf(a.gamma, b.gamma, t);
+    out.brightness = lerpf(a.brightness, b.brightness, t);
+    out.vibrancy = lerpf(a.vibrancy, b.vibrancy, t);
+    out.est_curve = lerpf(a.est_curve, b.est_curve, t);
+    out.est_radius = (int)lrintf(lerpf((float)a.est_radius, (float)b.est_radius, t));
+    out.est_min = (int)lrintf(lerpf((float)a.est_min, (float)b.est_min, t));
+    return genome_validate(out, reg);
+}
+
 }  // namespace rfk

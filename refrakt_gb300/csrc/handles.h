@@ -1,0 +1,47 @@
+// Definitions of the opaque ABI handles, shared by the host runtime's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "internal.h"
+
+struct rf_compiler {
+    std::shared_ptr<const rfk::Registry> reg;
+};
+
+struct rf_flame {
+    rfk::Genome g;
+    std::shared_ptr<const rfk::Registry> reg;
+    uint64_t uid = 0;
+    uint64_t version = 0;
+};
+
+struct rf_sim {
+    rf_sim_desc d{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t N = 0;
+    uint32_t T = 1, ppts = 0, slots = 4096, threads = 1024, L = 32, table_size = 1024;
+    float4* walk[2] = {nullptr, nullptr};
+    int cur = 0;
+    uint4* rng = nullptr;
+    uint16_t* table = nullptr;
+    uint32_t* base_prog = nullptr;
+    uint32_t* progs = nullptr;
+    uint32_t prog_stride = 0, prog_words = 0;
+    float4* palette = nullptr;
+    unsigned long long* counters = nullptr;  // [0] drawn [1] emitted [2] steps [3] call drawn [4] call emitted
+    uint8_t* trace = nullptr;
+    uint32_t trace_passes = 0;
+    uint64_t warmed_uid = 0, warmed_version = 0;
+    uint32_t pass = 0;
+    int splat = RF_SPLAT_AUTO;
+    // rf_render scratch
+    float4* r_bins = nullptr;
+    uint32_t* r_hits = nullptr;
+    float4* r_de = nullptr;
+    uchar4* r_img = nullptr;
+    double* r_stats = nullptr;
+    size_t r_bins_n = 0, r_img_n = 0;
+};
+

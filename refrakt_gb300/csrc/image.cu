@@ -258,6 +258,9 @@ static void de_tables(int R, int min_r, float curve, DeTables& T, std::vector<fl
     }
 }
 
+static cudaError_t launch_density_passes(const float4* in, uint32_t w, uint32_t h, const DeTables& T, float4* out,
+                                         uint8_t* rad, const float* dw, cudaStream_t st);
+
 cudaError_t launch_density(const float4* in, uint32_t w, uint32_t h, int R, int min_r, float curve, float4* out,
                            cudaStream_t st) {
     DeTables T;
@@ -271,16 +274,7 @@ cudaError_t launch_density(const float4* in, uint32_t w, uint32_t h, int R, int 
     e = cudaMallocAsync(&dw, wts.size() * sizeof(float), st);
     if (e != cudaSuccess) { cudaFreeAsync(rad, st); return e; }
     cudaMemcpyAsync(dw, wts.data(), wts.size() * sizeof(float), cudaMemcpyHostToDevice, st);
-    de_radius_kernel<<<1024, 256, 0, st>>>(in, n, T, rad);
-    const int rmax = R > min_r ? R : min_r;
-    const dim3 grid((w + kDeTileX - 1) / kDeTileX, (h + kDeTileY - 1) / kDeTileY);
-    const int threads = kDeTileX * kDeTileY;
-    if (rmax <= 3) de_gather_kernel<3><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
-    else if (rmax <= 6) de_gather_kernel<6><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
-    else if (rmax <= 9) de_gather_kernel<9><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
-    else if (rmax <= kDeMaxSmemR) de_gather_kernel<kDeMaxSmemR><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
-    else de_gather_global_kernel<<<dim3((w + 127) / 128, h), 128, 0, st>>>(in, rad, w, h, dw, T, out);
-    e = cudaGetLastError();
+    e = launch_density_passes(in, w, h, T, out, rad, dw, st);
     cudaFreeAsync(rad, st);
     cudaFreeAsync(dw, st);
     return e;
@@ -293,19 +287,11 @@ size_t density_weight_count(int R, int min_r) {
     return n;
 }
 
-// The same two passes with scratch the caller provides (a byte per bin for the radii, `dw_cap`
-// floats for the kernel weights); nothing is allocated.
-cudaError_t launch_density_scratch(const float4* in, uint32_t w, uint32_t h, int R, int min_r, float curve,
-                                   float4* out, uint8_t* rad, float* dw, size_t dw_cap, cudaStream_t st) {
-    DeTables T;
-    std::vector<float> wts;
-    de_tables(R, min_r, curve, T, wts);
-    if (wts.size() > dw_cap) return cudaErrorInvalidValue;
+static cudaError_t launch_density_passes(const float4* in, uint32_t w, uint32_t h, const DeTables& T, float4* out,
+                                         uint8_t* rad, const float* dw, cudaStream_t st) {
     const size_t n = (size_t)w * h;
-    cudaError_t e = cudaMemcpyAsync(dw, wts.data(), wts.size() * sizeof(float), cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return e;
     de_radius_kernel<<<1024, 256, 0, st>>>(in, n, T, rad);
-    const int rmax = R > min_r ? R : min_r;
+    const int rmax = T.R > T.min_r ? T.R : T.min_r;
     const dim3 grid((w + kDeTileX - 1) / kDeTileX, (h + kDeTileY - 1) / kDeTileY);
     const int threads = kDeTileX * kDeTileY;
     if (rmax <= 3) de_gather_kernel<3><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
@@ -314,6 +300,32 @@ cudaError_t launch_density_scratch(const float4* in, uint32_t w, uint32_t h, int
     else if (rmax <= kDeMaxSmemR) de_gather_kernel<kDeMaxSmemR><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
     else de_gather_global_kernel<<<dim3((w + 127) / 128, h), 128, 0, st>>>(in, rad, w, h, dw, T, out);
     return cudaGetLastError();
+}
+
+// The same two passes with scratch the caller provides (a byte per bin for the radii, `dw_cap`
+// floats for the kernel weights); nothing is allocated.
+cudaError_t launch_density_scratch(const float4* in, uint32_t w, uint32_t h, int R, int min_r, float curve,
+                                   float4* out, uint8_t* rad, float* dw, size_t dw_cap, cudaStream_t st) {
+    DeTables T;
+    std::vector<float> wts;
+    de_tables(R, min_r, curve, T, wts);
+    if (wts.size() > dw_cap) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemcpyAsync(dw, wts.data(), wts.size() * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    return launch_density_passes(in, w, h, T, out, rad, dw, st);
+}
+
+void density_weights(int R, int min_r, std::vector<float>& wts) {
+    DeTables T;
+    de_tables(R, min_r, 1.0f, T, wts);
+}
+
+cudaError_t launch_density_resident(const float4* in, uint32_t w, uint32_t h, int R, int min_r, float curve,
+                                    float4* out, uint8_t* rad, const float* dw, cudaStream_t st) {
+    DeTables T;
+    std::vector<float> wts;
+    de_tables(R, min_r, curve, T, wts);
+    return launch_density_passes(in, w, h, T, out, rad, dw, st);
 }
 
 cudaError_t launch_stats(const float4* in, uint32_t w, uint32_t h, double* out3, cudaStream_t st) {

@@ -110,6 +110,7 @@ int genome_param_buffer(const Genome& g, std::vector<float>& buf, std::string* l
 int genome_program(const Genome& g, const Registry& reg, std::vector<uint32_t>& prog);
 void genome_screen_affine(const Genome& g, uint32_t w, uint32_t h, float out[6]);
 int genome_xform_draws(const Genome& g, const Registry& reg, int xi);
+int genome_interpolate(const Genome& a, const Genome& b, float t, const Registry& reg, Genome& out);
 int genome_synthesize(int kind, uint64_t seed, uint32_t n_xforms, int final_xform, int force_param,
                       uint32_t width, uint32_t height, const Registry& reg, Genome& g);
 

@@ -5,6 +5,8 @@
 #include <stdint.h>
 #include <stddef.h>
 
+#include <vector>
+
 namespace rfk {
 
 struct ChaosArgs {
@@ -51,6 +53,14 @@ size_t density_weight_count(int radius, int min_radius);
 cudaError_t launch_density_scratch(const float4* in, uint32_t w, uint32_t h, int radius, int min_radius, float curve,
                                    float4* out, uint8_t* radius_scratch, float* weight_scratch,
                                    size_t weight_capacity, cudaStream_t st);
+// Kernel weights of density estimation depend on the radii alone: `density_weights` builds them on
+// the host, and `launch_density_resident` runs both passes with those weights already on the
+// device (`dw`) and a byte of radius scratch per bin (`rad`) — no allocation and no host copy,
+// so the passes can be captured in a CUDA graph and replayed.
+void density_weights(int radius, int min_radius, std::vector<float>& out);
+cudaError_t launch_density_resident(const float4* in, uint32_t w, uint32_t h, int radius, int min_radius,
+                                    float curve, float4* out, uint8_t* radius_scratch, const float* weights,
+                                    cudaStream_t st);
 cudaError_t launch_stats(const float4* in, uint32_t w, uint32_t h, double* out3, cudaStream_t st);
 cudaError_t launch_tonemap(const float4* in, uint32_t w, uint32_t h, uint32_t ss, float gamma, float brightness,
                            float vibrancy, float k2, const double* stats, float4* out_f32, uchar4* out8,

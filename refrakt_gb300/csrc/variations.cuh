@@ -39,9 +39,9 @@ struct VaryOut {  // a variation's value and the slot's RNG state after it
 };
 
 #ifndef RFK_VARY_INLINE
-#define RFK_VARY_ATTR __device__ __noinline__
+#define RFK_VARY_ATTR static __device__ __noinline__
 #else
-#define RFK_VARY_ATTR __device__ __forceinline__
+#define RFK_VARY_ATTR static __device__ __forceinline__
 #endif
 
 // Unweighted value of variation `id` (radial_blur applies its weight internally).  Kept out of

@@ -60,7 +60,8 @@ def build(force=False, verbose=False):
                     raise RuntimeError("nvcc failed on " + s)
                 if verbose and (r.stdout or r.stderr):
                     sys.stderr.write(r.stdout + r.stderr)
-    if force or jobs or not os.path.exists(LIB):
+    stale = not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs)
+    if force or jobs or stale:
         tmp = LIB + ".tmp.%d" % os.getpid()
         cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -246,3 +246,39 @@ def test_no_device_is_reported(rk):
     with pytest.raises(rk.RefraktError) as e:
         rk.Sim(4096)
     assert e.value.status in (6, 9)
+
+
+def test_interpolation_endpoints_and_midpoint(rk, compiler):
+    a = rk.Flame.synthesize(compiler, rk.SYNTH_RANDOM, 2, 512, 512, n_xforms=4)
+    b = rk.Flame.synthesize(compiler, rk.SYNTH_RANDOM, 3, 512, 512, n_xforms=10)
+    f0, f1, fh = a.interpolate(b, 0.0), a.interpolate(b, 1.0), a.interpolate(b, 0.5)
+    assert f0.info()["num_xforms"] == 10 and fh.info()["num_xforms"] == 10
+    la, lb, l0, l1, lh = (x.param_layout() for x in (a, b, f0, f1, fh))
+    pa, pb, p0, p1, ph = (x.param_buffer() for x in (a, b, f0, f1, fh))
+    for i in range(10):
+        for k in range(6):
+            wa = pa[la["xforms"][i]["affine"][k]] if i < 4 else pb[lb["xforms"][i]["affine"][k]]
+            wb = pb[lb["xforms"][i]["affine"][k]]
+            assert p0[l0["xforms"][i]["affine"][k]] == pytest.approx(wa)
+            assert p1[l1["xforms"][i]["affine"][k]] == pytest.approx(wb)
+            assert ph[lh["xforms"][i]["affine"][k]] == pytest.approx(0.5 * (wa + wb), abs=1e-6)
+        # xforms beyond a's four start at selection weight 0
+        if i >= 4:
+            assert p0[l0["xforms"][i]["weight"]] == 0.0
+        for v, idx in l1["xforms"][i]["variations"].items():
+            want = pb[lb["xforms"][i]["variations"][v]] if v in lb["xforms"][i]["variations"] else 0.0
+            assert p1[idx] == pytest.approx(want, abs=1e-7)
+
+
+def test_batch_rejects_bad_arguments_before_device_work(rk, compiler):
+    import ctypes
+    L = rk.library()
+    h = ctypes.c_void_p()
+    d = rk.BatchDesc(0, 0, 0, 1, 0.0, 1, 0)
+    assert L.rf_batch_create(None, 0, ctypes.byref(d), ctypes.byref(h)) == 1
+    f = rk.Flame.synthesize(compiler, rk.SYNTH_SMALL, 0, 64, 64)
+    items = (rk.BatchItem * 1)(rk.BatchItem(f._h, 64, 64, 1, 0, 0))  # zero points
+    assert L.rf_batch_create(items, 1, ctypes.byref(d), ctypes.byref(h)) == 1
+    assert not h.value
+    assert L.rf_batch_run(None) == 1 and L.rf_batch_sync(None, None) == 1
+    assert L.rf_batch_destroy(None) == 0
