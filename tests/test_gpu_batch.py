@@ -115,7 +115,10 @@ def test_captured_tail_equals_entry_points(rk, compiler, use_graph):
         img8 = torch.zeros(h, w, 4, dtype=torch.uint8, device="cuda")
         rk.tonemap(d_de, w * ss, h * ss, ss, info["gamma"], info["brightness"], info["vibrancy"], 0.0, None, img8)
         torch.cuda.synchronize()
-        assert np.array_equal(b.image(i), img8.cpu().numpy())
+        got, want = b.image(i).astype(np.int32), img8.cpu().numpy().astype(np.int32)
+        # the automatic k2 comes from an FP64 atomic sum, whose order may move its last bit
+        assert np.abs(got - want).max() <= 1
+        assert np.mean(got == want) > 0.999
 
 
 def test_autotuned_shape_covers_points(rk, compiler):
