@@ -250,6 +250,7 @@ def run_native(args):
     img = torch.zeros(H_OUT, W_OUT, 4, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
     sim.set_stream(stream)
+    sim.set_splat({"auto": R.SPLAT_AUTO, "global": R.SPLAT_GLOBAL, "warp": R.SPLAT_WARP}[args.splat])
 
     # bins smaller than the 129 MB L2: write a 256 MB buffer before every frame
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda") if W * H * 20 <= 129e6 else None
@@ -327,7 +328,7 @@ def run_native(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic genome (seed 1); no dataset",
         "config": {"workload": CONFIG_NAME, "points_per_frame": POINTS, "bins": [W, H], "output": [W_OUT, H_OUT],
                    "genome": GENOME, "walkers": walkers, "cta_slots": cta, "steps_per_launch": args.steps_per_launch,
-                   "passes_per_frame": passes, "fuse_passes": FUSE, "density_estimation": list(DE) if DE else None,
+                   "passes_per_frame": passes, "fuse_passes": FUSE, "splat": args.splat, "density_estimation": list(DE) if DE else None,
                    "l2": "bins %dx%d x 20 B = %.0f MB (L2 129 MB)%s" % (W, H, W * H * 20 / 1e6,
                          "; exceed L2" if W * H * 20 > 129e6 else "; an L2 flush separates frames"),
                    "parallelism": "replicas" if ws > 1 else "single"},
@@ -470,6 +471,7 @@ def main():
     ap.add_argument("--ctas-per-sm", type=int, default=4)
     ap.add_argument("--steps-per-launch", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--splat", default="auto", choices=["auto", "global", "warp"])
     ap.add_argument("--workload", default="frame1080", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     select_workload(args.workload)

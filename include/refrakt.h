@@ -276,6 +276,7 @@ typedef struct {
     float    k2;                /* tonemap k2 (<= 0: automatic per genome) */
     int32_t  use_graph;         /* 1: capture the whole batch in a CUDA graph */
     int32_t  device;
+    int32_t  splat;             /* rf_splat; AUTO chooses per genome from its probe histogram */
 } rf_batch_desc;
 RF_API int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc* d, rf_batch** out);
 /* Enqueues one whole batch (clear, draw, DE, tonemap) on the batch's own stream. */
@@ -291,6 +292,8 @@ RF_API int rf_batch_bins(rf_batch* b, uint32_t i, float** rgba, uint32_t** hits,
 RF_API int rf_batch_read_bins(rf_batch* b, uint32_t i, float* host_rgba, uint32_t* host_hits);
 /* The autotuned shape: walkers per unit, number of units, drawing passes per unit. */
 RF_API int rf_batch_info(const rf_batch* b, uint32_t* cta_slots, uint32_t* units, uint32_t* unit_passes);
+/* The splat strategy chosen for item i (RF_SPLAT_GLOBAL or RF_SPLAT_WARP); -1 for a bad index. */
+RF_API int rf_batch_splat(const rf_batch* b, uint32_t i);
 RF_API int rf_batch_destroy(rf_batch* b);
 
 /* Writes an RGBA8 image as an uncompressed PNG. */

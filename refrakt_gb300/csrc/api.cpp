@@ -80,6 +80,7 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.seed = s->d.seed;
         a.first_run = (first_run && done == 0) ? 1 : 0;
         a.draw = draw ? 1 : 0;
+        a.splat = s->splat == RF_SPLAT_WARP ? 1 : 0;
         if (ss) memcpy(a.ss, ss, sizeof(a.ss));
         a.W = W;
         a.H = H;
@@ -439,6 +440,7 @@ int rf_draw_to_bins(rf_sim* s, rf_flame* f, float* bins_rgba, uint32_t* bins_hit
                     uint32_t num_iter, uint64_t* drawn) {
     if (!s || !f || !bins_rgba) return fail(RF_ERR_INVALID_ARG, "rf_draw_to_bins: null argument");
     if (W == 0 || H == 0 || W > 65536 || H > 65536) return fail(RF_ERR_INVALID_ARG, "bin grid must be 1..65536 on each side");
+    if ((uint64_t)W * H >= 0xffffffffull) return fail(RF_ERR_CAPACITY, "bin grid must hold fewer than 2^32 - 1 bins");
     if (rf_needs_warmup(s, f)) return fail(RF_ERR_NEEDS_WARMUP, "flame changed or not warmed up: call rf_warmup");
     if (f->g.size[1] == 0) return fail(RF_ERR_INVALID_ARG, "genome size is zero");
     if (((uintptr_t)bins_rgba) & 15) return fail(RF_ERR_INVALID_ARG, "bins_rgba must be 16-byte aligned");
@@ -546,8 +548,11 @@ int rf_render(rf_sim* s, rf_flame* f, const rf_render_desc* d, uint8_t* out, dou
     const uint32_t ss = d->supersample ? d->supersample : 1;
     if (d->width == 0 || d->height == 0) return fail(RF_ERR_INVALID_ARG, "rf_render: empty image");
     if (f->g.size[1] == 0) return fail(RF_ERR_INVALID_ARG, "genome size is zero");
+    if ((uint64_t)d->width * ss > 65536 || (uint64_t)d->height * ss > 65536)
+        return fail(RF_ERR_INVALID_ARG, "rf_render: bin grid too large");
     const uint32_t W = d->width * ss, H = d->height * ss;
-    if (W > 65536 || H > 65536) return fail(RF_ERR_INVALID_ARG, "rf_render: bin grid too large");
+    if ((uint64_t)W * H >= 0xffffffffull)
+        return fail(RF_ERR_INVALID_ARG, "rf_render: bin grid too large");
     if (int rc = set_device(s)) return rc;
     const size_t nb = (size_t)W * H, ni = (size_t)d->width * d->height;
     if (s->r_bins_n != nb) {

@@ -10,17 +10,10 @@
 #include <cuda_runtime.h>
 
 #include "batch.h"
+#include "splat.cuh"
 #include "variations.cuh"
 
 namespace rfk {
-
-__device__ __forceinline__ void red_add_v4b(float4* p, float a, float b, float c, float d) {
-    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
-                 : "memory");
-}
-__device__ __forceinline__ void red_add_u32b(uint32_t* p, uint32_t v) {
-    asm volatile("red.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 
 __host__ __device__ inline size_t batch_smem_bytes(int slots, uint32_t max_prog_words) {
     size_t b = ((size_t)max_prog_words * 4 + 15) & ~(size_t)15;
@@ -134,14 +127,17 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) batch_kernel(const Ba
                     if (op > 0.0f) emitted++;
                     const float px = fmaf(I.ss[0], ex, fmaf(I.ss[2], ey, I.ss[4]));
                     const float py = fmaf(I.ss[1], ex, fmaf(I.ss[3], ey, I.ss[5]));
+                    uint32_t bin = kNoBin;
+                    float4 val = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     if (px >= 0.0f && py >= 0.0f && px < Wf && py < Hf && op > 0.0f) {
                         const uint32_t bx = (uint32_t)px, by = (uint32_t)py;
-                        const size_t idx = (size_t)(I.H - 1 - by) * I.W + bx;
+                        bin = (I.H - 1 - by) * I.W + bx;
                         const float4 col = s_pal[palette_index(ec)];
-                        red_add_v4b(I.bins + idx, col.x, col.y, col.z, op);
-                        if (I.hits) red_add_u32b(I.hits + idx, 1u);
+                        val = make_float4(col.x, col.y, col.z, op);
                         drawn++;
                     }
+                    if (I.splat) splat_warp(I.bins, I.hits, bin, val);
+                    else splat_global(I.bins, I.hits, bin, val);
                 }
             }
         }

@@ -14,6 +14,7 @@ struct BatchInstance {
     float4* bins;           // RGBA sums, W * H
     uint32_t* hits;         // counts, may be null
     uint32_t W, H;
+    uint32_t splat;         // 0: a reduction per point; 1: warp-aggregated (splat.cuh)
     float ss[6];            // screen affine
 };
 

@@ -32,6 +32,7 @@ struct Item {
     uchar4* img = nullptr;
     float4* palette = nullptr;
     uint32_t* dprog = nullptr;
+    uint32_t splat = 0;       // warp-aggregated splat for this genome
     uint8_t* rad = nullptr;   // density estimation: a radius byte per bin
     float* dw = nullptr;      // density estimation: kernel weights of every radius
     uint64_t passes = 0;  // drawing passes of SLOTS walkers the item needs
@@ -41,6 +42,7 @@ struct Item {
 
 constexpr uint64_t kUnitSeedStride = 0x9e3779b97f4a7c15ull;  // unit u of an item: seed + u * stride
 constexpr uint64_t kTableSeed = 0x5eed;                      // shared table: keyed by kTableSeed + slots
+constexpr double kCompactFraction = 0.125;  // occupied bins / probe points below this: compact attractor
 
 // Histogram L1 noise of a mixing domain relative to the reference's global shuffle, measured on
 // the CPU oracle (tests/test_oracle_self.py): variance grows with its square.
@@ -96,9 +98,10 @@ int cuda_err(cudaError_t e, const char* what) {
     return fail(RF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// Builds the instance and unit tables for a shape; `probe_passes` > 0 builds the autotuner's
-// probe instead (one unit per item, that many drawing passes, no fuse).
-int build_tables(rf_batch* b, uint32_t slots, uint32_t unit_passes, uint32_t probe_passes, uint32_t max_items) {
+// Builds the instance and unit tables for a shape; `probe_passes` > 0 builds an autotuner probe
+// instead (one unit per item, `probe_fuse` then `probe_passes` passes).
+int build_tables(rf_batch* b, uint32_t slots, uint32_t unit_passes, uint32_t probe_passes, uint32_t max_items,
+                 uint32_t probe_fuse = 0) {
     std::vector<BatchInstance> inst;
     std::vector<BatchUnit> units;
     const size_t n = std::min<size_t>(b->items.size(), max_items);
@@ -107,12 +110,13 @@ int build_tables(rf_batch* b, uint32_t slots, uint32_t unit_passes, uint32_t pro
         BatchInstance I{};
         I.prog = it.dprog;
         I.prog_words = (uint32_t)it.prog.size();
-        I.fuse = probe_passes ? 0 : b->fuse;
+        I.fuse = probe_passes ? probe_fuse : b->fuse;
         I.palette = it.palette;
         I.bins = it.bins;
         I.hits = it.hits;
         I.W = it.W;
         I.H = it.H;
+        I.splat = it.splat;
         genome_screen_affine(b->items[i].desc.flame->g, it.W, it.H, I.ss);
         inst.push_back(I);
         if (probe_passes) {
@@ -211,7 +215,8 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
             return fail(RF_ERR_INVALID_ARG, "rf_batch_create: item without genome, size or points");
         if (f->g.size[1] == 0) return fail(RF_ERR_INVALID_ARG, "rf_batch_create: genome size is zero");
         const uint32_t ss = items[i].supersample ? items[i].supersample : 1;
-        if ((uint64_t)items[i].width * ss > 65536 || (uint64_t)items[i].height * ss > 65536)
+        if ((uint64_t)items[i].width * ss > 65536 || (uint64_t)items[i].height * ss > 65536 ||
+            (uint64_t)items[i].width * ss * items[i].height * ss >= 0xffffffffull)
             return fail(RF_ERR_INVALID_ARG, "rf_batch_create: bin grid too large");
     }
     if (d->cta_slots && d->cta_slots != 1024 && d->cta_slots != 2048 && d->cta_slots != 4096)
@@ -289,6 +294,30 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
     }
     b->threads = 1024;
     if (int rc = make_table(b, b->slots)) return bail(rc);
+    // --- splat strategy per genome: a compact attractor (few occupied bins per point drawn in a
+    // 16-pass probe unit) takes the warp-aggregated reductions
+    if (d->splat == RF_SPLAT_AUTO) {
+        constexpr uint32_t kProbe = 16;
+        for (auto& it : b->items) {
+            const size_t nb = (size_t)it.W * it.H;
+            e = cudaMemsetAsync(it.bins, 0, nb * sizeof(float4), b->stream);
+            if (e == cudaSuccess) e = cudaMemsetAsync(it.hits, 0, nb * sizeof(uint32_t), b->stream);
+            if (e != cudaSuccess) return bail(cuda_err(e, "splat probe"));
+        }
+        if (int rc = build_tables(b, b->slots, 0, kProbe, n, b->fuse)) return bail(rc);
+        cudaMemsetAsync(b->queue, 0, sizeof(unsigned int), b->stream);
+        e = launch_batch((int)b->threads, (int)b->slots, args_for(b), b->stream, nullptr);
+        for (uint32_t i = 0; i < n && e == cudaSuccess; i++)
+            e = launch_stats(b->items[i].bins, b->items[i].W, b->items[i].H, b->stats + 3 * i, b->stream);
+        std::vector<double> st(3 * (size_t)n);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(st.data(), b->stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        if (e != cudaSuccess) return bail(cuda_err(e, "splat probe"));
+        const double probe_points = (double)b->slots * kProbe;
+        for (uint32_t i = 0; i < n; i++) b->items[i].splat = st[3 * i + 2] < kCompactFraction * probe_points ? 1u : 0u;
+    } else {
+        for (auto& it : b->items) it.splat = d->splat == RF_SPLAT_WARP ? 1u : 0u;
+    }
     // --- drawing passes per unit: >= 8 units per persistent CTA, fuse <= 5 % of a unit
     uint64_t total_passes = 0;
     for (auto& it : b->items) total_passes += (it.desc.points + b->slots - 1) / b->slots;
@@ -382,6 +411,11 @@ int rf_batch_read_bins(rf_batch* b, uint32_t i, float* host_rgba, uint32_t* host
     if (e == cudaSuccess && host_hits) e = cudaMemcpy(host_hits, it.hits, nb * sizeof(uint32_t), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_err(e, "rf_batch_read_bins");
     return RF_OK;
+}
+
+int rf_batch_splat(const rf_batch* b, uint32_t i) {
+    if (!b || i >= b->items.size()) return -1;
+    return b->items[i].splat ? RF_SPLAT_WARP : RF_SPLAT_GLOBAL;
 }
 
 int rf_batch_info(const rf_batch* b, uint32_t* cta_slots, uint32_t* units, uint32_t* unit_passes) {

@@ -15,17 +15,10 @@
 #include <cuda_runtime.h>
 
 #include "kernels.h"
+#include "splat.cuh"
 #include "variations.cuh"
 
 namespace rfk {
-
-__device__ __forceinline__ void red_add_v4(float4* p, float a, float b, float c, float d) {
-    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
-                 : "memory");
-}
-__device__ __forceinline__ void red_add_u32(uint32_t* p, uint32_t v) {
-    asm volatile("red.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 
 // Shared memory of a chaos CTA (dynamic, in this order):
 //   program words (prog_words), palette float4[256], walker exchange float4 [2][SLOTS],
@@ -158,14 +151,17 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) chaos_kernel(const Ch
                 if (op > 0.0f) emitted++;
                 const float px = fmaf(A.ss[0], ex, fmaf(A.ss[2], ey, A.ss[4]));
                 const float py = fmaf(A.ss[1], ex, fmaf(A.ss[3], ey, A.ss[5]));
+                uint32_t bin = kNoBin;
+                float4 val = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 if (px >= 0.0f && py >= 0.0f && px < W && py < H && op > 0.0f) {
                     const uint32_t bx = (uint32_t)px, by = (uint32_t)py;
-                    const size_t idx = (size_t)(A.H - 1 - by) * A.W + bx;  // flame.glsl:84 row flip
+                    bin = (A.H - 1 - by) * A.W + bx;  // flame.glsl:84 row flip; W*H < 2^32 - 1
                     const float4 col = s_pal[palette_index(ec)];
-                    red_add_v4(A.bins + idx, col.x, col.y, col.z, op);
-                    if (A.hits) red_add_u32(A.hits + idx, 1u);
+                    val = make_float4(col.x, col.y, col.z, op);
                     drawn++;
                 }
+                if (A.splat) splat_warp(A.bins, A.hits, bin, val);
+                else splat_global(A.bins, A.hits, bin, val);
             }
         }
     }

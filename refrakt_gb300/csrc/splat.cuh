@@ -1,0 +1,69 @@
+// Histogram splat of one point per lane (flame.glsl:81-86): RGBA sums (palette colour, opacity)
+// and a hit count per bin, as L2 reductions.
+//
+//   splat_global — one red.global.add.v4.f32 and one red.global.add.u32 per point.
+//   splat_warp   — warp-aggregated: lanes whose points fall into the same bin are found with
+//                  match.any; the lowest lane of each set adds the set's colours and issues one
+//                  v4 reduction and one count reduction of the set's size.  Where the attractor is
+//                  compact (every lane of a warp applies the same xform, so a contracting map
+//                  sends the warp's 32 walkers into a few bins) this divides the reductions on the
+//                  hottest addresses by up to 32.  The colour sums are added in a tree over the
+//                  set's lanes (the peer reduction of E. Westphal, "Voting and shuffling to
+//                  optimize atomic operations", GTC 2015), so only their FP32 rounding order
+//                  differs from splat_global; the counts are exact either way.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace rfk {
+
+constexpr uint32_t kNoBin = 0xffffffffu;
+
+__device__ __forceinline__ void red_add_f32x4(float4* p, float a, float b, float c, float d) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
+                 : "memory");
+}
+__device__ __forceinline__ void red_add_u32x1(uint32_t* p, uint32_t v) {
+    asm volatile("red.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void splat_global(float4* bins, uint32_t* hits, uint32_t bin, float4 v) {
+    if (bin == kNoBin) return;
+    red_add_f32x4(bins + bin, v.x, v.y, v.z, v.w);
+    if (hits) red_add_u32x1(hits + bin, 1u);
+}
+
+// Every lane of the warp must call this (bin = kNoBin for lanes without a point).
+__device__ __forceinline__ void splat_warp(float4* bins, uint32_t* hits, uint32_t bin, float4 v) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned peers = __match_any_sync(0xffffffffu, bin);
+    if (__all_sync(0xffffffffu, peers == (1u << lane))) {  // no two lanes share a bin
+        splat_global(bins, hits, bin, v);
+        return;
+    }
+    unsigned rank = __popc(peers & ((1u << lane) - 1u));
+    unsigned above = peers & (0xfffffffeu << lane);
+    while (__any_sync(0xffffffffu, above != 0u)) {
+        const int next = __ffs(above);  // 1 + lane of the next peer above, 0 if none
+        const int srcl = next ? next - 1 : (int)lane;
+        const float tx = __shfl_sync(0xffffffffu, v.x, srcl);
+        const float ty = __shfl_sync(0xffffffffu, v.y, srcl);
+        const float tz = __shfl_sync(0xffffffffu, v.z, srcl);
+        const float tw = __shfl_sync(0xffffffffu, v.w, srcl);
+        if (next) {
+            v.x += tx;
+            v.y += ty;
+            v.z += tz;
+            v.w += tw;
+        }
+        above &= __ballot_sync(0xffffffffu, (rank & 1u) == 0u);  // lanes at odd rank are merged
+        rank >>= 1;
+    }
+    if (bin != kNoBin && (peers & ((1u << lane) - 1u)) == 0u) {  // lowest lane of its set
+        red_add_f32x4(bins + bin, v.x, v.y, v.z, v.w);
+        if (hits) red_add_u32x1(hits + bin, (uint32_t)__popc(peers));
+    }
+}
+
+}  // namespace rfk
