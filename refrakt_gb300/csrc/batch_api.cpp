@@ -42,7 +42,7 @@ struct Item {
 
 constexpr uint64_t kUnitSeedStride = 0x9e3779b97f4a7c15ull;  // unit u of an item: seed + u * stride
 constexpr uint64_t kTableSeed = 0x5eed;                      // shared table: keyed by kTableSeed + slots
-constexpr double kCompactFraction = 0.125;  // occupied bins / probe points below this: compact attractor
+constexpr double kCompactDensity = 4.0;  // probe points per occupied bin above this: compact attractor
 
 // Histogram L1 noise of a mixing domain relative to the reference's global shuffle, measured on
 // the CPU oracle (tests/test_oracle_self.py): variance grows with its square.
@@ -294,7 +294,7 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
     }
     b->threads = 1024;
     if (int rc = make_table(b, b->slots)) return bail(rc);
-    // --- splat strategy per genome: a compact attractor (few occupied bins per point drawn in a
+    // --- splat strategy per genome: a compact attractor (many points per occupied bin in a
     // 16-pass probe unit) takes the warp-aggregated reductions
     if (d->splat == RF_SPLAT_AUTO) {
         constexpr uint32_t kProbe = 16;
@@ -313,8 +313,9 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
         if (e == cudaSuccess) e = cudaMemcpyAsync(st.data(), b->stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
         if (e != cudaSuccess) return bail(cuda_err(e, "splat probe"));
-        const double probe_points = (double)b->slots * kProbe;
-        for (uint32_t i = 0; i < n; i++) b->items[i].splat = st[3 * i + 2] < kCompactFraction * probe_points ? 1u : 0u;
+        // points drawn per occupied bin (opacity-weighted): large for a compact attractor
+        for (uint32_t i = 0; i < n; i++)
+            b->items[i].splat = st[3 * i] >= kCompactDensity * std::max(1.0, st[3 * i + 2]) ? 1u : 0u;
     } else {
         for (auto& it : b->items) it.splat = d->splat == RF_SPLAT_WARP ? 1u : 0u;
     }

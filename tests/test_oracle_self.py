@@ -57,8 +57,11 @@ def _noise(runs):
 def test_kernel_shuffle_schedule_matches_reference_scheme(small_genome, rich_genome, which):
     """The kernel's walker shuffle (a keyed permutation of each mixing domain every pass, a keyed
     global gather every L passes) against the reference's fresh global permutation per pass
-    (flame.cpp:317-325): a 4096-slot domain (a 4-CTA cluster) is as noisy as the reference's
-    scheme; a single 1024-slot CTA stays within 1.5x."""
+    (flame.cpp:317-325): a 4096-slot domain (one 1024-thread CTA, 4 slots per thread) is as noisy
+    as the reference's scheme; a 1024-slot domain stays within 1.5x.  (Measured with 16 seeds on
+    8192 walkers: 4096 slots 1.02x / 0.98x, 2048 1.09x / 1.03x, 1024 1.30x / 1.15x, 512 1.8x /
+    1.4x, 256 6.0x / 2.5x for the small / rich genome — a 256-slot domain is a single xform group,
+    whose walkers all take the same xform every pass.)"""
     g = small_genome if which == "small" else rich_genome
     kw = dict(walkers=8192, width=96, height=96, fuse=20, draw=48, want_rgba=False)
     seeds = range(16)
