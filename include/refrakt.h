@@ -296,6 +296,62 @@ RF_API int rf_batch_info(const rf_batch* b, uint32_t* cta_slots, uint32_t* units
 RF_API int rf_batch_splat(const rf_batch* b, uint32_t i);
 RF_API int rf_batch_destroy(rf_batch* b);
 
+/* ------------------------------------------------------------------------------------------
+ * Tensor-core GEMM of the learned density estimator (no reference counterpart; the reference
+ * has no learned path).  C[M x N] (+)= A[M x K] * B[N x K]^T with A, B bf16 device matrices,
+ * K contiguous (row strides lda, ldb in elements, multiples of 8, 16-byte aligned bases), FP32
+ * accumulation on tcgen05 tensor cores.  Modes: RF_GEMM_STORE_F32 (C float), RF_GEMM_STORE_BF16
+ * (C bf16 = relu?(acc + bias[n])), RF_GEMM_ATOMIC_F32 (C float += acc; required for splits > 1,
+ * which partitions K over CTAs).  Synchronises the stream.
+ * ---------------------------------------------------------------------------------------- */
+enum rf_gemm_mode { RF_GEMM_STORE_F32 = 0, RF_GEMM_STORE_BF16 = 1, RF_GEMM_ATOMIC_F32 = 2 };
+RF_API int rf_gemm_bf16(const void* A, const void* B, void* C, uint32_t M, uint32_t N, uint32_t K, uint32_t lda,
+                        uint32_t ldb, uint32_t ldc, int mode, const float* bias, int relu, uint32_t splits,
+                        void* stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Learned density estimation (no reference counterpart).  A U-Net maps the features of a
+ * short-run histogram to the converged, tonemapped RGB image: 4 levels of 32-48-64-96
+ * channels, two 3x3 convolutions + ReLU per level, 2x2 average pooling, nearest-neighbour
+ * upsampling with channel-concatenated skips, a 1x1 output convolution.  BF16 weights (FP32
+ * masters), FP32 accumulation on the tcgen05 tensor cores; forward, backward and Adam are the
+ * library's own kernels.  Tensors are device memory, NHWC: features bf16 [n, h, w, 8], images
+ * and targets FP32 [n, h, w, 3]; h and w multiples of 8.  The denoiser runs on its own stream
+ * (or the one set by rf_denoiser_set_stream); train_step with loss != NULL synchronises.
+ * ---------------------------------------------------------------------------------------- */
+typedef struct rf_denoiser rf_denoiser;
+typedef struct {
+    uint64_t max_pixels;        /* capacity: n * h * w of the largest call */
+    uint64_t seed;              /* He-normal initialisation */
+    int32_t  device;
+} rf_denoiser_desc;
+typedef struct {
+    uint32_t in_a, in_b, out, taps;  /* input channels (in_b: skip, concatenated), outputs, 9 or 1 */
+    int32_t  upsample, relu, level;  /* in_a upsampled 2x; ReLU; resolution level (0 = full) */
+    int32_t  src_a, src_b;           /* producing layer, -1 the features / none, -100-l the pool
+                                        of level l's input (the level above's last encoder conv) */
+} rf_denoiser_layer_info;
+RF_API int rf_denoiser_create(const rf_denoiser_desc* d, rf_denoiser** out);
+RF_API int rf_denoiser_destroy(rf_denoiser* d);
+RF_API int rf_denoiser_set_stream(rf_denoiser* d, void* stream);
+RF_API int rf_denoiser_num_layers(const rf_denoiser* d);
+RF_API int rf_denoiser_layer(const rf_denoiser* d, int i, rf_denoiser_layer_info* out);
+/* Parameters in layer order, each layer its weights [out][tap][in_a + in_b] then its bias. */
+RF_API size_t rf_denoiser_num_params(const rf_denoiser* d);
+RF_API int rf_denoiser_get_params(rf_denoiser* d, float* host, size_t cap);
+RF_API int rf_denoiser_set_params(rf_denoiser* d, const float* host, size_t count);
+/* Gradients of the last train_step, same layout as the parameters. */
+RF_API int rf_denoiser_gradients(rf_denoiser* d, float* host, size_t cap);
+/* Features of a histogram (bins float4 RGBA sums, width x height): [log10(1 + a k2),
+   rgb * log10(1 + a k2) / a, 0 x 4] as bf16; k2 <= 0 takes W*H / sum(a) (FP64 reduction). */
+RF_API int rf_denoiser_features(const float* bins_rgba, uint32_t width, uint32_t height, float k2, void* out_bf16,
+                                void* stream);
+/* out_rgb = clamp(net(feats), 0, 1). */
+RF_API int rf_denoiser_infer(rf_denoiser* d, const void* feats, uint32_t n, uint32_t h, uint32_t w, float* out_rgb);
+/* One Adam step (lr; betas 0.9, 0.999; eps 1e-8) on the mean L1 loss against target_rgb. */
+RF_API int rf_denoiser_train_step(rf_denoiser* d, const void* feats, const float* target_rgb, uint32_t n, uint32_t h,
+                                  uint32_t w, float lr, double* loss);
+
 /* Writes an RGBA8 image as an uncompressed PNG. */
 RF_API int rf_write_png(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height);
 

@@ -16,7 +16,8 @@ import os
 __all__ = ["RefraktError", "FlameCompiler", "Flame", "Sim", "library", "build", "density_estimate",
            "tonemap", "hist_stats", "shuffle_generate", "probe_xform", "write_png", "render",
            "SYNTH_SMALL", "SYNTH_RANDOM", "SYNTH_CONTRACT", "SYNTH_SPACEFILL",
-           "SPLAT_AUTO", "SPLAT_GLOBAL", "SPLAT_WARP"]
+           "SPLAT_AUTO", "SPLAT_GLOBAL", "SPLAT_WARP", "Batch", "Denoiser", "denoiser_features", "gemm_bf16",
+           "GEMM_STORE_F32", "GEMM_STORE_BF16", "GEMM_ATOMIC_F32"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "librefrakt_gb300.so")
@@ -71,6 +72,16 @@ class BatchDesc(ctypes.Structure):
     _fields_ = [("fuse_passes", ctypes.c_uint32), ("cta_slots", ctypes.c_uint32), ("unit_passes", ctypes.c_uint32),
                 ("density_estimation", ctypes.c_int32), ("k2", ctypes.c_float), ("use_graph", ctypes.c_int32),
                 ("device", ctypes.c_int32), ("splat", ctypes.c_int32)]
+
+
+class DenoiserDesc(ctypes.Structure):
+    _fields_ = [("max_pixels", ctypes.c_uint64), ("seed", ctypes.c_uint64), ("device", ctypes.c_int32)]
+
+
+class DenoiserLayer(ctypes.Structure):
+    _fields_ = [("in_a", ctypes.c_uint32), ("in_b", ctypes.c_uint32), ("out", ctypes.c_uint32),
+                ("taps", ctypes.c_uint32), ("upsample", ctypes.c_int32), ("relu", ctypes.c_int32),
+                ("level", ctypes.c_int32), ("src_a", ctypes.c_int32), ("src_b", ctypes.c_int32)]
 
 
 _lib = None
@@ -136,6 +147,22 @@ _SIGS = {
                        ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
     "rf_batch_splat": ([ctypes.c_void_p, ctypes.c_uint32], ctypes.c_int),
     "rf_batch_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "rf_gemm_bf16": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 6 +
+                     [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),
+    "rf_denoiser_create": ([ctypes.POINTER(DenoiserDesc), ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rf_denoiser_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "rf_denoiser_set_stream": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rf_denoiser_num_layers": ([ctypes.c_void_p], ctypes.c_int),
+    "rf_denoiser_layer": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(DenoiserLayer)], ctypes.c_int),
+    "rf_denoiser_num_params": ([ctypes.c_void_p], ctypes.c_size_t),
+    "rf_denoiser_get_params": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t], ctypes.c_int),
+    "rf_denoiser_set_params": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t], ctypes.c_int),
+    "rf_denoiser_gradients": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t], ctypes.c_int),
+    "rf_denoiser_features": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_void_p,
+                              ctypes.c_void_p], ctypes.c_int),
+    "rf_denoiser_infer": ([ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 3 + [ctypes.c_void_p], ctypes.c_int),
+    "rf_denoiser_train_step": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 3 +
+                               [ctypes.c_float, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     "rf_write_png": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
 }
 
@@ -482,6 +509,80 @@ def probe_xform(flame, xform, xyc, rng, out, first_run=False, stream=None):
     n = xyc.shape[0]
     _check(library().rf_probe_xform(flame._h, xform, n, _ptr(xyc), _ptr(rng), int(first_run), _ptr(out),
                                     _stream(stream)))
+
+
+GEMM_STORE_F32, GEMM_STORE_BF16, GEMM_ATOMIC_F32 = 0, 1, 2
+
+
+def gemm_bf16(a, b, c, mode=GEMM_STORE_F32, bias=None, relu=False, splits=1, stream=None):
+    """c (+)= a @ b.T on the tensor cores; a (M x K) and b (N x K) bf16 CUDA tensors."""
+    M, K = a.shape
+    N = b.shape[0]
+    _check(library().rf_gemm_bf16(_ptr(a), _ptr(b), _ptr(c), M, N, K, a.stride(0), b.stride(0), c.stride(0), mode,
+                                  _ptr(bias), int(relu), splits, _stream(stream)))
+
+
+class Denoiser:
+    """The learned density estimator (rf_denoiser_*): features [n, h, w, 8] bf16 and images /
+    targets [n, h, w, 3] float32 are CUDA tensors (h, w multiples of 8)."""
+
+    def __init__(self, max_pixels, seed=0, device=0):
+        h = ctypes.c_void_p()
+        _check(library().rf_denoiser_create(ctypes.byref(DenoiserDesc(max_pixels, seed, device)), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            library().rf_denoiser_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_stream(self, stream):
+        _check(library().rf_denoiser_set_stream(self._h, _stream(stream)))
+
+    def layers(self):
+        out = []
+        for i in range(library().rf_denoiser_num_layers(self._h)):
+            li = DenoiserLayer()
+            _check(library().rf_denoiser_layer(self._h, i, ctypes.byref(li)))
+            out.append({k: getattr(li, k) for k, _ in DenoiserLayer._fields_})
+        return out
+
+    def num_params(self):
+        return library().rf_denoiser_num_params(self._h)
+
+    def params(self):
+        import numpy as np
+        a = np.zeros(self.num_params(), np.float32)
+        _check(library().rf_denoiser_get_params(self._h, a.ctypes.data_as(ctypes.c_void_p), a.size))
+        return a
+
+    def set_params(self, a):
+        import numpy as np
+        a = np.ascontiguousarray(a, np.float32)
+        _check(library().rf_denoiser_set_params(self._h, a.ctypes.data_as(ctypes.c_void_p), a.size))
+
+    def gradients(self):
+        import numpy as np
+        a = np.zeros(self.num_params(), np.float32)
+        _check(library().rf_denoiser_gradients(self._h, a.ctypes.data_as(ctypes.c_void_p), a.size))
+        return a
+
+    def infer(self, feats, out):
+        n, h, w = feats.shape[:3]
+        _check(library().rf_denoiser_infer(self._h, _ptr(feats), n, h, w, _ptr(out)))
+
+    def train_step(self, feats, target, lr):
+        n, h, w = feats.shape[:3]
+        loss = ctypes.c_double()
+        _check(library().rf_denoiser_train_step(self._h, _ptr(feats), _ptr(target), n, h, w, lr, ctypes.byref(loss)))
+        return loss.value
+
+
+def denoiser_features(bins_rgba, width, height, out, k2=0.0, stream=None):
+    _check(library().rf_denoiser_features(_ptr(bins_rgba), width, height, k2, _ptr(out), _stream(stream)))
 
 
 def write_png(path, rgba8):
