@@ -42,7 +42,7 @@ struct Item {
 
 constexpr uint64_t kUnitSeedStride = 0x9e3779b97f4a7c15ull;  // unit u of an item: seed + u * stride
 constexpr uint64_t kTableSeed = 0x5eed;                      // shared table: keyed by kTableSeed + slots
-constexpr double kCompactDensity = 4.0;  // probe points per occupied bin above this: compact attractor
+constexpr double kCompactShare = 16.0;  // probe points sharing a point's bin above this: compact attractor
 
 // Histogram L1 noise of a mixing domain relative to the reference's global shuffle, measured on
 // the CPU oracle (tests/test_oracle_self.py): variance grows with its square.
@@ -294,8 +294,8 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
     }
     b->threads = 1024;
     if (int rc = make_table(b, b->slots)) return bail(rc);
-    // --- splat strategy per genome: a compact attractor (many points per occupied bin in a
-    // 16-pass probe unit) takes the warp-aggregated reductions
+    // --- splat strategy per genome: a compact attractor (its 16-pass probe unit's points share
+    // their bins with many others) takes the warp-aggregated reductions
     if (d->splat == RF_SPLAT_AUTO) {
         constexpr uint32_t kProbe = 16;
         for (auto& it : b->items) {
@@ -308,14 +308,15 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
         cudaMemsetAsync(b->queue, 0, sizeof(unsigned int), b->stream);
         e = launch_batch((int)b->threads, (int)b->slots, args_for(b), b->stream, nullptr);
         for (uint32_t i = 0; i < n && e == cudaSuccess; i++)
-            e = launch_stats(b->items[i].bins, b->items[i].W, b->items[i].H, b->stats + 3 * i, b->stream);
+            e = launch_hit_moments(b->items[i].hits, b->items[i].W, b->items[i].H, b->stats + 3 * i, b->stream);
         std::vector<double> st(3 * (size_t)n);
         if (e == cudaSuccess) e = cudaMemcpyAsync(st.data(), b->stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
         if (e != cudaSuccess) return bail(cuda_err(e, "splat probe"));
-        // points drawn per occupied bin (opacity-weighted): large for a compact attractor
+        // sum h^2 / sum h = the mean count of the bin a probe point fell into: about 1 + points /
+        // bins for a spread attractor, large where a warp's points pile into the same few bins
         for (uint32_t i = 0; i < n; i++)
-            b->items[i].splat = st[3 * i] >= kCompactDensity * std::max(1.0, st[3 * i + 2]) ? 1u : 0u;
+            b->items[i].splat = st[3 * i + 1] >= kCompactShare * std::max(1.0, st[3 * i]) ? 1u : 0u;
     } else {
         for (auto& it : b->items) it.splat = d->splat == RF_SPLAT_WARP ? 1u : 0u;
     }

@@ -335,6 +335,31 @@ cudaError_t launch_stats(const float4* in, uint32_t w, uint32_t h, double* out3,
     return cudaGetLastError();
 }
 
+// out2 = (sum h, sum h^2) of a hit-count histogram, FP64; out2 must start at zero
+__global__ void hit_moments_kernel(const uint32_t* __restrict__ hits, size_t n, double* out2) {
+    double s = 0.0, q = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double v = (double)hits[i];
+        s += v;
+        q += v * v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, o);
+        q += __shfl_down_sync(0xffffffffu, q, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out2, s);
+        atomicAdd(out2 + 1, q);
+    }
+}
+
+cudaError_t launch_hit_moments(const uint32_t* hits, uint32_t w, uint32_t h, double* out2, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(out2, 0, 2 * sizeof(double), st);
+    if (e != cudaSuccess) return e;
+    hit_moments_kernel<<<256, 256, 0, st>>>(hits, (size_t)w * h, out2);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_tonemap(const float4* in, uint32_t w, uint32_t h, uint32_t ss, float gamma, float brightness,
                            float vibrancy, float k2, const double* stats, float4* out_f32, uchar4* out8,
                            cudaStream_t st) {

@@ -62,6 +62,8 @@ void density_weights(int radius, int min_radius, std::vector<float>& out);
 cudaError_t launch_density_resident(const float4* in, uint32_t w, uint32_t h, int radius, int min_radius,
                                     float curve, float4* out, uint8_t* radius_scratch, const float* weights,
                                     cudaStream_t st);
+// (sum h, sum h^2) of a hit-count histogram in FP64 (the splat autotuner's concentration measure)
+cudaError_t launch_hit_moments(const uint32_t* hits, uint32_t w, uint32_t h, double* out2, cudaStream_t st);
 cudaError_t launch_stats(const float4* in, uint32_t w, uint32_t h, double* out3, cudaStream_t st);
 cudaError_t launch_tonemap(const float4* in, uint32_t w, uint32_t h, uint32_t ss, float gamma, float brightness,
                            float vibrancy, float k2, const double* stats, float4* out_f32, uchar4* out8,
