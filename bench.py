@@ -46,6 +46,10 @@ WORKLOADS = {
                        "1024x768 + 64 random genomes (2-16 xforms) at 512x512 / 1024x768 / 1920x1080, 200 spp, "
                        "one persistent graph-captured launch",
                   genome=None, out=(1024, 768), ss=1, points=None, de=(9, 0, 0.4), image=True),
+    "learned": dict(name="learned density estimation: U-Net (32-48-64-96, BF16 on tcgen05) trained on 2000 genomes "
+                         "(seeds 1000-2999, 2-12 xforms) at 512x512, 16 spp -> 1000-spp adaptive-DE target; 200 "
+                         "held-out genomes; 1080p frame time, learned vs plain",
+                    genome=None, out=(1920, 1080), ss=1, points=None, de=(9, 0, 0.4), image=True),
 }
 FUSE = 20
 WL = WORKLOADS["frame1080"]
@@ -460,6 +464,121 @@ def run_batch(args):
     return 0
 
 
+def run_learned(args):
+    import torch
+    import refrakt_gb300 as R
+    from refrakt_gb300 import learned as LD
+
+    ws, rank, local = _dist()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    R.build()
+    comp = R.FlameCompiler()
+    log = lambda m: print(m, file=sys.stderr, flush=True)
+    S = 512
+    n_train, n_test = args.learned_train, args.learned_test
+    tr_seeds = list(range(1000, 1000 + n_train))
+    te_seeds = list(range(3000, 3000 + n_test))
+    t0 = time.perf_counter()
+    tr = [LD.genome(R, comp, s, S, S) for s in tr_seeds]
+    te = [LD.genome(R, comp, s, S, S) for s in te_seeds]
+    feats = torch.empty(n_train, S, S, 8, dtype=torch.bfloat16, device="cuda")
+    targets = torch.empty(n_train, S, S, 3, device="cuda")
+    LD.render_features(tr, S, S, 16, [s * 7 + 1 for s in tr_seeds], feats)
+    LD.render_images(tr, S, S, 1000, [s * 7 + 2 for s in tr_seeds], targets)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    log("training data: %d pairs in %.1f s" % (n_train, t_data))
+    net = R.Denoiser(4 * S * S, seed=7)
+    t0 = time.perf_counter()
+    losses = LD.train(net, feats, targets, args.learned_steps, batch=4, lr=1e-3, log=log)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del feats, targets
+
+    # held-out evaluation against a 4000-spp adaptive-DE reference
+    ref = torch.empty(n_test, S, S, 3, device="cuda")
+    LD.render_images(te, S, S, 4000, [s * 7 + 3 for s in te_seeds], ref)
+    spps = [16, 32, 64, 125, 250, 500, 1000]
+    img = torch.empty(n_test, S, S, 3, device="cuda")
+    plain = {}
+    for k, spp in enumerate(spps):
+        LD.render_images(te, S, S, spp, [s * 7 + 10 + k for s in te_seeds], img)
+        plain[spp] = float(LD.l1(img, ref).mean())
+    f16 = torch.empty(n_test, S, S, 8, dtype=torch.bfloat16, device="cuda")
+    learned = {}
+    per_img = {}
+    for spp in (16, 32, 64):
+        LD.render_features(te, S, S, spp, [s * 7 + 20 + spp for s in te_seeds], f16)
+        LD.infer_all(net, f16, img)
+        e = LD.l1(img, ref)
+        learned[spp] = float(e.mean())
+        per_img[spp] = e
+    equiv = {spp: LD.plain_equivalent_spp(spps, [plain[x] for x in spps], learned[spp]) for spp in learned}
+    # 1080p frame, seconds per frame: plain (1000 spp + adaptive DE + tonemap) vs learned (16 spp + U-Net)
+    W1, H1 = 1920, 1080
+    f1 = LD.genome(R, comp, 1, W1, H1)
+    inf = R.Denoiser(W1 * H1, seed=0)
+    inf.set_params(net.params())
+    out1 = torch.empty(1, H1, W1, 3, device="cuda")
+    fe1 = torch.empty(1, H1, W1, 8, dtype=torch.bfloat16, device="cuda")
+
+    def learned_frame():
+        LD.render_features([f1], W1, H1, 16, [5], fe1)
+        inf.infer(fe1, out1)
+        torch.cuda.synchronize()
+
+    def plain_frame():
+        LD.render_images([f1], W1, H1, 1000, [5], out1)
+        torch.cuda.synchronize()
+
+    times = {}
+    with ClockSampler(local) as clk:
+        for name, fn in (("learned", learned_frame), ("plain", plain_frame)):
+            for _ in range(args.warmup):
+                fn()
+            ts = []
+            for _ in range(args.steps):
+                t = time.perf_counter()
+                fn()
+                ts.append(time.perf_counter() - t)
+            times[name] = statistics.median(ts)
+    # the fallback policy on the held-out set: split estimate from two 16-spp runs
+    lr_ = LD.LearnedRenderer(net, spp=16, bound=args.learned_bound)
+    fallbacks, est_err = 0, []
+    for k in range(min(32, n_test)):
+        out, est, fb = lr_.render(te[k], S, S, seed=te_seeds[k] * 7 + 40)
+        fallbacks += int(fb)
+        est_err.append((est, float((out - ref[k]).abs().mean())))
+    line = {
+        "metric": "s per 1080p frame at fixed L1 err, learned vs plain DE", "value": times["learned"],
+        "unit": "s/frame", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": times["learned"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16", "data": "synthetic genomes rendered by the library (seeds 1000-2999 train, 3000-%d test)" %
+                                  (3000 + n_test - 1),
+        "config": {"workload": CONFIG_NAME, "train_genomes": n_train, "test_genomes": n_test,
+                   "train_steps": args.learned_steps, "batch": 4, "resolution": [S, S],
+                   "params": net.num_params(), "input_spp": 16, "target_spp": 1000, "reference_spp": 4000},
+        "plain_s_per_frame": times["plain"],
+        "speedup_vs_plain": times["plain"] / times["learned"],
+        "l1_plain_by_spp": plain, "l1_learned_by_input_spp": learned,
+        "plain_spp_equivalent": equiv,
+        "iteration_ratio_at_plain_1000spp_error": None,
+        "learned_reaches_plain_1000spp_error": learned[16] <= plain[1000],
+        "train": {"data_s": t_data, "train_s": t_train, "loss_first": losses[0], "loss_last": losses[-1]},
+        "fallback": {"bound": args.learned_bound, "frames": min(32, n_test), "fallbacks": fallbacks,
+                     "estimate_vs_true_l1": est_err[:8]},
+        "gpu_launches": None,
+        "e2e": {"value": times["learned"], "unit": "s/frame", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "clocks": clk.summary(),
+    }
+    best = min(learned, key=lambda k: learned[k])
+    line["iteration_ratio_at_plain_1000spp_error"] = (1000.0 / best) if learned[best] <= plain[1000] else None
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -472,6 +591,10 @@ def main():
     ap.add_argument("--steps-per-launch", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--splat", default="auto", choices=["auto", "global", "warp"])
+    ap.add_argument("--learned-train", type=int, default=2000)
+    ap.add_argument("--learned-test", type=int, default=200)
+    ap.add_argument("--learned-steps", type=int, default=2000)
+    ap.add_argument("--learned-bound", type=float, default=0.02)
     ap.add_argument("--workload", default="frame1080", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     select_workload(args.workload)
@@ -479,6 +602,8 @@ def main():
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "learned":
+        return run_learned(args)
     return run_native(args)
 
 

@@ -277,6 +277,7 @@ typedef struct {
     int32_t  use_graph;         /* 1: capture the whole batch in a CUDA graph */
     int32_t  device;
     int32_t  splat;             /* rf_splat; AUTO chooses per genome from its probe histogram */
+    int32_t  image_f32;         /* 1: keep each tonemapped image in FP32 too (rf_batch_image_f32) */
 } rf_batch_desc;
 RF_API int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc* d, rf_batch** out);
 /* Enqueues one whole batch (clear, draw, DE, tonemap) on the batch's own stream. */
@@ -290,6 +291,11 @@ RF_API int rf_batch_image(rf_batch* b, uint32_t i, uint8_t* out_rgba8);
 RF_API int rf_batch_bins(rf_batch* b, uint32_t i, float** rgba, uint32_t** hits, uint32_t* width, uint32_t* height);
 /* Copies item i's bins to host memory (either pointer may be NULL). */
 RF_API int rf_batch_read_bins(rf_batch* b, uint32_t i, float* host_rgba, uint32_t* host_hits);
+/* Item i's FP32 tonemapped image, RGBA float [height][width][4], to device or host memory
+   (the batch must be created with image_f32). */
+RF_API int rf_batch_image_f32(rf_batch* b, uint32_t i, float* dst_rgba);
+/* Learned-DE input features of item i's bins (rf_denoiser_features) into device memory. */
+RF_API int rf_batch_features(rf_batch* b, uint32_t i, float k2, void* dst_bf16);
 /* The autotuned shape: walkers per unit, number of units, drawing passes per unit. */
 RF_API int rf_batch_info(const rf_batch* b, uint32_t* cta_slots, uint32_t* units, uint32_t* unit_passes);
 /* The splat strategy chosen for item i (RF_SPLAT_GLOBAL or RF_SPLAT_WARP); -1 for a bad index. */

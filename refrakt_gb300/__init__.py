@@ -71,7 +71,7 @@ class BatchItem(ctypes.Structure):
 class BatchDesc(ctypes.Structure):
     _fields_ = [("fuse_passes", ctypes.c_uint32), ("cta_slots", ctypes.c_uint32), ("unit_passes", ctypes.c_uint32),
                 ("density_estimation", ctypes.c_int32), ("k2", ctypes.c_float), ("use_graph", ctypes.c_int32),
-                ("device", ctypes.c_int32), ("splat", ctypes.c_int32)]
+                ("device", ctypes.c_int32), ("splat", ctypes.c_int32), ("image_f32", ctypes.c_int32)]
 
 
 class DenoiserDesc(ctypes.Structure):
@@ -145,6 +145,8 @@ _SIGS = {
     "rf_batch_read_bins": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rf_batch_info": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
                        ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
+    "rf_batch_image_f32": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),
+    "rf_batch_features": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_float, ctypes.c_void_p], ctypes.c_int),
     "rf_batch_splat": ([ctypes.c_void_p, ctypes.c_uint32], ctypes.c_int),
     "rf_batch_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "rf_gemm_bf16": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 6 +
@@ -427,7 +429,7 @@ class Batch:
     (flame, width, height, points, seed, supersample) tuples."""
 
     def __init__(self, items, fuse_passes=20, cta_slots=0, unit_passes=0, density_estimation=True, k2=0.0,
-                 use_graph=True, device=0, splat=0):
+                 use_graph=True, device=0, splat=0, image_f32=False):
         arr = (BatchItem * len(items))()
         self.sizes = []
         self._flames = [it[0] for it in items]  # keep the genomes alive as long as the batch
@@ -436,7 +438,8 @@ class Batch:
             ss = it[5] if len(it) > 5 else 1
             arr[i] = BatchItem(flame._h, w, h, ss, points, seed)
             self.sizes.append((w, h, ss))
-        d = BatchDesc(fuse_passes, cta_slots, unit_passes, int(density_estimation), k2, int(use_graph), device, splat)
+        d = BatchDesc(fuse_passes, cta_slots, unit_passes, int(density_estimation), k2, int(use_graph), device, splat,
+                      int(image_f32))
         h = ctypes.c_void_p()
         _check(library().rf_batch_create(arr, len(items), ctypes.byref(d), ctypes.byref(h)))
         self._h = h
@@ -463,6 +466,14 @@ class Batch:
         img = out if out is not None else np.zeros((h, w, 4), np.uint8)
         _check(library().rf_batch_image(self._h, i, img.ctypes.data_as(ctypes.c_void_p)))
         return img
+
+    def image_f32(self, i, out):
+        """Item i's FP32 tonemapped RGBA image into `out` (a [h, w, 4] float32 CUDA tensor or array)."""
+        _check(library().rf_batch_image_f32(self._h, i, _ptr(out)))
+
+    def features(self, i, out, k2=0.0):
+        """Item i's learned-DE input features into `out` (a [h*ss, w*ss, 8] bf16 CUDA tensor)."""
+        _check(library().rf_batch_features(self._h, i, k2, _ptr(out)))
 
     def bins(self, i):
         """Host copies of item i's RGBA sums (H, W, 4 float32) and hit counts (H, W uint32)."""
@@ -514,12 +525,20 @@ def probe_xform(flame, xform, xyc, rng, out, first_run=False, stream=None):
 GEMM_STORE_F32, GEMM_STORE_BF16, GEMM_ATOMIC_F32 = 0, 1, 2
 
 
+def _rows_ptr(x):
+    """Device address of a 2-D CUDA tensor whose rows are contiguous (any row stride)."""
+    if x.dim() != 2 or not x.is_cuda or x.stride(1) != 1:
+        raise ValueError("expected a 2-D CUDA tensor with contiguous rows")
+    return ctypes.c_void_p(x.data_ptr())
+
+
 def gemm_bf16(a, b, c, mode=GEMM_STORE_F32, bias=None, relu=False, splits=1, stream=None):
-    """c (+)= a @ b.T on the tensor cores; a (M x K) and b (N x K) bf16 CUDA tensors."""
+    """c (+)= a @ b.T on the tensor cores; a (M x K) and b (N x K) bf16 CUDA tensors with
+    contiguous rows (row strides multiples of 8 elements)."""
     M, K = a.shape
     N = b.shape[0]
-    _check(library().rf_gemm_bf16(_ptr(a), _ptr(b), _ptr(c), M, N, K, a.stride(0), b.stride(0), c.stride(0), mode,
-                                  _ptr(bias), int(relu), splits, _stream(stream)))
+    _check(library().rf_gemm_bf16(_rows_ptr(a), _rows_ptr(b), _rows_ptr(c), M, N, K, a.stride(0), b.stride(0),
+                                  c.stride(0), mode, _ptr(bias), int(relu), splits, _stream(stream)))
 
 
 class Denoiser:

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "batch.h"
+#include "denoise_ops.h"
 #include "handles.h"
 #include "kernels.h"
 
@@ -30,6 +31,7 @@ struct Item {
     uint32_t* hits = nullptr;
     float4* de = nullptr;
     uchar4* img = nullptr;
+    float4* img_f32 = nullptr;  // FP32 tonemapped image (rf_batch_desc.image_f32)
     float4* palette = nullptr;
     uint32_t* dprog = nullptr;
     uint32_t splat = 0;       // warp-aggregated splat for this genome
@@ -83,7 +85,7 @@ void destroy_batch(rf_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     for (auto& it : b->items) {
-        void* ptrs[] = {it.bins, it.hits, it.de, it.img, it.palette, it.dprog, it.rad, it.dw};
+        void* ptrs[] = {it.bins, it.hits, it.de, it.img, it.img_f32, it.palette, it.dprog, it.rad, it.dw};
         for (void* p : ptrs) if (p) cudaFree(p);
     }
     void* ptrs[] = {b->table, b->dinst, b->dunits, b->queue, b->counters, b->stats};
@@ -196,7 +198,7 @@ int enqueue(rf_batch* b) {
             if (e != cudaSuccess) return cuda_err(e, "batch stats");
             stt = b->stats + 3 * i;
         }
-        e = launch_tonemap(src, it.W, it.H, it.ss, it.gamma, it.brightness, it.vibrancy, b->d.k2, stt, nullptr, it.img, st);
+        e = launch_tonemap(src, it.W, it.H, it.ss, it.gamma, it.brightness, it.vibrancy, b->d.k2, stt, it.img_f32, it.img, st);
         if (e != cudaSuccess) return cuda_err(e, "batch tonemap");
     }
     return RF_OK;
@@ -253,6 +255,8 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
             if (e == cudaSuccess) e = cudaMemcpy(it.dw, wts.data(), wts.size() * sizeof(float), cudaMemcpyHostToDevice);
         }
         if (e == cudaSuccess) e = cudaMalloc((void**)&it.img, (size_t)items[i].width * items[i].height * sizeof(uchar4));
+        if (e == cudaSuccess && d->image_f32)
+            e = cudaMalloc((void**)&it.img_f32, (size_t)items[i].width * items[i].height * sizeof(float4));
         if (e == cudaSuccess) e = cudaMalloc((void**)&it.palette, 256 * sizeof(float4));
         if (e == cudaSuccess) e = cudaMalloc((void**)&it.dprog, it.prog.size() * 4);
         if (e == cudaSuccess) e = cudaMemcpy(it.palette, f->g.palette, 256 * sizeof(float4), cudaMemcpyHostToDevice);
@@ -418,6 +422,32 @@ int rf_batch_read_bins(rf_batch* b, uint32_t i, float* host_rgba, uint32_t* host
 int rf_batch_splat(const rf_batch* b, uint32_t i) {
     if (!b || i >= b->items.size()) return -1;
     return b->items[i].splat ? RF_SPLAT_WARP : RF_SPLAT_GLOBAL;
+}
+
+int rf_batch_image_f32(rf_batch* b, uint32_t i, float* dst_rgba) {
+    if (!b || i >= b->items.size() || !dst_rgba) return fail(RF_ERR_INVALID_ARG, "rf_batch_image_f32: bad arguments");
+    const Item& it = b->items[i];
+    if (!it.img_f32) return fail(RF_ERR_INVALID_ARG, "rf_batch_image_f32: batch created without image_f32");
+    cudaSetDevice(b->device);
+    cudaError_t e = cudaMemcpyAsync(dst_rgba, it.img_f32, (size_t)it.desc.width * it.desc.height * sizeof(float4),
+                                    cudaMemcpyDefault, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return cuda_err(e, "rf_batch_image_f32");
+    return RF_OK;
+}
+
+int rf_batch_features(rf_batch* b, uint32_t i, float k2, void* dst_bf16) {
+    if (!b || i >= b->items.size() || !dst_bf16) return fail(RF_ERR_INVALID_ARG, "rf_batch_features: bad arguments");
+    const Item& it = b->items[i];
+    cudaSetDevice(b->device);
+    cudaError_t e = cudaSuccess;
+    if (!(k2 > 0.0f)) e = launch_stats(it.bins, it.W, it.H, b->stats + 3 * i, b->stream);
+    if (e == cudaSuccess)
+        e = launch_features(it.bins, (uint64_t)it.W * it.H, k2, b->stats + 3 * i,
+                            static_cast<__nv_bfloat16*>(dst_bf16), b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return cuda_err(e, "rf_batch_features");
+    return RF_OK;
 }
 
 int rf_batch_info(const rf_batch* b, uint32_t* cta_slots, uint32_t* units, uint32_t* unit_passes) {

@@ -1,0 +1,116 @@
+"""Learned density estimation: data generation, training and evaluation around the C-ABI
+denoiser (rf_denoiser_*), with the plain adaptive-DE path as fallback and judge.
+
+The renderer generates its own training pairs: for each random genome, the features of a
+short-run histogram (16 samples per pixel, no density estimation) and the converged target (the
+1000-spp adaptive-DE tonemapped image) — both through the batched persistent launch.  Training
+and inference run the library's own tensor-core kernels; PyTorch only holds device buffers.
+
+A frame rendered on the learned path carries an error estimate: two independent short runs are
+denoised, and half the mean absolute difference of the two outputs estimates the error of their
+average.  Frames whose estimate exceeds the bound are rendered on the plain path instead.
+"""
+import math
+import time
+
+import numpy as np
+
+from . import Batch, Denoiser, SYNTH_RANDOM, Flame
+
+DE = (9, 0, 0.4)  # adaptive DE of the plain path: max radius, min radius, curve
+
+
+def genome(R, comp, seed, w, h):
+    """A training / held-out genome: 2-12 xforms by seed, with a final xform, 3 random
+    variations per xform from the implemented set, affine coefficients in [-1.2, 1.2]."""
+    f = Flame.synthesize(comp, SYNTH_RANDOM, seed, w, h, n_xforms=2 + seed % 11, final_xform=True)
+    f.set_estimator(*DE)
+    return f
+
+
+def render_features(flames, w, h, spp, seeds, out, device=0, chunk=256):
+    """Features [len(flames), h, w, 8] bf16 of spp-sample histograms (no DE) into `out`."""
+    for c0 in range(0, len(flames), chunk):
+        part = flames[c0:c0 + chunk]
+        b = Batch([(f, w, h, spp * w * h, s) for f, s in zip(part, seeds[c0:c0 + chunk])],
+                  density_estimation=False, device=device)
+        b.run()
+        b.sync()
+        for i in range(len(part)):
+            b.features(i, out[c0 + i])
+        b.close()
+
+
+def render_images(flames, w, h, spp, seeds, out, device=0, chunk=256, de=True):
+    """Tonemapped RGB [len(flames), h, w, 3] float32 of spp-sample renders (adaptive DE) into `out`."""
+    import torch
+    tmp = torch.empty(h, w, 4, device=out.device)
+    for c0 in range(0, len(flames), chunk):
+        part = flames[c0:c0 + chunk]
+        b = Batch([(f, w, h, spp * w * h, s) for f, s in zip(part, seeds[c0:c0 + chunk])],
+                  density_estimation=de, image_f32=True, device=device)
+        b.run()
+        b.sync()
+        for i in range(len(part)):
+            b.image_f32(i, tmp)
+            out[c0 + i].copy_(tmp[..., :3])
+        b.close()
+
+
+def l1(a, b):
+    """Mean absolute error per image (RGB in [0, 1])."""
+    return (a - b).abs().flatten(1).mean(1)
+
+
+def train(net, feats, targets, steps, batch=4, lr=1e-3, seed=0, log=None):
+    """Adam on random minibatches of whole images; cosine learning-rate decay to lr / 20."""
+    import torch
+    g = torch.Generator().manual_seed(seed)
+    n = feats.shape[0]
+    losses = []
+    for s in range(steps):
+        idx = torch.randint(0, n, (batch,), generator=g).tolist()
+        f = torch.stack([feats[i] for i in idx])
+        t = torch.stack([targets[i] for i in idx])
+        # random flips keep the attractors' orientation statistics symmetric
+        if s % 2:
+            f, t = f.flip(2).contiguous(), t.flip(2).contiguous()
+        a = lr * (0.05 + 0.95 * 0.5 * (1 + math.cos(math.pi * s / max(1, steps))))
+        losses.append(net.train_step(f, t, a))
+        if log and (s % 100 == 0 or s == steps - 1):
+            log("step %d loss %.5f lr %.2e" % (s, losses[-1], a))
+    return losses
+
+
+def infer_all(net, feats, out, batch=4):
+    for i in range(0, feats.shape[0], batch):
+        net.infer(feats[i:i + batch].contiguous(), out[i:i + batch])
+
+
+def plain_equivalent_spp(spps, errs, e):
+    """The plain path's samples per pixel at error e, by log-log interpolation of its curve."""
+    ls, le = np.log(np.asarray(spps, float)), np.log(np.asarray(errs, float))
+    order = np.argsort(le)
+    return float(np.exp(np.interp(math.log(e), le[order], ls[order])))
+
+
+class LearnedRenderer:
+    """The learned path for one frame with its fallback: two short runs of `spp` samples per
+    pixel are denoised; if half their mean absolute difference exceeds `bound`, the frame is
+    rendered on the plain path (`plain_spp`, adaptive DE) instead."""
+
+    def __init__(self, net, spp=16, bound=0.02, plain_spp=1000, device=0):
+        self.net, self.spp, self.bound, self.plain_spp, self.device = net, spp, bound, plain_spp, device
+
+    def render(self, flame, w, h, seed=0):
+        import torch
+        feats = torch.empty(2, h, w, 8, dtype=torch.bfloat16, device="cuda")
+        render_features([flame, flame], w, h, self.spp, [seed, seed + 1], feats, self.device)
+        out = torch.empty(2, h, w, 3, device="cuda")
+        self.net.infer(feats, out)
+        est = 0.5 * float((out[0] - out[1]).abs().mean())
+        if est <= self.bound:
+            return 0.5 * (out[0] + out[1]), est, False
+        img = torch.empty(1, h, w, 3, device="cuda")
+        render_images([flame], w, h, self.plain_spp, [seed], img, self.device)
+        return img[0], est, True
