@@ -172,7 +172,9 @@ RF_API int  rf_needs_warmup(const rf_sim* s, const rf_flame* f);
    jitter, random colours) followed by num_passes passes, nothing drawn. */
 RF_API int  rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_width);
 
-/* Splat strategy for rf_draw_to_bins. */
+/* Splat strategy for rf_draw_to_bins: one L2 reduction per point (GLOBAL), warp-aggregated
+   reductions of the points that share a bin (WARP), or per warp and pass the aggregated form
+   when a cheap test finds two lanes sharing a bin (AUTO, the default). */
 enum rf_splat { RF_SPLAT_AUTO = 0, RF_SPLAT_GLOBAL = 1, RF_SPLAT_WARP = 2 };
 /* flame::draw_to_bins(bins, bins_width, num_iter) (flame.cpp:283-330): num_iter passes over
    every walker, drawing into caller-owned device bins.  bins_hits may be NULL.  When `drawn`
@@ -294,7 +296,8 @@ RF_API int rf_batch_read_bins(rf_batch* b, uint32_t i, float* host_rgba, uint32_
 /* Item i's FP32 tonemapped image, RGBA float [height][width][4], to device or host memory
    (the batch must be created with image_f32). */
 RF_API int rf_batch_image_f32(rf_batch* b, uint32_t i, float* dst_rgba);
-/* Learned-DE input features of item i's bins (rf_denoiser_features) into device memory. */
+/* Learned-DE input features of item i's bins (rf_denoiser_features) into device memory; the
+   base channels carry the item's FP32 image when the batch keeps one (image_f32, supersample 1). */
 RF_API int rf_batch_features(rf_batch* b, uint32_t i, float k2, void* dst_bf16);
 /* The autotuned shape: walkers per unit, number of units, drawing passes per unit. */
 RF_API int rf_batch_info(const rf_batch* b, uint32_t* cta_slots, uint32_t* units, uint32_t* unit_passes);
@@ -349,10 +352,12 @@ RF_API int rf_denoiser_set_params(rf_denoiser* d, const float* host, size_t coun
 /* Gradients of the last train_step, same layout as the parameters. */
 RF_API int rf_denoiser_gradients(rf_denoiser* d, float* host, size_t cap);
 /* Features of a histogram (bins float4 RGBA sums, width x height): [log10(1 + a k2),
-   rgb * log10(1 + a k2) / a, 0 x 4] as bf16; k2 <= 0 takes W*H / sum(a) (FP64 reduction). */
-RF_API int rf_denoiser_features(const float* bins_rgba, uint32_t width, uint32_t height, float k2, void* out_bf16,
-                                void* stream);
-/* out_rgb = clamp(net(feats), 0, 1). */
+   rgb * log10(1 + a k2) / a, base.rgb, 0] as bf16; k2 <= 0 takes W*H / sum(a) (FP64
+   reduction).  base_rgba (may be NULL) is the plain path's FP32 tonemapped image of the same
+   histogram (rf_tonemap out_f32): the network predicts a residual on it. */
+RF_API int rf_denoiser_features(const float* bins_rgba, uint32_t width, uint32_t height, float k2,
+                                const float* base_rgba, void* out_bf16, void* stream);
+/* out_rgb = clamp(base + net(feats), 0, 1). */
 RF_API int rf_denoiser_infer(rf_denoiser* d, const void* feats, uint32_t n, uint32_t h, uint32_t w, float* out_rgb);
 /* One Adam step (lr; betas 0.9, 0.999; eps 1e-8) on the mean L1 loss against target_rgb. */
 RF_API int rf_denoiser_train_step(rf_denoiser* d, const void* feats, const float* target_rgb, uint32_t n, uint32_t h,

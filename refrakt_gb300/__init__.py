@@ -161,7 +161,7 @@ _SIGS = {
     "rf_denoiser_set_params": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t], ctypes.c_int),
     "rf_denoiser_gradients": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t], ctypes.c_int),
     "rf_denoiser_features": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_void_p,
-                              ctypes.c_void_p], ctypes.c_int),
+                              ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rf_denoiser_infer": ([ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 3 + [ctypes.c_void_p], ctypes.c_int),
     "rf_denoiser_train_step": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 3 +
                                [ctypes.c_float, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
@@ -600,8 +600,8 @@ class Denoiser:
         return loss.value
 
 
-def denoiser_features(bins_rgba, width, height, out, k2=0.0, stream=None):
-    _check(library().rf_denoiser_features(_ptr(bins_rgba), width, height, k2, _ptr(out), _stream(stream)))
+def denoiser_features(bins_rgba, width, height, out, k2=0.0, base=None, stream=None):
+    _check(library().rf_denoiser_features(_ptr(bins_rgba), width, height, k2, _ptr(base), _ptr(out), _stream(stream)))
 
 
 def write_png(path, rgba8):

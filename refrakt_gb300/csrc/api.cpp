@@ -80,7 +80,7 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.seed = s->d.seed;
         a.first_run = (first_run && done == 0) ? 1 : 0;
         a.draw = draw ? 1 : 0;
-        a.splat = s->splat == RF_SPLAT_WARP ? 1 : 0;
+        a.splat = s->splat == RF_SPLAT_WARP ? 1 : (s->splat == RF_SPLAT_GLOBAL ? 0 : 2);
         if (ss) memcpy(a.ss, ss, sizeof(a.ss));
         a.W = W;
         a.H = H;

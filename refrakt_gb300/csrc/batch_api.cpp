@@ -443,7 +443,7 @@ int rf_batch_features(rf_batch* b, uint32_t i, float k2, void* dst_bf16) {
     cudaError_t e = cudaSuccess;
     if (!(k2 > 0.0f)) e = launch_stats(it.bins, it.W, it.H, b->stats + 3 * i, b->stream);
     if (e == cudaSuccess)
-        e = launch_features(it.bins, (uint64_t)it.W * it.H, k2, b->stats + 3 * i,
+        e = launch_features(it.bins, (uint64_t)it.W * it.H, k2, b->stats + 3 * i, it.ss == 1 ? it.img_f32 : nullptr,
                             static_cast<__nv_bfloat16*>(dst_bf16), b->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) return cuda_err(e, "rf_batch_features");

@@ -9,6 +9,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <random>
 #include <string>
@@ -235,7 +236,7 @@ int backward(rf_denoiser* D, const __nv_bfloat16* input, const float* target, fl
         const __nv_bfloat16* dztp;
         uint32_t ldz;
         if (i == D->out_conv) {
-            e = launch_l1_head(D->z, c.b, target, P0, D->dpred, D->dpred_t, ldp, c.gb, D->loss, st);
+            e = launch_l1_head(D->z, c.b, input, target, P0, D->dpred, D->dpred_t, ldp, c.gb, D->loss, st);
             if (e != cudaSuccess) return cuda_fail(e, "l1 head");
             dzp = D->dpred;
             dztp = D->dpred_t;
@@ -358,10 +359,11 @@ int rf_denoiser_create(const rf_denoiser_desc* desc, rf_denoiser** out) {
         std::vector<float> hw(nw);
         std::normal_distribution<float> nd(0.0f, std::sqrt(2.0f / (float)c.K()));
         for (size_t k = 0; k < nw; k++) hw[k] = nd(gen);
-        if (c.taps == 9 && c.src_a < 0)  // network input: zero the 4 padding channels' weights
+        if (c.taps == 9 && c.src_a < 0)  // network input: zero the padding channel's weights
             for (uint32_t co = 0; co < c.cout; co++)
-                for (uint32_t t = 0; t < 9; t++)
-                    for (uint32_t ci = 4; ci < kIn; ci++) hw[(size_t)co * c.K() + t * kIn + ci] = 0.0f;
+                for (uint32_t t = 0; t < 9; t++) hw[(size_t)co * c.K() + t * kIn + kIn - 1] = 0.0f;
+        if (c.taps == 1)  // the output layer starts at zero: the first prediction is the plain image
+            std::fill(hw.begin(), hw.end(), 0.0f);
         if (e == cudaSuccess) e = dalloc(D, &c.w, nw);
         if (e == cudaSuccess) e = dalloc(D, &c.gw, nw);
         if (e == cudaSuccess) e = dalloc(D, &c.mw, nw);
@@ -484,8 +486,8 @@ int rf_denoiser_set_params(rf_denoiser* D, const float* host, size_t count) {
     return refresh_bf16(D);
 }
 
-int rf_denoiser_features(const float* bins_rgba, uint32_t width, uint32_t height, float k2, void* out_bf16,
-                         void* stream) {
+int rf_denoiser_features(const float* bins_rgba, uint32_t width, uint32_t height, float k2, const float* base_rgba,
+                         void* out_bf16, void* stream) {
     if (!bins_rgba || !out_bf16 || !width || !height) return fail(RF_ERR_INVALID_ARG, "rf_denoiser_features: bad arguments");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     double* stats = nullptr;
@@ -496,7 +498,7 @@ int rf_denoiser_features(const float* bins_rgba, uint32_t width, uint32_t height
     }
     if (e == cudaSuccess)
         e = launch_features(reinterpret_cast<const float4*>(bins_rgba), (uint64_t)width * height, k2, stats,
-                            static_cast<__nv_bfloat16*>(out_bf16), st);
+                            reinterpret_cast<const float4*>(base_rgba), static_cast<__nv_bfloat16*>(out_bf16), st);
     if (stats) cudaFreeAsync(stats, st);
     if (e != cudaSuccess) return cuda_fail(e, "rf_denoiser_features");
     return RF_OK;
@@ -508,7 +510,8 @@ int rf_denoiser_infer(rf_denoiser* D, const void* feats, uint32_t n, uint32_t h,
     cudaSetDevice(D->device);
     if (int rc = forward(D, static_cast<const __nv_bfloat16*>(feats), true)) return rc;
     const Conv& oc = D->convs[D->out_conv];
-    cudaError_t e = launch_head(D->z, oc.b, (uint64_t)n * h * w, out_rgb, D->stream);
+    cudaError_t e = launch_head(D->z, oc.b, static_cast<const __nv_bfloat16*>(feats), (uint64_t)n * h * w, out_rgb,
+                                D->stream);
     if (e != cudaSuccess) return cuda_fail(e, "rf_denoiser_infer");
     return RF_OK;
 }

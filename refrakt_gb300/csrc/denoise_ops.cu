@@ -159,13 +159,18 @@ __global__ void avgpool_back_kernel(const float* __restrict__ dy, uint32_t c, ui
     }
 }
 
-// output head: pred = z + bias (z = [P x 3] FP32 from the 1x1 convolution), L1 loss against
-// target [P x 3]; writes d pred = sign(pred - target) / (3P) as bf16 [P x 8] (zero padded) and
-// its transpose [8 x P], the bias gradient and the loss sum
+// the plain path's image carried in feature channels 4..6: the network predicts a residual on it
+__device__ __forceinline__ float base_of(const __nv_bfloat16* __restrict__ feats, uint64_t p, int ch) {
+    return __bfloat162float(feats[p * 8 + 4 + ch]);
+}
+
+// output head: pred = base + z + bias (z = [P x 3] FP32 from the 1x1 convolution), L1 loss
+// against target [P x 3]; writes d pred = sign(pred - target) / (3P) as bf16 [P x 8] (zero
+// padded) and its transpose [8 x P], the bias gradient and the loss sum
 __global__ void l1_head_kernel(const float* __restrict__ z, const float* __restrict__ bias,
-                               const float* __restrict__ target, uint64_t P, __nv_bfloat16* __restrict__ dpred,
-                               __nv_bfloat16* __restrict__ dpred_t, uint32_t ldp, float* __restrict__ dbias,
-                               double* __restrict__ loss) {
+                               const __nv_bfloat16* __restrict__ feats, const float* __restrict__ target, uint64_t P,
+                               __nv_bfloat16* __restrict__ dpred, __nv_bfloat16* __restrict__ dpred_t, uint32_t ldp,
+                               float* __restrict__ dbias, double* __restrict__ loss) {
     const float inv = 1.0f / (3.0f * (float)P);
     float db[3] = {0, 0, 0};
     double ls = 0.0;
@@ -173,7 +178,7 @@ __global__ void l1_head_kernel(const float* __restrict__ z, const float* __restr
         __align__(16) __nv_bfloat16 g8[8];
         for (int q = 0; q < 8; q++) g8[q] = __float2bfloat16_rn(0.0f);
         for (int ch = 0; ch < 3; ch++) {
-            const float d = z[p * 3 + ch] + bias[ch] - target[p * 3 + ch];
+            const float d = base_of(feats, p, ch) + z[p * 3 + ch] + bias[ch] - target[p * 3 + ch];
             ls += fabs((double)d);
             const float g = d > 0.0f ? inv : (d < 0.0f ? -inv : 0.0f);
             db[ch] += g;
@@ -191,11 +196,11 @@ __global__ void l1_head_kernel(const float* __restrict__ z, const float* __restr
     if ((threadIdx.x & 31) == 0) atomicAdd(loss, ls);
 }
 
-// inference head: out = clamp(z + bias, 0, 1)
-__global__ void head_kernel(const float* __restrict__ z, const float* __restrict__ bias, uint64_t P,
-                            float* __restrict__ out) {
+// inference head: out = clamp(base + z + bias, 0, 1)
+__global__ void head_kernel(const float* __restrict__ z, const float* __restrict__ bias,
+                            const __nv_bfloat16* __restrict__ feats, uint64_t P, float* __restrict__ out) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < P * 3; i += (uint64_t)gridDim.x * blockDim.x)
-        out[i] = fminf(fmaxf(z[i] + bias[i % 3], 0.0f), 1.0f);
+        out[i] = fminf(fmaxf(base_of(feats, i / 3, (int)(i % 3)) + z[i] + bias[i % 3], 0.0f), 1.0f);
 }
 
 // Adam on FP32 master weights; refreshes the bf16 copy used as the forward GEMM operand
@@ -227,10 +232,11 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, 
 }
 
 // input features of a histogram (RGBA sums float4 per bin, W x H): 8 bf16 channels
-//   [0] l = log10(1 + a * k2), [1..3] colour * l / a, [4..7] 0
-// — the tonemap's log-density scaling (tonemap.glsl:18-26) without the gamma step
+//   [0] l = log10(1 + a * k2), [1..3] colour * l / a — the tonemap's log-density scaling
+//   (tonemap.glsl:18-26) without the gamma step; [4..6] the plain path's tonemapped RGB of the
+//   same histogram (base, may be null: zeros), on which the network predicts a residual; [7] 0
 __global__ void features_kernel(const float4* __restrict__ bins, uint64_t n, float k2, const double* __restrict__ stats,
-                                __nv_bfloat16* __restrict__ out) {
+                                const float4* __restrict__ base, __nv_bfloat16* __restrict__ out) {
     const float k = k2 > 0.0f ? k2 : (float)((double)n / fmax(stats[0], 1e-30));
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const float4 c = bins[i];
@@ -244,7 +250,11 @@ __global__ void features_kernel(const float4* __restrict__ bins, uint64_t n, flo
         f[1] = __float2bfloat16_rn(c.x * s);
         f[2] = __float2bfloat16_rn(c.y * s);
         f[3] = __float2bfloat16_rn(c.z * s);
-        for (int q = 4; q < 8; q++) f[q] = __float2bfloat16_rn(0.0f);
+        const float4 bb = base ? base[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        f[4] = __float2bfloat16_rn(bb.x);
+        f[5] = __float2bfloat16_rn(bb.y);
+        f[6] = __float2bfloat16_rn(bb.z);
+        f[7] = __float2bfloat16_rn(0.0f);
         *reinterpret_cast<uint4*>(out + i * 8) = *reinterpret_cast<const uint4*>(f);
     }
 }
@@ -297,14 +307,16 @@ cudaError_t launch_avgpool_back(const float* dy, uint32_t c, uint32_t n, uint32_
     return cudaGetLastError();
 }
 
-cudaError_t launch_l1_head(const float* z, const float* bias, const float* target, uint64_t P, __nv_bfloat16* dpred,
-                           __nv_bfloat16* dpred_t, uint32_t ldp, float* dbias, double* loss, cudaStream_t st) {
-    l1_head_kernel<<<grid_for(P, 256), 256, 0, st>>>(z, bias, target, P, dpred, dpred_t, ldp, dbias, loss);
+cudaError_t launch_l1_head(const float* z, const float* bias, const __nv_bfloat16* feats, const float* target,
+                           uint64_t P, __nv_bfloat16* dpred, __nv_bfloat16* dpred_t, uint32_t ldp, float* dbias,
+                           double* loss, cudaStream_t st) {
+    l1_head_kernel<<<grid_for(P, 256), 256, 0, st>>>(z, bias, feats, target, P, dpred, dpred_t, ldp, dbias, loss);
     return cudaGetLastError();
 }
 
-cudaError_t launch_head(const float* z, const float* bias, uint64_t P, float* out, cudaStream_t st) {
-    head_kernel<<<grid_for(P * 3, 256), 256, 0, st>>>(z, bias, P, out);
+cudaError_t launch_head(const float* z, const float* bias, const __nv_bfloat16* feats, uint64_t P, float* out,
+                        cudaStream_t st) {
+    head_kernel<<<grid_for(P * 3, 256), 256, 0, st>>>(z, bias, feats, P, out);
     return cudaGetLastError();
 }
 
@@ -316,9 +328,9 @@ cudaError_t launch_adam(float* w, const float* g, float* m, float* v, uint32_t n
     return cudaGetLastError();
 }
 
-cudaError_t launch_features(const float4* bins, uint64_t n, float k2, const double* stats, __nv_bfloat16* out,
-                            cudaStream_t st) {
-    features_kernel<<<grid_for(n, 256), 256, 0, st>>>(bins, n, k2, stats, out);
+cudaError_t launch_features(const float4* bins, uint64_t n, float k2, const double* stats, const float4* base,
+                            __nv_bfloat16* out, cudaStream_t st) {
+    features_kernel<<<grid_for(n, 256), 256, 0, st>>>(bins, n, k2, stats, base, out);
     return cudaGetLastError();
 }
 

@@ -21,13 +21,15 @@ cudaError_t launch_split_concat_grad(const float* dx, uint32_t ca, uint32_t cb, 
                                      float* dlow, float* dskip, cudaStream_t st);
 cudaError_t launch_avgpool_back(const float* dy, uint32_t c, uint32_t n, uint32_t h, uint32_t w, float* dx,
                                 cudaStream_t st);
-cudaError_t launch_l1_head(const float* z, const float* bias, const float* target, uint64_t P, __nv_bfloat16* dpred,
-                           __nv_bfloat16* dpred_t, uint32_t ldp, float* dbias, double* loss, cudaStream_t st);
-cudaError_t launch_head(const float* z, const float* bias, uint64_t P, float* out, cudaStream_t st);
+cudaError_t launch_l1_head(const float* z, const float* bias, const __nv_bfloat16* feats, const float* target,
+                           uint64_t P, __nv_bfloat16* dpred, __nv_bfloat16* dpred_t, uint32_t ldp, float* dbias,
+                           double* loss, cudaStream_t st);
+cudaError_t launch_head(const float* z, const float* bias, const __nv_bfloat16* feats, uint64_t P, float* out,
+                        cudaStream_t st);
 cudaError_t launch_adam(float* w, const float* g, float* m, float* v, uint32_t n, float lr, float b1, float b2,
                         float eps, uint32_t t, uint32_t cout, uint32_t K, uint32_t taps, __nv_bfloat16* w16,
                         __nv_bfloat16* wf16, uint32_t ldf, cudaStream_t st);
-cudaError_t launch_features(const float4* bins, uint64_t n, float k2, const double* stats, __nv_bfloat16* out,
-                            cudaStream_t st);
+cudaError_t launch_features(const float4* bins, uint64_t n, float k2, const double* stats, const float4* base,
+                            __nv_bfloat16* out, cudaStream_t st);
 
 }  // namespace rfk

@@ -160,7 +160,8 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) chaos_kernel(const Ch
                     val = make_float4(col.x, col.y, col.z, op);
                     drawn++;
                 }
-                if (A.splat) splat_warp(A.bins, A.hits, bin, val);
+                if (A.splat == 1) splat_warp(A.bins, A.hits, bin, val);
+                else if (A.splat == 2) splat_adaptive(A.bins, A.hits, bin, val);
                 else splat_global(A.bins, A.hits, bin, val);
             }
         }

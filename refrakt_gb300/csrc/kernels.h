@@ -25,7 +25,7 @@ struct ChaosArgs {
     uint64_t seed;
     int first_run;           // pass 0 reads the start points, jitters, draws colours
     int draw;
-    int splat;               // 0: a reduction per point; 1: warp-aggregated (splat.cuh)
+    int splat;               // 0: a reduction per point; 1: warp-aggregated; 2: adaptive (splat.cuh)
     float ss[6];             // screen affine
     uint32_t W, H;
     float4* bins;            // RGBA sums

@@ -11,6 +11,9 @@
 //                  set's lanes (the peer reduction of E. Westphal, "Voting and shuffling to
 //                  optimize atomic operations", GTC 2015), so only their FP32 rounding order
 //                  differs from splat_global; the counts are exact either way.
+//   splat_adaptive — per warp and pass: lane pairs (2i, 2i+1) compare bins with one shuffle;
+//                  the warp takes splat_warp when any pair shares a bin (a compact attractor),
+//                  splat_global otherwise, so spread attractors pay one shuffle and one vote.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -64,6 +67,13 @@ __device__ __forceinline__ void splat_warp(float4* bins, uint32_t* hits, uint32_
         red_add_f32x4(bins + bin, v.x, v.y, v.z, v.w);
         if (hits) red_add_u32x1(hits + bin, (uint32_t)__popc(peers));
     }
+}
+
+// Every lane of the warp must call this.
+__device__ __forceinline__ void splat_adaptive(float4* bins, uint32_t* hits, uint32_t bin, float4 v) {
+    const uint32_t other = __shfl_xor_sync(0xffffffffu, bin, 1);
+    if (__any_sync(0xffffffffu, bin != kNoBin && bin == other)) splat_warp(bins, hits, bin, v);
+    else splat_global(bins, hits, bin, v);
 }
 
 }  // namespace rfk

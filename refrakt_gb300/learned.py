@@ -2,8 +2,9 @@
 denoiser (rf_denoiser_*), with the plain adaptive-DE path as fallback and judge.
 
 The renderer generates its own training pairs: for each random genome, the features of a
-short-run histogram (16 samples per pixel, no density estimation) and the converged target (the
-1000-spp adaptive-DE tonemapped image) — both through the batched persistent launch.  Training
+short-run render (16 samples per pixel: the histogram's log density and colour, and the plain
+path's adaptive-DE image of it, on which the network predicts a residual) and the converged
+target (the 1000-spp adaptive-DE tonemapped image) — both through the batched persistent launch.  Training
 and inference run the library's own tensor-core kernels; PyTorch only holds device buffers.
 
 A frame rendered on the learned path carries an error estimate: two independent short runs are
@@ -29,11 +30,12 @@ def genome(R, comp, seed, w, h):
 
 
 def render_features(flames, w, h, spp, seeds, out, device=0, chunk=256):
-    """Features [len(flames), h, w, 8] bf16 of spp-sample histograms (no DE) into `out`."""
+    """Features [len(flames), h, w, 8] bf16 of spp-sample renders into `out`: the raw histogram's
+    log density and colour, and the plain path's image (adaptive DE + tonemap) of it."""
     for c0 in range(0, len(flames), chunk):
         part = flames[c0:c0 + chunk]
         b = Batch([(f, w, h, spp * w * h, s) for f, s in zip(part, seeds[c0:c0 + chunk])],
-                  density_estimation=False, device=device)
+                  density_estimation=True, image_f32=True, device=device)
         b.run()
         b.sync()
         for i in range(len(part)):

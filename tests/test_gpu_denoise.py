@@ -51,13 +51,24 @@ def torch_unet(layers, params, feats, round_acts=True):
 
 @pytest.fixture(scope="module")
 def net(rk):
-    return rk.Denoiser(4 * 64 * 64, seed=5)
+    d = rk.Denoiser(4 * 64 * 64, seed=5)
+    # random parameters everywhere (the output layer starts at zero after creation)
+    rng = np.random.default_rng(0)
+    p, o = np.zeros(d.num_params(), np.float32), 0
+    for L in d.layers():
+        k = L["taps"] * (L["in_a"] + L["in_b"])
+        p[o:o + L["out"] * k] = rng.normal(0, np.sqrt(2.0 / k), L["out"] * k)
+        o += L["out"] * k
+        p[o:o + L["out"]] = rng.normal(0, 0.05, L["out"])
+        o += L["out"]
+    d.set_params(p)
+    return d
 
 
 def _feats(n, h, w, seed):
     g = torch.Generator(device="cuda").manual_seed(seed)
     f = torch.zeros(n, h, w, 8, device="cuda")
-    f[..., :4] = torch.rand(n, h, w, 4, device="cuda", generator=g)
+    f[..., :7] = torch.rand(n, h, w, 7, device="cuda", generator=g)
     return f.to(torch.bfloat16)
 
 
@@ -76,7 +87,7 @@ def test_forward_matches_torch(rk, net, n, h, w):
     net.infer(f, out)
     torch.cuda.synchronize()
     ref, _ = torch_unet(net.layers(), net.params(), f.float())
-    ref = ref.clamp(0, 1).detach()
+    ref = (f.float()[..., 4:7] + ref).clamp(0, 1).detach()
     err = (out - ref).abs()
     assert float(err.mean()) < 2e-3, float(err.mean())
     assert float(err.max()) < 3e-2, float(err.max())
@@ -90,8 +101,7 @@ def test_gradients_match_autograd(rk, net):
     net.train_step(f, target, 0.0)  # lr 0: gradients only
     got = net.gradients()
     ref, ws = torch_unet(net.layers(), net.params(), f.float())
-    bias_out = ws[-1][1]
-    loss = (ref - target).abs().mean()
+    loss = (f.float()[..., 4:7] + ref - target).abs().mean()
     loss.backward()
     o = 0
     for (w_, b_), L in zip(ws, net.layers()):
@@ -106,6 +116,15 @@ def test_gradients_match_autograd(rk, net):
         assert cos > 0.98, (L, cos)
         assert np.linalg.norm(mine - gw) <= 0.2 * np.linalg.norm(gw) + 1e-6, L
         assert np.allclose(mb, gb, rtol=0.1, atol=0.05 * np.abs(gb).max() + 1e-6), L
+
+
+def test_output_starts_at_the_plain_image(rk):
+    d = rk.Denoiser(64 * 64, seed=2)
+    f = _feats(1, 32, 32, 4)
+    out = torch.zeros(1, 32, 32, 3, device="cuda")
+    d.infer(f, out)
+    torch.cuda.synchronize()
+    assert torch.equal(out, f.float()[..., 4:7].clamp(0, 1))
 
 
 def test_training_reduces_loss(rk):
@@ -131,5 +150,11 @@ def test_features_of_histogram(rk):
     a = b[..., 3]
     l = torch.where(a > 0, torch.log10(1 + a * k2), torch.zeros_like(a))
     s = torch.where(a > 0, l / a, torch.zeros_like(a))
+    base = torch.rand(H, W, 4, device="cuda", generator=g)
+    out2 = torch.zeros_like(out)
+    rk.denoiser_features(bins, W, H, out2, k2=0.0, base=base)
+    torch.cuda.synchronize()
     ref = torch.cat([l[..., None], b[..., :3] * s[..., None], torch.zeros(H, W, 4, device="cuda", dtype=torch.float64)], -1)
     assert torch.allclose(out.double(), ref, rtol=2 ** -7, atol=1e-6)
+    ref[..., 4:7] = base[..., :3].double()
+    assert torch.allclose(out2.double(), ref, rtol=2 ** -7, atol=1e-6)

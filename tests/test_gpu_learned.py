@@ -22,12 +22,12 @@ def test_small_pipeline(rk, compiler):
     net = rk.Denoiser(4 * S * S, seed=3)
     losses = LD.train(net, feats, targets, 300, batch=4, lr=2e-3)
     assert sum(losses[-20:]) / 20 < 0.6 * sum(losses[:20]) / 20
-    # on the training genomes the denoised short run is closer to the target than the plain one
-    short = torch.empty(n, S, S, 3, device="cuda")
-    LD.render_images(fl, S, S, 16, [s + 3 for s in seeds], short)
+    # on the training genomes the denoised short run is closer to the target than the plain
+    # path's image of the same short run (feature channels 4..6)
     den = torch.empty(n, S, S, 3, device="cuda")
     LD.infer_all(net, feats, den)
-    assert float(LD.l1(den, targets).mean()) < float(LD.l1(short, targets).mean())
+    plain = feats.float()[..., 4:7]
+    assert float(LD.l1(den, targets).mean()) < float(LD.l1(plain, targets).mean())
 
 
 @pytest.mark.parametrize("bound,expect_fallback", [(0.0, True), (1.0, False)])
@@ -46,4 +46,4 @@ def test_plain_equivalent_spp():
     spps = [16, 64, 256, 1024]
     errs = [0.16, 0.08, 0.04, 0.02]  # error halves per 4x samples
     assert abs(LD.plain_equivalent_spp(spps, errs, 0.04) - 256) < 1e-6
-    assert abs(LD.plain_equivalent_spp(spps, errs, 0.0565685) - 512) < 1.0
+    assert abs(LD.plain_equivalent_spp(spps, errs, 0.0565685) - 128) < 0.1
