@@ -163,13 +163,20 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _traffic():
-    """DRAM bytes per chaos launch from the committed ncu summary of this workload (or None)."""
+def _profile_figure(workload, key):
+    """A figure ("<key>: <int>") from the committed ncu summary of this workload (or None)."""
+    import re
     try:
-        with open(os.path.join(ROOT, "profiles", "chaos_kernel_1080p.json")) as f:
-            return json.load(f).get("dram_bytes_per_launch")
-    except Exception:
+        with open(os.path.join(ROOT, "profiles", "chaos_kernel_%s.md" % workload)) as f:
+            m = re.search(r"^%s: (\d+)" % re.escape(key), f.read(), re.M)
+        return int(m.group(1)) if m else None
+    except OSError:
         return None
+
+
+def _traffic(workload):
+    """DRAM bytes per chaos launch from the committed ncu summary of this workload (or None)."""
+    return _profile_figure(workload, "dram bytes per launch")
 
 
 def cpu_baseline(genome_xml, seconds=12.0, threads=None):
@@ -245,7 +252,7 @@ def run_native(args):
     cta = args.cta_slots
     walkers = WL.get("walkers") or sms * args.ctas_per_sm * cta
     sim = R.Sim(walkers, cta_slots=cta, cta_threads=args.cta_threads, steps_per_launch=args.steps_per_launch,
-                seed=1000 + rank, device=local)
+                seed=1000 + rank, device=local, specialize={"auto": 0, "on": 1, "off": -1}[args.specialize])
     passes = (POINTS + walkers - 1) // walkers
     launches = (passes + args.steps_per_launch - 1) // args.steps_per_launch
     bins = torch.zeros(H, W, 4, device="cuda")
@@ -325,14 +332,24 @@ def run_native(args):
     bytes_per_point = 20  # payload of the histogram reductions: float4 RGBA + uint32 count
     pts_per_launch = walkers * args.steps_per_launch
     achieved = bytes_per_point * pts_per_launch / (per_launch_ms * 1e-3) / 1e9
-    traffic = _traffic()
+    prof_key = {"frame1080": "1080p"}.get(args.workload, args.workload)
+    traffic = _traffic(prof_key)
+    inst = _profile_figure(prof_key, "thread instructions per point")
+    sms_ = torch.cuda.get_device_properties(local).multi_processor_count
+    issue = None
+    if inst:
+        clk_mhz = (clk.summary() or {}).get("sm_mhz") or 2070.0
+        bound = sms_ * 4 * clk_mhz * 1e6 * 32 / inst / 1e9  # Gpoints/s at one warp instruction per scheduler-cycle
+        issue = {"thread_inst_per_point": inst, "bound_gpoints_s": bound,
+                 "frac": (pts_per_launch / (per_launch_ms * 1e-3) / 1e9) / bound}
     line = {
         "metric": "Gpoints/s histogrammed", "value": value, "unit": "Gpoints/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic genome (seed 1); no dataset",
         "config": {"workload": CONFIG_NAME, "points_per_frame": POINTS, "bins": [W, H], "output": [W_OUT, H_OUT],
                    "genome": GENOME, "walkers": walkers, "cta_slots": cta, "steps_per_launch": args.steps_per_launch,
-                   "passes_per_frame": passes, "fuse_passes": FUSE, "splat": args.splat, "density_estimation": list(DE) if DE else None,
+                   "passes_per_frame": passes, "fuse_passes": FUSE, "splat": args.splat,
+                   "specialized_kernel": sim.specialized(), "density_estimation": list(DE) if DE else None,
                    "l2": "bins %dx%d x 20 B = %.0f MB (L2 129 MB)%s" % (W, H, W * H * 20 / 1e6,
                          "; exceed L2" if W * H * 20 > 129e6 else "; an L2 flush separates frames"),
                    "parallelism": "replicas" if ws > 1 else "single"},
@@ -342,9 +359,9 @@ def run_native(args):
         "e2e": {"value": e2e_value, "unit": "Gpoints/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "s_per_frame": e2e_step / 1e3},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "chaos_kernel", "peak_source": peak_kind,
+                     "traffic": traffic, "kernel": "rfk_chaos_spec" if sim.specialized() else "chaos_kernel", "peak_source": peak_kind,
                      "algorithmic_bytes_per_point": bytes_per_point, "points_per_launch": pts_per_launch,
-                     "launch_ms": per_launch_ms,
+                     "launch_ms": per_launch_ms, "issue": issue,
                      "note": "atomic-reduction payload per point; the chaos game is bound by SM issue and L2 "
                              "reduction throughput, not DRAM"},
         "clocks": clk.summary(),
@@ -591,6 +608,8 @@ def main():
     ap.add_argument("--steps-per-launch", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--splat", default="auto", choices=["auto", "global", "warp"])
+    ap.add_argument("--specialize", default="auto", choices=["auto", "on", "off"],
+                    help="genome-specialised chaos kernel compiled at run time")
     ap.add_argument("--learned-train", type=int, default=2000)
     ap.add_argument("--learned-test", type=int, default=200)
     ap.add_argument("--learned-steps", type=int, default=2000)

@@ -157,6 +157,9 @@ typedef struct {
     uint32_t steps_per_launch;  /* passes per persistent launch L (0 = 32; 1 = the reference's
                                    per-pass global gather) */
     int32_t  device;            /* CUDA device ordinal */
+    int32_t  specialize;        /* genome-specialised kernels compiled at run time (NVRTC) for each
+                                   genome structure rf_warmup meets: 0 = when the run-time compiler
+                                   loads (else the interpreted kernel), 1 = required, -1 = never */
 } rf_sim_desc;
 
 /* flame::set_sim_parameters(total_particles, temporal_samples, shuffle_count). */
@@ -362,6 +365,18 @@ RF_API int rf_denoiser_infer(rf_denoiser* d, const void* feats, uint32_t n, uint
 /* One Adam step (lr; betas 0.9, 0.999; eps 1e-8) on the mean L1 loss against target_rgb. */
 RF_API int rf_denoiser_train_step(rf_denoiser* d, const void* feats, const float* target_rgb, uint32_t n, uint32_t h,
                                   uint32_t w, float lr, double* loss);
+
+/* ------------------------------------------------------------------------------------------
+ * Genome-specialised chaos kernels (no reference counterpart; the reference generates GLSL per
+ * genome, variation_table.cpp:217-264).  The CUDA source the run-time compiler builds for this
+ * genome's structure and CTA shape (`needed` receives its size incl. NUL), and a compile-only
+ * check that needs no device (cubin size in *cubin_bytes).
+ * ---------------------------------------------------------------------------------------- */
+RF_API int rf_flame_kernel_source(const rf_flame* f, uint32_t cta_threads, uint32_t cta_slots, char* buf, size_t cap,
+                                  size_t* needed);
+RF_API int rf_flame_kernel_compile(const rf_flame* f, uint32_t cta_threads, uint32_t cta_slots, size_t* cubin_bytes);
+/* 1 when the sim's next launches use a specialised kernel (after rf_warmup), else 0. */
+RF_API int rf_sim_specialized(const rf_sim* s);
 
 /* Writes an RGBA8 image as an uncompressed PNG. */
 RF_API int rf_write_png(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height);

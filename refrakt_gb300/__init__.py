@@ -54,7 +54,8 @@ class FlameInfo(ctypes.Structure):
 class SimDesc(ctypes.Structure):
     _fields_ = [("walkers", ctypes.c_uint64), ("temporal_samples", ctypes.c_uint32),
                 ("shuffle_count", ctypes.c_uint32), ("seed", ctypes.c_uint64), ("cta_slots", ctypes.c_uint32),
-                ("cta_threads", ctypes.c_uint32), ("steps_per_launch", ctypes.c_uint32), ("device", ctypes.c_int32)]
+                ("cta_threads", ctypes.c_uint32), ("steps_per_launch", ctypes.c_uint32), ("device", ctypes.c_int32),
+                ("specialize", ctypes.c_int32)]
 
 
 class RenderDesc(ctypes.Structure):
@@ -165,6 +166,11 @@ _SIGS = {
     "rf_denoiser_infer": ([ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 3 + [ctypes.c_void_p], ctypes.c_int),
     "rf_denoiser_train_step": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 3 +
                                [ctypes.c_float, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    "rf_flame_kernel_source": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t,
+                                ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    "rf_flame_kernel_compile": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_size_t)],
+                                ctypes.c_int),
+    "rf_sim_specialized": ([ctypes.c_void_p], ctypes.c_int),
     "rf_write_png": ([ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32], ctypes.c_int),
 }
 
@@ -354,6 +360,20 @@ class Flame:
         _check(library().rf_flame_screen_affine(self._h, width, height, out))
         return list(out)
 
+    def kernel_source(self, cta_threads=1024, cta_slots=4096):
+        """CUDA source of this genome's specialised chaos kernel."""
+        n = ctypes.c_size_t()
+        _check(library().rf_flame_kernel_source(self._h, cta_threads, cta_slots, None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        _check(library().rf_flame_kernel_source(self._h, cta_threads, cta_slots, buf, n.value, None))
+        return buf.value.decode()
+
+    def kernel_compile(self, cta_threads=1024, cta_slots=4096):
+        """Compiles the specialised kernel for sm_103a (no device needed); returns the cubin size."""
+        n = ctypes.c_size_t()
+        _check(library().rf_flame_kernel_compile(self._h, cta_threads, cta_slots, ctypes.byref(n)))
+        return n.value
+
     def xform_draws(self, xform):
         return library().rf_flame_xform_draws(self._h, xform)
 
@@ -363,8 +383,9 @@ class Sim:
     per-flame ``warmup`` / ``draw_to_bins`` (src/flame.cpp:105-330)."""
 
     def __init__(self, walkers, temporal_samples=1, shuffle_count=1024, seed=0, cta_slots=4096, cta_threads=0,
-                 steps_per_launch=32, device=0):
-        d = SimDesc(walkers, temporal_samples, shuffle_count, seed, cta_slots, cta_threads, steps_per_launch, device)
+                 steps_per_launch=32, device=0, specialize=0):
+        d = SimDesc(walkers, temporal_samples, shuffle_count, seed, cta_slots, cta_threads, steps_per_launch, device,
+                    specialize)
         h = ctypes.c_void_p()
         _check(library().rf_sim_create(ctypes.byref(d), ctypes.byref(h)))
         self._h = h
@@ -380,6 +401,10 @@ class Sim:
 
     def set_stream(self, stream):
         _check(library().rf_sim_set_stream(self._h, _stream(stream)))
+
+    def specialized(self):
+        """True when the launches after the last warmup use a genome-specialised kernel."""
+        return bool(library().rf_sim_specialized(self._h))
 
     def enable_xid_trace(self, passes):
         _check(library().rf_sim_enable_xid_trace(self._h, passes))

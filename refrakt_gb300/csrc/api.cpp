@@ -40,6 +40,7 @@ static std::atomic<uint64_t> g_uid{1};
 using namespace rfk;
 
 #include "handles.h"
+#include "specialize.h"
 
 namespace {
 
@@ -92,7 +93,9 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.trace_passes = s->trace_passes;
         a.n_groups = (uint32_t)(s->N / kGroup);
         const uint32_t grid = (uint32_t)(s->N / s->slots);
-        cudaError_t e = launch_chaos((int)s->threads, (int)s->slots, a, grid, s->stream);
+        cudaError_t e = s->spec ? launch_spec(s->spec, (int)s->threads, (int)s->slots, a, grid,
+                                              chaos_smem(s->slots, a.prog_words, a.steps), s->stream)
+                                : launch_chaos((int)s->threads, (int)s->slots, a, grid, s->stream);
         if (e != cudaSuccess) return cuda_fail(e, "chaos kernel launch");
         s->cur ^= 1;
         s->pass += steps;
@@ -416,6 +419,13 @@ int rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_width) {
     if (int rc = genome_program(f->g, *f->reg, prog)) return rc;
     if (int rc = genome_validate(f->g, *f->reg)) return rc;
     s->prog_words = (uint32_t)prog.size();
+    s->spec = nullptr;
+    if (s->d.specialize >= 0) {
+        const void* k = nullptr;
+        const int rc = spec_kernel(prog, (int)s->threads, (int)s->slots, s->device, &k);
+        if (rc == RF_OK) s->spec = k;
+        else if (s->d.specialize > 0) return rc;  // required
+    }
     RF_CUDA(cudaMemcpyAsync(s->base_prog, prog.data(), prog.size() * 4, cudaMemcpyHostToDevice, s->stream));
     RF_CUDA(launch_animate(s->base_prog, s->prog_words, s->T, tss_width, s->progs, s->prog_stride, s->stream));
     RF_CUDA(cudaMemcpyAsync(s->palette, f->g.palette, sizeof(f->g.palette), cudaMemcpyHostToDevice, s->stream));
@@ -427,6 +437,34 @@ int rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_width) {
     if (int rc = launch_passes(s, 1 + num_passes, true, false, nullptr, nullptr, 0, 0, nullptr)) return rc;
     s->warmed_uid = f->uid;
     s->warmed_version = f->version;
+    return RF_OK;
+}
+
+int rf_sim_specialized(const rf_sim* s) { return s && s->spec ? 1 : 0; }
+
+int rf_flame_kernel_source(const rf_flame* f, uint32_t cta_threads, uint32_t cta_slots, char* buf, size_t cap,
+                           size_t* needed) {
+    if (!f || !cta_threads || cta_slots % cta_threads) return fail(RF_ERR_INVALID_ARG, "rf_flame_kernel_source: bad arguments");
+    std::vector<uint32_t> prog;
+    if (int rc = genome_program(f->g, *f->reg, prog)) return rc;
+    const std::string src = spec_source(prog, (int)cta_threads, (int)(cta_slots / cta_threads));
+    if (needed) *needed = src.size() + 1;
+    if (buf && cap) {
+        const size_t n = std::min(cap - 1, src.size());
+        memcpy(buf, src.data(), n);
+        buf[n] = 0;
+        if (n < src.size()) return fail(RF_ERR_CAPACITY, "rf_flame_kernel_source: buffer too small");
+    }
+    return RF_OK;
+}
+
+int rf_flame_kernel_compile(const rf_flame* f, uint32_t cta_threads, uint32_t cta_slots, size_t* cubin_bytes) {
+    if (!f || !cta_threads || cta_slots % cta_threads) return fail(RF_ERR_INVALID_ARG, "rf_flame_kernel_compile: bad arguments");
+    std::vector<uint32_t> prog;
+    if (int rc = genome_program(f->g, *f->reg, prog)) return rc;
+    std::vector<char> cubin;
+    if (int rc = spec_compile(spec_source(prog, (int)cta_threads, (int)(cta_slots / cta_threads)), cubin)) return rc;
+    if (cubin_bytes) *cubin_bytes = cubin.size();
     return RF_OK;
 }
 

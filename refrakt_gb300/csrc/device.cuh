@@ -2,8 +2,7 @@
 // shuffle, start points, and the first-pass jitter.
 #pragma once
 
-#include <cuda_runtime.h>
-#include <stdint.h>
+#include "rtc_types.h"
 
 #include "program.h"
 

@@ -36,6 +36,7 @@ struct rf_sim {
     uint64_t warmed_uid = 0, warmed_version = 0;
     uint32_t pass = 0;
     int splat = RF_SPLAT_AUTO;
+    const void* spec = nullptr;  // genome-specialised kernel of the warmed flame (specialize.cpp)
     // rf_render scratch
     float4* r_bins = nullptr;
     uint32_t* r_hits = nullptr;

@@ -7,35 +7,11 @@
 
 #include <vector>
 
+#include "chaos_args.h"
+
 namespace rfk {
 
-struct ChaosArgs {
-    const uint32_t* progs;   // one compiled genome per temporal sample
-    uint32_t prog_stride;    // words between copies
-    uint32_t prog_words;     // words staged per CTA
-    const float4* walk_in;   // N walkers (x, y, colour, unused)
-    float4* walk_out;
-    uint4* rng;              // N JSF32 states
-    const uint16_t* table;   // table_size permutations of a CTA's slots (the mixing domain)
-    uint32_t table_size;
-    uint32_t ppts;           // walkers per temporal sample
-    uint32_t chunks_per_ts;  // CTAs (mixing domains) per temporal sample
-    uint32_t pass0;          // pass index of this launch's first pass
-    uint32_t steps;          // passes in this launch
-    uint64_t seed;
-    int first_run;           // pass 0 reads the start points, jitters, draws colours
-    int draw;
-    int splat;               // 0: a reduction per point; 1: warp-aggregated; 2: adaptive (splat.cuh)
-    float ss[6];             // screen affine
-    uint32_t W, H;
-    float4* bins;            // RGBA sums
-    uint32_t* hits;          // counts (may be null)
-    const float4* palette;   // 256 entries
-    unsigned long long* counters;  // [0] drawn [1] emitted [2] walker-steps
-    uint8_t* trace;          // xform id per (pass, 256-group), may be null
-    uint32_t trace_passes;
-    uint32_t n_groups;
-};
+
 
 size_t chaos_smem(int slots, uint32_t prog_words, uint32_t steps);
 bool chaos_shape_supported(int threads, int slots);

@@ -8,7 +8,7 @@
 // uint32; float fields are stored bit-cast.  One copy exists per temporal sample.
 #pragma once
 
-#include <stdint.h>
+#include "rtc_types.h"
 
 namespace rfk {
 

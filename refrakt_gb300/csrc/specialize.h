@@ -1,0 +1,25 @@
+// Genome-specialised chaos kernels compiled at run time (specialize.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "chaos_args.h"
+
+namespace rfk {
+
+// CUDA source of the specialised kernel for a compiled genome and CTA shape
+std::string spec_source(const std::vector<uint32_t>& prog, int threads, int spt);
+// compiles source for sm_103a with the run-time compiler (no device needed)
+int spec_compile(const std::string& src, std::vector<char>& cubin);
+// true when the run-time compiler can be loaded (else *why says why)
+bool spec_available(std::string* why);
+// the compiled kernel for this genome's structure (cached); RF_OK or a status with rf_last_error
+int spec_kernel(const std::vector<uint32_t>& prog, int threads, int slots, int device, const void** out);
+cudaError_t launch_spec(const void* kernel, int threads, int slots, const ChaosArgs& a, uint32_t grid, size_t smem,
+                        cudaStream_t st);
+
+}  // namespace rfk

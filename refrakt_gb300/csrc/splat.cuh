@@ -16,8 +16,7 @@
 //                  splat_global otherwise, so spread attractors pay one shuffle and one vote.
 #pragma once
 
-#include <cuda_runtime.h>
-#include <stdint.h>
+#include "rtc_types.h"
 
 namespace rfk {
 

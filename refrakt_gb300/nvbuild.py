@@ -19,8 +19,34 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 
 
+# device headers the run-time compiler sees (specialize.cpp), embedded into the library
+RTC_HEADERS = ["rtc_types.h", "program.h", "device.cuh", "variations.cuh", "splat.cuh", "chaos_args.h",
+               "chaos_body.cuh"]
+
+
+def _rtc_headers_source():
+    """Writes _build/rtc_headers.cpp: the RTC_HEADERS as string literals (kRtcHeader*)."""
+    out = os.path.join(OBJ_DIR, "rtc_headers.cpp")
+    parts = ["// generated by nvbuild.py: device headers for the run-time compiler", "namespace rfk {",
+             "extern const int kRtcHeaderCount = %d;" % len(RTC_HEADERS),
+             "extern const char* const kRtcHeaderNames[] = {%s};" % ", ".join('"%s"' % h for h in RTC_HEADERS),
+             "extern const char* const kRtcHeaderSources[] = {"]
+    for h in RTC_HEADERS:
+        with open(os.path.join(CSRC, h)) as f:
+            text = f.read()
+        assert ")RFKHDR\"" not in text
+        parts.append('R"RFKHDR(%s)RFKHDR",' % text)
+    parts += ["};", "}  // namespace rfk", ""]
+    body = "\n".join(parts)
+    if not os.path.exists(out) or open(out).read() != body:
+        with open(out, "w") as f:
+            f.write(body)
+    return out
+
+
 def _sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp"))) + \
+        [_rtc_headers_source()]
 
 
 def _headers():
@@ -63,7 +89,7 @@ def build(force=False, verbose=False):
     stale = not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs)
     if force or jobs or stale:
         tmp = LIB + ".tmp.%d" % os.getpid()
-        cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

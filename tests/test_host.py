@@ -282,3 +282,19 @@ def test_batch_rejects_bad_arguments_before_device_work(rk, compiler):
     assert not h.value
     assert L.rf_batch_run(None) == 1 and L.rf_batch_sync(None, None) == 1
     assert L.rf_batch_destroy(None) == 0
+
+
+def test_specialised_kernel_source_and_compile(rk, compiler):
+    """The generated source names each xform's variations as constants and compiles for
+    sm_103a with the run-time compiler (no device needed)."""
+    f = rk.Flame.synthesize(compiler, rk.SYNTH_RANDOM, 1, 256, 256, n_xforms=8, final_xform=True, force_parametric=True)
+    src = f.kernel_source(1024, 4096)
+    lay = f.param_layout()
+    nvar = sum(len(x["variations"]) for x in lay["xforms"]) + len(lay["final_xform"]["variations"])
+    assert src.count("vary_impl(") == nvar  # one inlined call per (xform, variation)
+    assert "case -1:" in src and "chaos_body<1024, 4, rfk::GenEval>" in src
+    assert f.kernel_source(1024, 4096) == src  # deterministic: the cache key
+    g = rk.Flame.synthesize(compiler, rk.SYNTH_SMALL, 0, 256, 256)
+    assert g.kernel_source(512, 2048).count("case ") == 2  # 3 xforms: cases 0, 1 and default
+    assert f.kernel_compile(1024, 4096) > 10000
+    assert g.kernel_compile(256, 256) > 10000
