@@ -35,7 +35,8 @@ WORKLOADS = {
                       out=(1920, 1080), ss=2, points=1000 * 3840 * 2160, de=(9, 0, 0.4), image=True),
     "small": dict(name="small genome (seed 0, 3 xforms), 512x512 bins, 65,536 walkers x 256 passes",
                   genome=dict(kind=0, seed=0, n_xforms=0, final_xform=False, force_parametric=False),
-                  out=(512, 512), ss=1, points=65536 * 256, de=None, image=True, walkers=65536),
+                  out=(512, 512), ss=1, points=65536 * 256, de=None, image=True, walkers=65536,
+                  cta_slots=2048),  # 65,536 walkers fill only 16 CTAs of 4096 slots
     "contract": dict(name="contracting genome (seed 4, 6 xforms), 1920x1080 bins, 2^34 points",
                      genome=dict(kind=2, seed=4, n_xforms=0, final_xform=False, force_parametric=False),
                      out=(1920, 1080), ss=1, points=2 ** 34, de=None, image=False),
@@ -164,19 +165,20 @@ def _peaks():
 
 
 def _profile_figure(workload, key):
-    """A figure ("<key>: <int>") from the committed ncu summary of this workload (or None)."""
+    """A figure ("<key>: <number>") from the committed ncu summary of this workload (or None)."""
     import re
     try:
         with open(os.path.join(ROOT, "profiles", "chaos_kernel_%s.md" % workload)) as f:
-            m = re.search(r"^%s: (\d+)" % re.escape(key), f.read(), re.M)
-        return int(m.group(1)) if m else None
+            m = re.search(r"^%s: ([0-9.]+)" % re.escape(key), f.read(), re.M)
+        return float(m.group(1)) if m else None
     except OSError:
         return None
 
 
 def _traffic(workload):
     """DRAM bytes per chaos launch from the committed ncu summary of this workload (or None)."""
-    return _profile_figure(workload, "dram bytes per launch")
+    v = _profile_figure(workload, "dram bytes per launch")
+    return int(v) if v is not None else None
 
 
 def cpu_baseline(genome_xml, seconds=12.0, threads=None):
@@ -249,7 +251,7 @@ def run_native(args):
     xml = flame.to_xml()
     info = flame.info()
     sms = torch.cuda.get_device_properties(local).multi_processor_count
-    cta = args.cta_slots
+    cta = args.cta_slots or WL.get("cta_slots", 4096)
     walkers = WL.get("walkers") or sms * args.ctas_per_sm * cta
     sim = R.Sim(walkers, cta_slots=cta, cta_threads=args.cta_threads, steps_per_launch=args.steps_per_launch,
                 seed=1000 + rank, device=local, specialize={"auto": 0, "on": 1, "off": -1}[args.specialize])
@@ -333,14 +335,14 @@ def run_native(args):
     pts_per_launch = walkers * args.steps_per_launch
     achieved = bytes_per_point * pts_per_launch / (per_launch_ms * 1e-3) / 1e9
     prof_key = {"frame1080": "1080p"}.get(args.workload, args.workload)
-    traffic = _traffic(prof_key)
-    inst = _profile_figure(prof_key, "thread instructions per point")
+    traffic = _traffic(prof_key) if sim.specialized() else None
+    inst = _profile_figure(prof_key, "warp instructions per point") if sim.specialized() else None
     sms_ = torch.cuda.get_device_properties(local).multi_processor_count
     issue = None
     if inst:
         clk_mhz = (clk.summary() or {}).get("sm_mhz") or 2070.0
-        bound = sms_ * 4 * clk_mhz * 1e6 * 32 / inst / 1e9  # Gpoints/s at one warp instruction per scheduler-cycle
-        issue = {"thread_inst_per_point": inst, "bound_gpoints_s": bound,
+        bound = sms_ * 4 * clk_mhz * 1e6 / inst / 1e9  # Gpoints/s at one warp instruction per scheduler-cycle
+        issue = {"warp_inst_per_point": inst, "bound_gpoints_s": bound,
                  "frac": (pts_per_launch / (per_launch_ms * 1e-3) / 1e9) / bound}
     line = {
         "metric": "Gpoints/s histogrammed", "value": value, "unit": "Gpoints/s", "n_gpus": ws, "steps": args.steps,
@@ -602,7 +604,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--cta-slots", type=int, default=4096)
+    ap.add_argument("--cta-slots", type=int, default=0, help="walker slots per CTA (0: the workload's default)")
     ap.add_argument("--cta-threads", type=int, default=0)
     ap.add_argument("--ctas-per-sm", type=int, default=4)
     ap.add_argument("--steps-per-launch", type=int, default=32)

@@ -4,9 +4,10 @@
 // The reference does density estimation as a GL point-sprite raster pass with additive
 // blending (src/main.cpp:490-515, shaders/density_vert.glsl:26-63, density_frag.glsl:9-18):
 // every non-empty bin becomes a sprite of radius r = max(min, min(R, int(R / a^curve))) whose
-// fragments add color * (1 - d^2) * (2/pi) / r^2.  Here the same sum is a gather: each output
-// bin reads the bins within the largest radius present near it and keeps those whose disc
-// covers it.  The disc is the symmetric restatement 4 (dx^2 + dy^2) <= (2r + 1)^2 with
+// fragments add color * (1 - d^2) * (2/pi) / r^2.  Here each CTA owns an output tile in shared
+// memory and every non-empty bin of the tile and its halo adds its disc's part inside the tile
+// (radii above 12 gather from global memory).  The disc is the symmetric restatement
+// 4 (dx^2 + dy^2) <= (2r + 1)^2 with
 // d^2 = (dx^2 + dy^2) / (r + 0.5)^2 (the GL sprite's sub-pixel centring depends on point
 // rasterisation rules).  Radii come from thresholds on a, computed on the host in FP64, and
 // the kernel weights from a per-radius table, so every radius and weight is exactly defined.
@@ -19,7 +20,6 @@
 
 namespace rfk {
 
-constexpr int kDeTileX = 32, kDeTileY = 8;
 constexpr int kDeMaxSmemR = 12;  // radius handled through shared-memory tiles
 
 struct DeTables {
@@ -52,64 +52,59 @@ __global__ void de_radius_kernel(const float4* __restrict__ in, size_t n, const 
     }
 }
 
-// pass 2: gather through a shared-memory tile with a halo of R bins
+// pass 2: a CTA owns a 64 x 16 output tile in shared memory; every
+// non-empty bin of the tile and its R halo adds its disc's part inside the tile with shared-
+// memory atomics — the GL sprite pass restricted to one tile.  Work follows the sprites' area
+// (mostly radius 0 and 1 at converged sample counts) instead of the tile's largest radius.
+constexpr int kDsX = 64, kDsY = 16, kDsThreads = 256;
+
 template <int R>
-__global__ void __launch_bounds__(kDeTileX * kDeTileY) de_gather_kernel(
+__global__ void __launch_bounds__(kDsThreads) de_scatter_kernel(
     const float4* __restrict__ in, const uint8_t* __restrict__ rad, uint32_t w, uint32_t h,
     const float* __restrict__ weights, const DeTables T, float4* __restrict__ out) {
-    constexpr int SW = kDeTileX + 2 * R, SH = kDeTileY + 2 * R;
-    __shared__ float4 s_c[SH][SW];
-    __shared__ uint8_t s_r[SH][SW];
-    __shared__ int s_max;
-    const int tx = threadIdx.x % kDeTileX, ty = threadIdx.x / kDeTileX;
-    const int x0 = blockIdx.x * kDeTileX - R, y0 = blockIdx.y * kDeTileY - R;
-    if (threadIdx.x == 0) s_max = 0;
+    constexpr int SW = kDsX + 2 * R, SH = kDsY + 2 * R;
+    __shared__ float s_acc[4][kDsY][kDsX];
+    float* acc = &s_acc[0][0][0];
+    for (int i = threadIdx.x; i < 4 * kDsY * kDsX; i += kDsThreads) acc[i] = 0.0f;
     __syncthreads();
-    int lmax = 0;
-    for (int i = threadIdx.x; i < SW * SH; i += blockDim.x) {
-        const int sx = i % SW, sy = i / SW;
-        const int gx = x0 + sx, gy = y0 + sy;
-        float4 v = make_float4(0, 0, 0, 0);
-        uint8_t r = 255;
-        if (gx >= 0 && gy >= 0 && gx < (int)w && gy < (int)h) {
-            const size_t gi = (size_t)gy * w + gx;
-            r = rad[gi];
-            if (r != 255) v = in[gi];
-        }
-        s_c[sy][sx] = v;
-        s_r[sy][sx] = r;
-        if (r != 255 && r > lmax) lmax = r;
-    }
-    atomicMax(&s_max, lmax);
-    __syncthreads();
-    const int ox = blockIdx.x * kDeTileX + tx, oy = blockIdx.y * kDeTileY + ty;
-    if (ox >= (int)w || oy >= (int)h) return;
-    const int rm = s_max;
-    float4 acc = make_float4(0, 0, 0, 0);
-    for (int dy = -rm; dy <= rm; dy++) {
-        for (int dx = -rm; dx <= rm; dx++) {
-            const int sx = tx + R + dx, sy = ty + R + dy;
-            const int r = s_r[sy][sx];
-            if (r == 255) continue;
-            const int ax = dx < 0 ? -dx : dx, ay = dy < 0 ? -dy : dy;
-            if (ax > r || ay > r) continue;
-            float wt;
-            if (r == 0) wt = 1.0f;
-            else {
-                if (4 * (ax * ax + ay * ay) > (2 * r + 1) * (2 * r + 1)) continue;
-                wt = weights[T.wbase[r] + ay * (r + 1) + ax];
+    const int tx0 = blockIdx.x * kDsX, ty0 = blockIdx.y * kDsY;
+    for (int i = threadIdx.x; i < SW * SH; i += kDsThreads) {
+        const int gx = tx0 - R + i % SW, gy = ty0 - R + i / SW;
+        if (gx < 0 || gy < 0 || gx >= (int)w || gy >= (int)h) continue;
+        const size_t gi = (size_t)gy * w + gx;
+        const int r = rad[gi];
+        if (r == 255) continue;
+        // the disc's bounding box inside the tile
+        const int xa = max(gx - r, tx0), xb = min(gx + r, min(tx0 + kDsX, (int)w) - 1);
+        const int ya = max(gy - r, ty0), yb = min(gy + r, min(ty0 + kDsY, (int)h) - 1);
+        if (xa > xb || ya > yb) continue;
+        const float4 v = in[gi];
+        const int lim = (2 * r + 1) * (2 * r + 1);
+        const float* wr = weights + T.wbase[r];
+        for (int oy = ya; oy <= yb; oy++) {
+            const int ay = oy > gy ? oy - gy : gy - oy;
+            for (int ox = xa; ox <= xb; ox++) {
+                const int ax = ox > gx ? ox - gx : gx - ox;
+                if (4 * (ax * ax + ay * ay) > lim) continue;
+                const float wt = r == 0 ? 1.0f : wr[ay * (r + 1) + ax];
+                const int o = (oy - ty0) * kDsX + (ox - tx0);
+                atomicAdd(acc + o, v.x * wt);
+                atomicAdd(acc + kDsY * kDsX + o, v.y * wt);
+                atomicAdd(acc + 2 * kDsY * kDsX + o, v.z * wt);
+                atomicAdd(acc + 3 * kDsY * kDsX + o, v.w * wt);
             }
-            const float4 v = s_c[sy][sx];
-            acc.x = fmaf(v.x, wt, acc.x);
-            acc.y = fmaf(v.y, wt, acc.y);
-            acc.z = fmaf(v.z, wt, acc.z);
-            acc.w = fmaf(v.w, wt, acc.w);
         }
     }
-    out[(size_t)oy * w + ox] = acc;
+    __syncthreads();
+    for (int i = threadIdx.x; i < kDsY * kDsX; i += kDsThreads) {
+        const int ox = tx0 + i % kDsX, oy = ty0 + i / kDsX;
+        if (ox < (int)w && oy < (int)h)
+            out[(size_t)oy * w + ox] = make_float4(acc[i], acc[kDsY * kDsX + i], acc[2 * kDsY * kDsX + i],
+                                                   acc[3 * kDsY * kDsX + i]);
+    }
 }
 
-// large radii: the same gather straight from global memory
+// large radii: the gather straight from global memory
 __global__ void de_gather_global_kernel(const float4* __restrict__ in, const uint8_t* __restrict__ rad,
                                         uint32_t w, uint32_t h, const float* __restrict__ weights,
                                         const DeTables T, float4* __restrict__ out) {
@@ -292,12 +287,11 @@ static cudaError_t launch_density_passes(const float4* in, uint32_t w, uint32_t 
     const size_t n = (size_t)w * h;
     de_radius_kernel<<<1024, 256, 0, st>>>(in, n, T, rad);
     const int rmax = T.R > T.min_r ? T.R : T.min_r;
-    const dim3 grid((w + kDeTileX - 1) / kDeTileX, (h + kDeTileY - 1) / kDeTileY);
-    const int threads = kDeTileX * kDeTileY;
-    if (rmax <= 3) de_gather_kernel<3><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
-    else if (rmax <= 6) de_gather_kernel<6><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
-    else if (rmax <= 9) de_gather_kernel<9><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
-    else if (rmax <= kDeMaxSmemR) de_gather_kernel<kDeMaxSmemR><<<grid, threads, 0, st>>>(in, rad, w, h, dw, T, out);
+    const dim3 grid((w + kDsX - 1) / kDsX, (h + kDsY - 1) / kDsY);
+    if (rmax <= 3) de_scatter_kernel<3><<<grid, kDsThreads, 0, st>>>(in, rad, w, h, dw, T, out);
+    else if (rmax <= 6) de_scatter_kernel<6><<<grid, kDsThreads, 0, st>>>(in, rad, w, h, dw, T, out);
+    else if (rmax <= 9) de_scatter_kernel<9><<<grid, kDsThreads, 0, st>>>(in, rad, w, h, dw, T, out);
+    else if (rmax <= kDeMaxSmemR) de_scatter_kernel<kDeMaxSmemR><<<grid, kDsThreads, 0, st>>>(in, rad, w, h, dw, T, out);
     else de_gather_global_kernel<<<dim3((w + 127) / 128, h), 128, 0, st>>>(in, rad, w, h, dw, T, out);
     return cudaGetLastError();
 }
