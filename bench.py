@@ -484,6 +484,7 @@ def run_batch(args):
 
 
 def run_learned(args):
+    import numpy as np
     import torch
     import refrakt_gb300 as R
     from refrakt_gb300 import learned as LD
@@ -502,13 +503,15 @@ def run_learned(args):
     t0 = time.perf_counter()
     tr = [LD.genome(R, comp, s, S, S) for s in tr_seeds]
     te = [LD.genome(R, comp, s, S, S) for s in te_seeds]
-    feats = torch.empty(n_train, S, S, 8, dtype=torch.bfloat16, device="cuda")
+    levels = [int(x) for x in args.learned_spp.split(",")]
+    feats = [torch.empty(n_train, S, S, 8, dtype=torch.bfloat16, device="cuda") for _ in levels]
     targets = torch.empty(n_train, S, S, 3, device="cuda")
-    LD.render_features(tr, S, S, 16, [s * 7 + 1 for s in tr_seeds], feats)
+    for k, spp in enumerate(levels):
+        LD.render_features(tr, S, S, spp, [s * 7 + 1 + 100 * k for s in tr_seeds], feats[k])
     LD.render_images(tr, S, S, 1000, [s * 7 + 2 for s in tr_seeds], targets)
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
-    log("training data: %d pairs in %.1f s" % (n_train, t_data))
+    log("training data: %d genomes x %d input levels in %.1f s" % (n_train, len(levels), t_data))
     net = R.Denoiser(4 * S * S, seed=7)
     t0 = time.perf_counter()
     losses = LD.train(net, feats, targets, args.learned_steps, batch=4, lr=1e-3, log=log)
@@ -527,14 +530,13 @@ def run_learned(args):
         plain[spp] = float(LD.l1(img, ref).mean())
     f16 = torch.empty(n_test, S, S, 8, dtype=torch.bfloat16, device="cuda")
     learned = {}
-    per_img = {}
-    for spp in (16, 32, 64):
+    for spp in levels:
         LD.render_features(te, S, S, spp, [s * 7 + 20 + spp for s in te_seeds], f16)
         LD.infer_all(net, f16, img)
-        e = LD.l1(img, ref)
-        learned[spp] = float(e.mean())
-        per_img[spp] = e
+        learned[spp] = float(LD.l1(img, ref).mean())
     equiv = {spp: LD.plain_equivalent_spp(spps, [plain[x] for x in spps], learned[spp]) for spp in learned}
+    meets = [spp for spp in levels if learned[spp] <= plain[1000]]
+    spp_fast = min(meets) if meets else min(levels)
     # 1080p frame, seconds per frame: plain (1000 spp + adaptive DE + tonemap) vs learned (16 spp + U-Net)
     W1, H1 = 1920, 1080
     f1 = LD.genome(R, comp, 1, W1, H1)
@@ -544,7 +546,7 @@ def run_learned(args):
     fe1 = torch.empty(1, H1, W1, 8, dtype=torch.bfloat16, device="cuda")
 
     def learned_frame():
-        LD.render_features([f1], W1, H1, 16, [5], fe1)
+        LD.render_features([f1], W1, H1, spp_fast, [5], fe1)
         inf.infer(fe1, out1)
         torch.cuda.synchronize()
 
@@ -563,13 +565,16 @@ def run_learned(args):
                 fn()
                 ts.append(time.perf_counter() - t)
             times[name] = statistics.median(ts)
-    # the fallback policy on the held-out set: split estimate from two 16-spp runs
-    lr_ = LD.LearnedRenderer(net, spp=16, bound=args.learned_bound)
+    # the fallback policy on the held-out set: split estimates from two short runs
+    lr_ = LD.LearnedRenderer(net, spp=spp_fast, bound=args.learned_bound)
     fallbacks, est_err = 0, []
     for k in range(min(32, n_test)):
-        out, est, fb = lr_.render(te[k], S, S, seed=te_seeds[k] * 7 + 40)
-        fallbacks += int(fb)
-        est_err.append((est, float((out - ref[k]).abs().mean())))
+        out, est, pest = lr_.estimate(te[k], S, S, seed=te_seeds[k] * 7 + 40)
+        fallbacks += int(est > args.learned_bound)
+        est_err.append((est, pest, float((out - ref[k]).abs().mean())))
+    true_e = np.array([x[2] for x in est_err])
+    est_corr = {"learned_split": float(np.corrcoef([x[0] for x in est_err], true_e)[0, 1]),
+                "plain_split": float(np.corrcoef([x[1] for x in est_err], true_e)[0, 1])}
     line = {
         "metric": "s per 1080p frame at fixed L1 err, learned vs plain DE", "value": times["learned"],
         "unit": "s/frame", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -578,7 +583,8 @@ def run_learned(args):
                                   (3000 + n_test - 1),
         "config": {"workload": CONFIG_NAME, "train_genomes": n_train, "test_genomes": n_test,
                    "train_steps": args.learned_steps, "batch": 4, "resolution": [S, S],
-                   "params": net.num_params(), "input_spp": 16, "target_spp": 1000, "reference_spp": 4000},
+                   "params": net.num_params(), "input_spp": levels, "target_spp": 1000, "reference_spp": 4000,
+                   "frame_spp_learned": spp_fast},
         "plain_s_per_frame": times["plain"],
         "speedup_vs_plain": times["plain"] / times["learned"],
         "l1_plain_by_spp": plain, "l1_learned_by_input_spp": learned,
@@ -587,13 +593,15 @@ def run_learned(args):
         "learned_reaches_plain_1000spp_error": learned[16] <= plain[1000],
         "train": {"data_s": t_data, "train_s": t_train, "loss_first": losses[0], "loss_last": losses[-1]},
         "fallback": {"bound": args.learned_bound, "frames": min(32, n_test), "fallbacks": fallbacks,
-                     "estimate_vs_true_l1": est_err[:8]},
+                     "correlation_with_true_l1": est_corr, "estimate_vs_true_l1": est_err[:8]},
         "gpu_launches": None,
         "e2e": {"value": times["learned"], "unit": "s/frame", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "clocks": clk.summary(),
     }
-    best = min(learned, key=lambda k: learned[k])
-    line["iteration_ratio_at_plain_1000spp_error"] = (1000.0 / best) if learned[best] <= plain[1000] else None
+    line["iteration_ratio_at_plain_1000spp_error"] = (1000.0 / spp_fast) if meets else None
+    line["learned_reaches_plain_1000spp_error"] = bool(meets)
+    if args.learned_save:
+        np.save(args.learned_save, net.params())
     print(json.dumps(line))
     return 0
 
@@ -616,6 +624,8 @@ def main():
     ap.add_argument("--learned-test", type=int, default=200)
     ap.add_argument("--learned-steps", type=int, default=2000)
     ap.add_argument("--learned-bound", type=float, default=0.02)
+    ap.add_argument("--learned-spp", default="16,32,64,128", help="input sample counts the denoiser trains on")
+    ap.add_argument("--learned-save", default="", help="write the trained parameters (.npy) here")
     ap.add_argument("--workload", default="frame1080", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     select_workload(args.workload)

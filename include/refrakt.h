@@ -301,7 +301,7 @@ RF_API int rf_batch_read_bins(rf_batch* b, uint32_t i, float* host_rgba, uint32_
 RF_API int rf_batch_image_f32(rf_batch* b, uint32_t i, float* dst_rgba);
 /* Learned-DE input features of item i's bins (rf_denoiser_features) into device memory; the
    base channels carry the item's FP32 image when the batch keeps one (image_f32, supersample 1). */
-RF_API int rf_batch_features(rf_batch* b, uint32_t i, float k2, void* dst_bf16);
+RF_API int rf_batch_features(rf_batch* b, uint32_t i, float k2, float level, void* dst_bf16);
 /* The autotuned shape: walkers per unit, number of units, drawing passes per unit. */
 RF_API int rf_batch_info(const rf_batch* b, uint32_t* cta_slots, uint32_t* units, uint32_t* unit_passes);
 /* The splat strategy chosen for item i (RF_SPLAT_GLOBAL or RF_SPLAT_WARP); -1 for a bad index. */
@@ -355,11 +355,12 @@ RF_API int rf_denoiser_set_params(rf_denoiser* d, const float* host, size_t coun
 /* Gradients of the last train_step, same layout as the parameters. */
 RF_API int rf_denoiser_gradients(rf_denoiser* d, float* host, size_t cap);
 /* Features of a histogram (bins float4 RGBA sums, width x height): [log10(1 + a k2),
-   rgb * log10(1 + a k2) / a, base.rgb, 0] as bf16; k2 <= 0 takes W*H / sum(a) (FP64
+   rgb * log10(1 + a k2) / a, base.rgb, level] as bf16; k2 <= 0 takes W*H / sum(a) (FP64
    reduction).  base_rgba (may be NULL) is the plain path's FP32 tonemapped image of the same
-   histogram (rf_tonemap out_f32): the network predicts a residual on it. */
+   histogram (rf_tonemap out_f32): the network predicts a residual on it.  level codes the run's
+   sample count for a network trained on several (refrakt_gb300.learned uses log2(spp) / 10). */
 RF_API int rf_denoiser_features(const float* bins_rgba, uint32_t width, uint32_t height, float k2,
-                                const float* base_rgba, void* out_bf16, void* stream);
+                                const float* base_rgba, float level, void* out_bf16, void* stream);
 /* out_rgb = clamp(base + net(feats), 0, 1). */
 RF_API int rf_denoiser_infer(rf_denoiser* d, const void* feats, uint32_t n, uint32_t h, uint32_t w, float* out_rgb);
 /* One Adam step (lr; betas 0.9, 0.999; eps 1e-8) on the mean L1 loss against target_rgb. */

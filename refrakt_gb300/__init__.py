@@ -147,7 +147,8 @@ _SIGS = {
     "rf_batch_info": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
                        ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
     "rf_batch_image_f32": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),
-    "rf_batch_features": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_float, ctypes.c_void_p], ctypes.c_int),
+    "rf_batch_features": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_float, ctypes.c_float, ctypes.c_void_p],
+                          ctypes.c_int),
     "rf_batch_splat": ([ctypes.c_void_p, ctypes.c_uint32], ctypes.c_int),
     "rf_batch_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "rf_gemm_bf16": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 6 +
@@ -162,7 +163,7 @@ _SIGS = {
     "rf_denoiser_set_params": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t], ctypes.c_int),
     "rf_denoiser_gradients": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t], ctypes.c_int),
     "rf_denoiser_features": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_void_p,
-                              ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+                              ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rf_denoiser_infer": ([ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 3 + [ctypes.c_void_p], ctypes.c_int),
     "rf_denoiser_train_step": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 3 +
                                [ctypes.c_float, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
@@ -496,9 +497,9 @@ class Batch:
         """Item i's FP32 tonemapped RGBA image into `out` (a [h, w, 4] float32 CUDA tensor or array)."""
         _check(library().rf_batch_image_f32(self._h, i, _ptr(out)))
 
-    def features(self, i, out, k2=0.0):
+    def features(self, i, out, k2=0.0, level=0.0):
         """Item i's learned-DE input features into `out` (a [h*ss, w*ss, 8] bf16 CUDA tensor)."""
-        _check(library().rf_batch_features(self._h, i, k2, _ptr(out)))
+        _check(library().rf_batch_features(self._h, i, k2, level, _ptr(out)))
 
     def bins(self, i):
         """Host copies of item i's RGBA sums (H, W, 4 float32) and hit counts (H, W uint32)."""
@@ -625,8 +626,9 @@ class Denoiser:
         return loss.value
 
 
-def denoiser_features(bins_rgba, width, height, out, k2=0.0, base=None, stream=None):
-    _check(library().rf_denoiser_features(_ptr(bins_rgba), width, height, k2, _ptr(base), _ptr(out), _stream(stream)))
+def denoiser_features(bins_rgba, width, height, out, k2=0.0, base=None, level=0.0, stream=None):
+    _check(library().rf_denoiser_features(_ptr(bins_rgba), width, height, k2, _ptr(base), level, _ptr(out),
+                                          _stream(stream)))
 
 
 def write_png(path, rgba8):

@@ -436,7 +436,7 @@ int rf_batch_image_f32(rf_batch* b, uint32_t i, float* dst_rgba) {
     return RF_OK;
 }
 
-int rf_batch_features(rf_batch* b, uint32_t i, float k2, void* dst_bf16) {
+int rf_batch_features(rf_batch* b, uint32_t i, float k2, float level, void* dst_bf16) {
     if (!b || i >= b->items.size() || !dst_bf16) return fail(RF_ERR_INVALID_ARG, "rf_batch_features: bad arguments");
     const Item& it = b->items[i];
     cudaSetDevice(b->device);
@@ -444,7 +444,7 @@ int rf_batch_features(rf_batch* b, uint32_t i, float k2, void* dst_bf16) {
     if (!(k2 > 0.0f)) e = launch_stats(it.bins, it.W, it.H, b->stats + 3 * i, b->stream);
     if (e == cudaSuccess)
         e = launch_features(it.bins, (uint64_t)it.W * it.H, k2, b->stats + 3 * i, it.ss == 1 ? it.img_f32 : nullptr,
-                            static_cast<__nv_bfloat16*>(dst_bf16), b->stream);
+                            level, static_cast<__nv_bfloat16*>(dst_bf16), b->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) return cuda_err(e, "rf_batch_features");
     return RF_OK;

@@ -487,7 +487,7 @@ int rf_denoiser_set_params(rf_denoiser* D, const float* host, size_t count) {
 }
 
 int rf_denoiser_features(const float* bins_rgba, uint32_t width, uint32_t height, float k2, const float* base_rgba,
-                         void* out_bf16, void* stream) {
+                         float level, void* out_bf16, void* stream) {
     if (!bins_rgba || !out_bf16 || !width || !height) return fail(RF_ERR_INVALID_ARG, "rf_denoiser_features: bad arguments");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     double* stats = nullptr;
@@ -498,7 +498,7 @@ int rf_denoiser_features(const float* bins_rgba, uint32_t width, uint32_t height
     }
     if (e == cudaSuccess)
         e = launch_features(reinterpret_cast<const float4*>(bins_rgba), (uint64_t)width * height, k2, stats,
-                            reinterpret_cast<const float4*>(base_rgba), static_cast<__nv_bfloat16*>(out_bf16), st);
+                            reinterpret_cast<const float4*>(base_rgba), level, static_cast<__nv_bfloat16*>(out_bf16), st);
     if (stats) cudaFreeAsync(stats, st);
     if (e != cudaSuccess) return cuda_fail(e, "rf_denoiser_features");
     return RF_OK;

@@ -234,9 +234,10 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, 
 // input features of a histogram (RGBA sums float4 per bin, W x H): 8 bf16 channels
 //   [0] l = log10(1 + a * k2), [1..3] colour * l / a — the tonemap's log-density scaling
 //   (tonemap.glsl:18-26) without the gamma step; [4..6] the plain path's tonemapped RGB of the
-//   same histogram (base, may be null: zeros), on which the network predicts a residual; [7] 0
+//   same histogram (base, may be null: zeros), on which the network predicts a residual;
+//   [7] `level`, the caller's code of the run's sample count (the noise level)
 __global__ void features_kernel(const float4* __restrict__ bins, uint64_t n, float k2, const double* __restrict__ stats,
-                                const float4* __restrict__ base, __nv_bfloat16* __restrict__ out) {
+                                const float4* __restrict__ base, float level, __nv_bfloat16* __restrict__ out) {
     const float k = k2 > 0.0f ? k2 : (float)((double)n / fmax(stats[0], 1e-30));
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const float4 c = bins[i];
@@ -254,7 +255,7 @@ __global__ void features_kernel(const float4* __restrict__ bins, uint64_t n, flo
         f[4] = __float2bfloat16_rn(bb.x);
         f[5] = __float2bfloat16_rn(bb.y);
         f[6] = __float2bfloat16_rn(bb.z);
-        f[7] = __float2bfloat16_rn(0.0f);
+        f[7] = __float2bfloat16_rn(level);
         *reinterpret_cast<uint4*>(out + i * 8) = *reinterpret_cast<const uint4*>(f);
     }
 }
@@ -329,8 +330,8 @@ cudaError_t launch_adam(float* w, const float* g, float* m, float* v, uint32_t n
 }
 
 cudaError_t launch_features(const float4* bins, uint64_t n, float k2, const double* stats, const float4* base,
-                            __nv_bfloat16* out, cudaStream_t st) {
-    features_kernel<<<grid_for(n, 256), 256, 0, st>>>(bins, n, k2, stats, base, out);
+                            float level, __nv_bfloat16* out, cudaStream_t st) {
+    features_kernel<<<grid_for(n, 256), 256, 0, st>>>(bins, n, k2, stats, base, level, out);
     return cudaGetLastError();
 }
 

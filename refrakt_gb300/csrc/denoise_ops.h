@@ -30,6 +30,6 @@ cudaError_t launch_adam(float* w, const float* g, float* m, float* v, uint32_t n
                         float eps, uint32_t t, uint32_t cout, uint32_t K, uint32_t taps, __nv_bfloat16* w16,
                         __nv_bfloat16* wf16, uint32_t ldf, cudaStream_t st);
 cudaError_t launch_features(const float4* bins, uint64_t n, float k2, const double* stats, const float4* base,
-                            __nv_bfloat16* out, cudaStream_t st);
+                            float level, __nv_bfloat16* out, cudaStream_t st);
 
 }  // namespace rfk

@@ -21,6 +21,11 @@ from . import Batch, Denoiser, SYNTH_RANDOM, Flame
 DE = (9, 0, 0.4)  # adaptive DE of the plain path: max radius, min radius, curve
 
 
+def level(spp):
+    """Feature channel 7: the short run's sample count, log2(spp) / 10."""
+    return math.log2(spp) / 10.0
+
+
 def genome(R, comp, seed, w, h):
     """A training / held-out genome: 2-12 xforms by seed, with a final xform, 3 random
     variations per xform from the implemented set, affine coefficients in [-1.2, 1.2]."""
@@ -39,7 +44,7 @@ def render_features(flames, w, h, spp, seeds, out, device=0, chunk=256):
         b.run()
         b.sync()
         for i in range(len(part)):
-            b.features(i, out[c0 + i])
+            b.features(i, out[c0 + i], level=level(spp))
         b.close()
 
 
@@ -65,14 +70,18 @@ def l1(a, b):
 
 
 def train(net, feats, targets, steps, batch=4, lr=1e-3, seed=0, log=None):
-    """Adam on random minibatches of whole images; cosine learning-rate decay to lr / 20."""
+    """Adam on random minibatches of whole images; cosine learning-rate decay to lr / 20.
+    `feats` is one [n, h, w, 8] tensor or a list of them (one per input sample count, each
+    against the same targets): every minibatch image draws its sample count at random."""
     import torch
     g = torch.Generator().manual_seed(seed)
-    n = feats.shape[0]
+    levels = feats if isinstance(feats, (list, tuple)) else [feats]
+    n = levels[0].shape[0]
     losses = []
     for s in range(steps):
         idx = torch.randint(0, n, (batch,), generator=g).tolist()
-        f = torch.stack([feats[i] for i in idx])
+        lv = torch.randint(0, len(levels), (batch,), generator=g).tolist()
+        f = torch.stack([levels[l][i] for l, i in zip(lv, idx)])
         t = torch.stack([targets[i] for i in idx])
         # random flips keep the attractors' orientation statistics symmetric
         if s % 2:
@@ -98,21 +107,33 @@ def plain_equivalent_spp(spps, errs, e):
 
 class LearnedRenderer:
     """The learned path for one frame with its fallback: two short runs of `spp` samples per
-    pixel are denoised; if half their mean absolute difference exceeds `bound`, the frame is
-    rendered on the plain path (`plain_spp`, adaptive DE) instead."""
+    pixel are denoised; the error estimate is half the mean absolute difference of the two
+    denoised outputs plus `plain_weight` times that of the two plain images (the sampling noise
+    the network has to remove); above `bound` the frame is rendered on the plain path
+    (`plain_spp`, adaptive DE) instead."""
 
-    def __init__(self, net, spp=16, bound=0.02, plain_spp=1000, device=0):
+    def __init__(self, net, spp=16, bound=0.02, plain_spp=1000, plain_weight=0.0, device=0):
         self.net, self.spp, self.bound, self.plain_spp, self.device = net, spp, bound, plain_spp, device
+        self.plain_weight = plain_weight
 
-    def render(self, flame, w, h, seed=0):
+    def estimate(self, flame, w, h, seed=0):
+        """(denoised average, learned split estimate, plain split estimate) of two short runs."""
         import torch
         feats = torch.empty(2, h, w, 8, dtype=torch.bfloat16, device="cuda")
         render_features([flame, flame], w, h, self.spp, [seed, seed + 1], feats, self.device)
         out = torch.empty(2, h, w, 3, device="cuda")
         self.net.infer(feats, out)
         est = 0.5 * float((out[0] - out[1]).abs().mean())
-        if est <= self.bound:
-            return 0.5 * (out[0] + out[1]), est, False
-        img = torch.empty(1, h, w, 3, device="cuda")
-        render_images([flame], w, h, self.plain_spp, [seed], img, self.device)
-        return img[0], est, True
+        plain = 0.5 * float((feats[0, ..., 4:7].float() - feats[1, ..., 4:7].float()).abs().mean())
+        return 0.5 * (out[0] + out[1]), est, plain
+
+    def render(self, flame, w, h, seed=0):
+        """(image, error estimate, fell back)."""
+        import torch
+        img, est, plain = self.estimate(flame, w, h, seed)
+        e = est + self.plain_weight * plain
+        if e <= self.bound:
+            return img, e, False
+        full = torch.empty(1, h, w, 3, device="cuda")
+        render_images([flame], w, h, self.plain_spp, [seed], full, self.device)
+        return full[0], e, True
