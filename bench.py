@@ -285,7 +285,11 @@ def run_native(args):
         if DE:
             R.density_estimate(bins, W, H, DE[0], DE[1], DE[2], de, stream=stream)
             src = de
+        if ev:
+            ev[2].record(stream)
         R.tonemap(src, W, H, SS, info["gamma"], info["brightness"], info["vibrancy"], 0.0, None, img, stream=stream)
+        if ev:
+            ev[3].record(stream)
 
     def barrier():
         if ws > 1:
@@ -295,7 +299,7 @@ def run_native(args):
     for _ in range(args.warmup):
         frame()
     barrier()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    evs = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(4)) for _ in range(args.steps)]
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
@@ -306,7 +310,23 @@ def run_native(args):
         t1.record(stream)
         barrier()
     ms = t0.elapsed_time(t1)
-    draw_ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    draw_ms = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
+    image_passes = None
+    if WL["image"]:
+        de_ms = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps
+        tm_ms = sum(e[2].elapsed_time(e[3]) for e in evs) / args.steps
+        nb = W * H
+        # algorithmic bytes: DE radius pass 16 B read + 1 B write, gather/scatter pass 16 B read +
+        # 1 B radius read + 16 B write per bin; stats 16 B read per bin (FP64 reduction) + tonemap
+        # 16 B read per bin + 4 B write per output pixel
+        de_bytes = nb * (16 + 1 + 16 + 1 + 16) if DE else 0
+        tm_bytes = nb * 16 + nb * 16 + W_OUT * H_OUT * 4
+        peak_, _ = _peaks()
+        image_passes = {"de_ms": de_ms if DE else 0.0, "de_bytes": de_bytes,
+                        "de_gbs": de_bytes / (de_ms * 1e-3) / 1e9 if DE and de_ms > 0 else None,
+                        "stats_tonemap_ms": tm_ms, "stats_tonemap_bytes": tm_bytes,
+                        "stats_tonemap_gbs": tm_bytes / (tm_ms * 1e-3) / 1e9 if tm_ms > 0 else None,
+                        "peak_gbs": peak_}
     ms_step = slowest_rank_ms(ms / args.steps)
     value = replica_throughput(POINTS, ms / args.steps)
 
@@ -357,6 +377,7 @@ def run_native(args):
                    "parallelism": "replicas" if ws > 1 else "single"},
         "s_per_frame": ms_step / 1e3,
         "draw_ms_per_frame": draw_ms,
+        "image_passes": image_passes,
         "gpu_launches": (launches + (FUSE + args.steps_per_launch - 1) // args.steps_per_launch + 4) * args.steps,
         "e2e": {"value": e2e_value, "unit": "Gpoints/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "s_per_frame": e2e_step / 1e3},

@@ -283,6 +283,9 @@ typedef struct {
     int32_t  device;
     int32_t  splat;             /* rf_splat; AUTO chooses per genome from its probe histogram */
     int32_t  image_f32;         /* 1: keep each tonemapped image in FP32 too (rf_batch_image_f32) */
+    int32_t  specialize;        /* genome structures with >= 2 units per SM get their own launch
+                                   of a specialised kernel compiled at run time: 0 = when the
+                                   run-time compiler loads, 1 = required, -1 = never */
 } rf_batch_desc;
 RF_API int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc* d, rf_batch** out);
 /* Enqueues one whole batch (clear, draw, DE, tonemap) on the batch's own stream. */
@@ -304,6 +307,8 @@ RF_API int rf_batch_image_f32(rf_batch* b, uint32_t i, float* dst_rgba);
 RF_API int rf_batch_features(rf_batch* b, uint32_t i, float k2, float level, void* dst_bf16);
 /* The autotuned shape: walkers per unit, number of units, drawing passes per unit. */
 RF_API int rf_batch_info(const rf_batch* b, uint32_t* cta_slots, uint32_t* units, uint32_t* unit_passes);
+/* 1 when item i is drawn by a genome-specialised kernel, 0 by the interpreted one, -1 bad index. */
+RF_API int rf_batch_specialized(const rf_batch* b, uint32_t i);
 /* The splat strategy chosen for item i (RF_SPLAT_GLOBAL or RF_SPLAT_WARP); -1 for a bad index. */
 RF_API int rf_batch_splat(const rf_batch* b, uint32_t i);
 RF_API int rf_batch_destroy(rf_batch* b);

@@ -72,7 +72,8 @@ class BatchItem(ctypes.Structure):
 class BatchDesc(ctypes.Structure):
     _fields_ = [("fuse_passes", ctypes.c_uint32), ("cta_slots", ctypes.c_uint32), ("unit_passes", ctypes.c_uint32),
                 ("density_estimation", ctypes.c_int32), ("k2", ctypes.c_float), ("use_graph", ctypes.c_int32),
-                ("device", ctypes.c_int32), ("splat", ctypes.c_int32), ("image_f32", ctypes.c_int32)]
+                ("device", ctypes.c_int32), ("splat", ctypes.c_int32), ("image_f32", ctypes.c_int32),
+                ("specialize", ctypes.c_int32)]
 
 
 class DenoiserDesc(ctypes.Structure):
@@ -150,6 +151,7 @@ _SIGS = {
     "rf_batch_features": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_float, ctypes.c_float, ctypes.c_void_p],
                           ctypes.c_int),
     "rf_batch_splat": ([ctypes.c_void_p, ctypes.c_uint32], ctypes.c_int),
+    "rf_batch_specialized": ([ctypes.c_void_p, ctypes.c_uint32], ctypes.c_int),
     "rf_batch_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "rf_gemm_bf16": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 6 +
                      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),
@@ -455,7 +457,7 @@ class Batch:
     (flame, width, height, points, seed, supersample) tuples."""
 
     def __init__(self, items, fuse_passes=20, cta_slots=0, unit_passes=0, density_estimation=True, k2=0.0,
-                 use_graph=True, device=0, splat=0, image_f32=False):
+                 use_graph=True, device=0, splat=0, image_f32=False, specialize=0):
         arr = (BatchItem * len(items))()
         self.sizes = []
         self._flames = [it[0] for it in items]  # keep the genomes alive as long as the batch
@@ -465,7 +467,7 @@ class Batch:
             arr[i] = BatchItem(flame._h, w, h, ss, points, seed)
             self.sizes.append((w, h, ss))
         d = BatchDesc(fuse_passes, cta_slots, unit_passes, int(density_estimation), k2, int(use_graph), device, splat,
-                      int(image_f32))
+                      int(image_f32), specialize)
         h = ctypes.c_void_p()
         _check(library().rf_batch_create(arr, len(items), ctypes.byref(d), ctypes.byref(h)))
         self._h = h
@@ -515,7 +517,8 @@ class Batch:
         a, b, c = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
         _check(library().rf_batch_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return {"cta_slots": a.value, "units": b.value, "unit_passes": c.value,
-                "splat": [library().rf_batch_splat(self._h, i) for i in range(len(self.sizes))]}
+                "splat": [library().rf_batch_splat(self._h, i) for i in range(len(self.sizes))],
+                "specialized": [library().rf_batch_specialized(self._h, i) for i in range(len(self.sizes))]}
 
 
 def render(sim, flame, *a, **k):

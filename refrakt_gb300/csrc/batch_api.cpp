@@ -11,10 +11,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
+#include <string>
 #include <cstring>
 #include <vector>
 
 #include "batch.h"
+#include "specialize.h"
 #include "denoise_ops.h"
 #include "handles.h"
 #include "kernels.h"
@@ -35,6 +38,8 @@ struct Item {
     float4* palette = nullptr;
     uint32_t* dprog = nullptr;
     uint32_t splat = 0;       // warp-aggregated splat for this genome
+    int group = -1;           // specialised launch group (-1: the interpreted launch)
+    std::string structure;    // genome structure (specialisation key)
     uint8_t* rad = nullptr;   // density estimation: a radius byte per bin
     float* dw = nullptr;      // density estimation: kernel weights of every radius
     uint64_t passes = 0;  // drawing passes of SLOTS walkers the item needs
@@ -44,6 +49,8 @@ struct Item {
 
 constexpr uint64_t kUnitSeedStride = 0x9e3779b97f4a7c15ull;  // unit u of an item: seed + u * stride
 constexpr uint64_t kTableSeed = 0x5eed;                      // shared table: keyed by kTableSeed + slots
+constexpr size_t kMaxSpecGroups = 4;       // specialised launches per batch
+constexpr uint32_t kSpecMinUnitsPerSM = 2;  // a structure gets its own launch from 2 units per SM
 constexpr double kCompactShare = 16.0;  // probe points sharing a point's bin above this: compact attractor
 
 // Histogram L1 noise of a mixing domain relative to the reference's global shuffle, measured on
@@ -55,8 +62,16 @@ double mixing_efficiency(uint32_t slots) {
 
 }  // namespace
 
+struct SpecGroup {  // units of one genome structure, drawn by its specialised kernel
+    const void* kernel = nullptr;
+    int grid = 0;
+    uint32_t first = 0, count = 0;
+};
+
 struct rf_batch {
     int device = 0;
+    std::vector<SpecGroup> groups;
+    uint32_t interp_first = 0, interp_count = 0;
     cudaStream_t stream = nullptr;
     rf_batch_desc d{};
     std::vector<Item> items;
@@ -132,8 +147,28 @@ int build_tables(rf_batch* b, uint32_t slots, uint32_t unit_passes, uint32_t pro
             units.push_back(BatchUnit{(uint32_t)i, (uint32_t)per, it.desc.seed + u * kUnitSeedStride});
         it.passes = per * nu;
     }
-    // longest units first, instances interleaved, so the queue's tail is short
-    std::stable_sort(units.begin(), units.end(), [](const BatchUnit& x, const BatchUnit& y) { return x.draw > y.draw; });
+    // by launch group (specialised groups in order, the interpreted launch last), then longest
+    // units first, instances interleaved, so each queue's tail is short
+    auto rank = [&](const BatchUnit& u) {
+        const int g = probe_passes ? -1 : b->items[u.instance].group;
+        return g < 0 ? (int)b->groups.size() : g;
+    };
+    std::stable_sort(units.begin(), units.end(), [&](const BatchUnit& x, const BatchUnit& y) {
+        const int rx = rank(x), ry = rank(y);
+        return rx != ry ? rx < ry : x.draw > y.draw;
+    });
+    if (!probe_passes) {
+        for (auto& g : b->groups) g.count = 0;
+        b->interp_count = 0;
+        for (const BatchUnit& u : units) {
+            const int g = b->items[u.instance].group;
+            if (g < 0) b->interp_count++;
+            else b->groups[g].count++;
+        }
+        uint32_t f = 0;
+        for (auto& g : b->groups) { g.first = f; f += g.count; }
+        b->interp_first = f;
+    }
     cudaFree(b->dinst);
     cudaFree(b->dunits);
     b->dinst = nullptr;
@@ -156,12 +191,12 @@ int make_table(rf_batch* b, uint32_t slots) {
     return RF_OK;
 }
 
-BatchArgs args_for(rf_batch* b) {
+BatchArgs args_for(rf_batch* b, uint32_t first = 0, uint32_t count = ~0u, uint32_t queue = 0) {
     BatchArgs a{};
     a.inst = b->dinst;
-    a.units = b->dunits;
-    a.n_units = b->n_units;
-    a.queue = b->queue;
+    a.units = b->dunits + first;
+    a.n_units = count == ~0u ? b->n_units : count;
+    a.queue = b->queue + queue;
     a.table = b->table;
     a.table_size = b->table_size;
     a.max_prog_words = b->max_prog_words;
@@ -172,7 +207,7 @@ BatchArgs args_for(rf_batch* b) {
 // the whole batch on b->stream: clear, persistent chaos launch, per-item DE and tonemap
 int enqueue(rf_batch* b) {
     cudaStream_t st = b->stream;
-    cudaError_t e = cudaMemsetAsync(b->queue, 0, sizeof(unsigned int), st);
+    cudaError_t e = cudaMemsetAsync(b->queue, 0, (b->groups.size() + 1) * sizeof(unsigned int), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->counters, 0, 3 * sizeof(unsigned long long), st);
     for (auto& it : b->items) {
         if (e != cudaSuccess) break;
@@ -181,7 +216,15 @@ int enqueue(rf_batch* b) {
         if (e == cudaSuccess) e = cudaMemsetAsync(it.hits, 0, nb * sizeof(uint32_t), st);
     }
     if (e != cudaSuccess) return cuda_err(e, "batch clear");
-    e = launch_batch((int)b->threads, (int)b->slots, args_for(b), st, nullptr);
+    for (size_t g = 0; g < b->groups.size() && e == cudaSuccess; g++) {
+        const SpecGroup& G = b->groups[g];
+        if (G.count)
+            e = launch_batch_spec(G.kernel, (int)b->threads, (int)b->slots, G.grid,
+                                  args_for(b, G.first, G.count, (uint32_t)g), st);
+    }
+    if (e == cudaSuccess && b->interp_count)
+        e = launch_batch((int)b->threads, (int)b->slots,
+                         args_for(b, b->interp_first, b->interp_count, (uint32_t)b->groups.size()), st, nullptr);
     if (e != cudaSuccess) return cuda_err(e, "batch kernel");
     for (size_t i = 0; i < b->items.size(); i++) {
         Item& it = b->items[i];
@@ -265,7 +308,7 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
         b->max_prog_words = std::max(b->max_prog_words, (uint32_t)it.prog.size());
         b->points += items[i].points;
     }
-    e = cudaMalloc((void**)&b->queue, sizeof(unsigned int));
+    e = cudaMalloc((void**)&b->queue, (kMaxSpecGroups + 1) * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->counters, 3 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->stats, 3 * sizeof(double) * n);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
@@ -331,6 +374,39 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
     per = std::max<uint64_t>(per, d->unit_passes ? 1 : 20ull * b->fuse);
     per = std::min<uint64_t>(per, 1u << 20);
     b->unit_passes = (uint32_t)per;
+    // --- genome-specialised kernels for structures that fill the GPU on their own (animation
+    // frames); the rest stays on the interpreted kernel
+    if (d->specialize >= 0) {
+        std::map<std::string, uint64_t> units_of;
+        for (auto& it : b->items) {
+            it.structure = spec_structure(it.prog);
+            units_of[it.structure] += std::max<uint64_t>(1, ((it.desc.points + b->slots - 1) / b->slots + per - 1) / per);
+        }
+        std::vector<std::pair<uint64_t, std::string>> big;
+        for (auto& kv : units_of)
+            if (kv.second >= (uint64_t)kSpecMinUnitsPerSM * sms) big.push_back({kv.second, kv.first});
+        std::sort(big.rbegin(), big.rend());
+        if (big.size() > kMaxSpecGroups) big.resize(kMaxSpecGroups);
+        for (auto& bg : big) {
+            const Item* rep = nullptr;
+            for (auto& it : b->items)
+                if (it.structure == bg.second) { rep = &it; break; }
+            const void* k = nullptr;
+            int rc = spec_kernel(rep->prog, (int)b->threads, (int)b->slots, b->device, &k, SpecKind::Batch);
+            int grid = rc == RF_OK ? batch_spec_grid(k, (int)b->threads, (int)b->slots, b->max_prog_words) : 0;
+            if (rc == RF_OK && grid == 0) rc = fail(RF_ERR_CUDA, "specialised batch kernel: no resident CTA");
+            if (rc != RF_OK) {
+                if (d->specialize > 0) return bail(rc);
+                continue;
+            }
+            SpecGroup G;
+            G.kernel = k;
+            G.grid = grid;
+            b->groups.push_back(G);
+            for (auto& it : b->items)
+                if (it.structure == bg.second) it.group = (int)b->groups.size() - 1;
+        }
+    }
     if (int rc = build_tables(b, b->slots, b->unit_passes, 0, n)) return bail(rc);
     if (d->use_graph) {
         e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
@@ -417,6 +493,11 @@ int rf_batch_read_bins(rf_batch* b, uint32_t i, float* host_rgba, uint32_t* host
     if (e == cudaSuccess && host_hits) e = cudaMemcpy(host_hits, it.hits, nb * sizeof(uint32_t), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_err(e, "rf_batch_read_bins");
     return RF_OK;
+}
+
+int rf_batch_specialized(const rf_batch* b, uint32_t i) {
+    if (!b || i >= b->items.size()) return -1;
+    return b->items[i].group >= 0 ? 1 : 0;
 }
 
 int rf_batch_splat(const rf_batch* b, uint32_t i) {

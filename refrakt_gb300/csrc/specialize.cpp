@@ -126,9 +126,10 @@ std::map<std::string, std::unique_ptr<Spec>> g_cache;  // key: device + source
 
 }  // namespace
 
-std::string spec_source(const std::vector<uint32_t>& prog, int threads, int spt) {
+// struct GenEval: one inlined evaluator per xform of this genome's structure
+static std::string gen_eval(const std::vector<uint32_t>& prog) {
     std::ostringstream o;
-    o << "// generated: genome-specialised chaos kernel\n#include \"chaos_body.cuh\"\nnamespace rfk {\n"
+    o << "namespace rfk {\n"
       << "struct GenEval {\n  static __device__ __forceinline__ void apply(const uint32_t* __restrict__ prog, int xi, "
          "uint32_t, float& x, float& y, float& c, float& op, bool first_run, Jsf& rng) {\n    switch (xi) {\n";
     const uint32_t nx = prog[H_NX];
@@ -142,12 +143,27 @@ std::string spec_source(const std::vector<uint32_t>& prog, int threads, int spt)
         emit_xform(o, prog, prog[H_FINAL], true);
         o << "      break; }\n";
     }
-    o << "    }\n  }\n};\n}  // namespace rfk\n"
-      << "extern \"C\" __global__ void __launch_bounds__(" << threads << ", " << 1024 / threads
-      << ") rfk_chaos_spec(const rfk::ChaosArgs A) {\n  rfk::chaos_body<" << threads << ", " << spt
-      << ", rfk::GenEval>(A);\n}\n";
+    o << "    }\n  }\n};\n}  // namespace rfk\n";
     return o.str();
 }
+
+std::string spec_source(const std::vector<uint32_t>& prog, int threads, int spt, SpecKind kind) {
+    std::ostringstream o;
+    o << "// generated: genome-specialised " << (kind == SpecKind::Batch ? "batch" : "chaos") << " kernel\n"
+      << (kind == SpecKind::Batch ? "#include \"batch_body.cuh\"\n" : "#include \"chaos_body.cuh\"\n")
+      << gen_eval(prog);
+    if (kind == SpecKind::Batch)
+        o << "extern \"C\" __global__ void __launch_bounds__(" << threads << ", " << 1024 / threads
+          << ") rfk_batch_spec(const rfk::BatchArgs A) {\n  rfk::batch_body<" << threads << ", " << spt
+          << ", rfk::GenEval>(A);\n}\n";
+    else
+        o << "extern \"C\" __global__ void __launch_bounds__(" << threads << ", " << 1024 / threads
+          << ") rfk_chaos_spec(const rfk::ChaosArgs A) {\n  rfk::chaos_body<" << threads << ", " << spt
+          << ", rfk::GenEval>(A);\n}\n";
+    return o.str();
+}
+
+std::string spec_structure(const std::vector<uint32_t>& prog) { return gen_eval(prog); }
 
 bool spec_available(std::string* why) {
     const Nvrtc& n = nvrtc();
@@ -179,11 +195,12 @@ int spec_compile(const std::string& src, std::vector<char>& cubin) {
     return RF_OK;
 }
 
-int spec_kernel(const std::vector<uint32_t>& prog, int threads, int slots, int device, const void** out) {
+int spec_kernel(const std::vector<uint32_t>& prog, int threads, int slots, int device, const void** out,
+                SpecKind kind) {
     *out = nullptr;
     if (prog.size() < (size_t)H_XOFF || prog[H_MAGIC] != kProgMagic)
         return fail(RF_ERR_INVALID_ARG, "spec_kernel: not a compiled genome");
-    const std::string src = spec_source(prog, threads, slots / threads);
+    const std::string src = spec_source(prog, threads, slots / threads, kind);
     const std::string key = std::to_string(device) + "\n" + src;
     std::lock_guard<std::mutex> lk(g_mu);
     auto it = g_cache.find(key);
@@ -195,7 +212,8 @@ int spec_kernel(const std::vector<uint32_t>& prog, int threads, int slots, int d
     if (int rc = spec_compile(src, cubin)) return rc;
     auto spec = std::make_unique<Spec>();
     cudaError_t e = cudaLibraryLoadData(&spec->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
-    if (e == cudaSuccess) e = cudaLibraryGetKernel(&spec->kernel, spec->lib, "rfk_chaos_spec");
+    if (e == cudaSuccess)
+        e = cudaLibraryGetKernel(&spec->kernel, spec->lib, kind == SpecKind::Batch ? "rfk_batch_spec" : "rfk_chaos_spec");
     if (e != cudaSuccess) return fail(RF_ERR_CUDA, std::string("loading the specialised kernel: ") + cudaGetErrorString(e));
     *out = reinterpret_cast<const void*>(spec->kernel);
     g_cache.emplace(key, std::move(spec));

@@ -156,3 +156,30 @@ def test_autotuned_shape_covers_points(rk, compiler):
     assert st["binned"] > 0.3 * sum(pts)
     for i in range(12):
         assert b.image(i)[..., :3].max() > 0
+
+
+@pytest.mark.parametrize("kind", ["affine", "random"])
+def test_specialised_group_equals_interpreted(rk, compiler, kind):
+    """A genome structure with >= 2 units per SM gets its own specialised persistent launch; its
+    histograms equal the interpreted kernel's count for count."""
+    if kind == "affine":
+        fl = [rk.Flame.from_xml(LINEAR, compiler)]
+    else:
+        fl = [rk.Flame.synthesize(compiler, rk.SYNTH_RANDOM, 2, 128, 128, n_xforms=5, final_xform=True)]
+    other = rk.Flame.synthesize(compiler, rk.SYNTH_SMALL, 3, 96, 96)
+    units = 2 * torch.cuda.get_device_properties(0).multi_processor_count + 8
+    items = [(fl[0], 128, 128, units * 1024 * 16, 21), (fl[0], 128, 128, 4 * 1024 * 16, 22), (other, 96, 96, 1024 * 16, 23)]
+    res = []
+    for spec in (0, -1):
+        b = rk.Batch(items, cta_slots=1024, unit_passes=16, density_estimation=False, specialize=spec)
+        info = b.info()
+        assert info["specialized"] == ([1, 1, 0] if spec == 0 else [0, 0, 0])
+        b.run()
+        st = b.sync()
+        res.append(([b.bins(i) for i in range(3)], st))
+        b.close()
+    (a, sa), (c, sc) = res
+    assert sa["points"] == sc["points"] and sa["binned"] == sc["binned"]
+    for i in range(3):
+        assert np.array_equal(a[i][1], c[i][1]), i
+        assert np.allclose(a[i][0], c[i][0], rtol=1e-4, atol=1e-3)
