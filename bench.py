@@ -525,20 +525,29 @@ def run_learned(args):
     tr = [LD.genome(R, comp, s, S, S) for s in tr_seeds]
     te = [LD.genome(R, comp, s, S, S) for s in te_seeds]
     levels = [int(x) for x in args.learned_spp.split(",")]
-    feats = [torch.empty(n_train, S, S, 8, dtype=torch.bfloat16, device="cuda") for _ in levels]
+    # one network over all input levels, or (separate) one network per level
+    groups = [[l] for l in levels] if args.learned_separate else [levels]
     targets = torch.empty(n_train, S, S, 3, device="cuda")
-    for k, spp in enumerate(levels):
-        LD.render_features(tr, S, S, spp, [s * 7 + 1 + 100 * k for s in tr_seeds], feats[k])
     LD.render_images(tr, S, S, 1000, [s * 7 + 2 for s in tr_seeds], targets)
-    torch.cuda.synchronize()
+    nets, losses, t_train = {}, {}, 0.0
     t_data = time.perf_counter() - t0
-    log("training data: %d genomes x %d input levels in %.1f s" % (n_train, len(levels), t_data))
-    net = R.Denoiser(4 * S * S, seed=7)
-    t0 = time.perf_counter()
-    losses = LD.train(net, feats, targets, args.learned_steps, batch=4, lr=1e-3, log=log)
-    torch.cuda.synchronize()
-    t_train = time.perf_counter() - t0
-    del feats, targets
+    for gi, grp in enumerate(groups):
+        t0 = time.perf_counter()
+        feats = [torch.empty(n_train, S, S, 8, dtype=torch.bfloat16, device="cuda") for _ in grp]
+        for k, spp in enumerate(grp):
+            LD.render_features(tr, S, S, spp, [s * 7 + 1 + 100 * levels.index(spp) for s in tr_seeds], feats[k])
+        torch.cuda.synchronize()
+        t_data += time.perf_counter() - t0
+        log("training data: %d genomes x input levels %s" % (n_train, grp))
+        net = R.Denoiser(4 * S * S, seed=7 + gi)
+        t0 = time.perf_counter()
+        ls = LD.train(net, feats, targets, args.learned_steps, batch=4, lr=1e-3, log=log)
+        torch.cuda.synchronize()
+        t_train += time.perf_counter() - t0
+        for spp in grp:
+            nets[spp], losses[spp] = net, (ls[0], ls[-1])
+        del feats
+    del targets
 
     # held-out evaluation against a 4000-spp adaptive-DE reference
     ref = torch.empty(n_test, S, S, 3, device="cuda")
@@ -553,11 +562,12 @@ def run_learned(args):
     learned = {}
     for spp in levels:
         LD.render_features(te, S, S, spp, [s * 7 + 20 + spp for s in te_seeds], f16)
-        LD.infer_all(net, f16, img)
+        LD.infer_all(nets[spp], f16, img)
         learned[spp] = float(LD.l1(img, ref).mean())
     equiv = {spp: LD.plain_equivalent_spp(spps, [plain[x] for x in spps], learned[spp]) for spp in learned}
     meets = [spp for spp in levels if learned[spp] <= plain[1000]]
     spp_fast = min(meets) if meets else min(levels)
+    net = nets[spp_fast]
     # 1080p frame, seconds per frame: plain (1000 spp + adaptive DE + tonemap) vs learned (16 spp + U-Net)
     W1, H1 = 1920, 1080
     f1 = LD.genome(R, comp, 1, W1, H1)
@@ -612,7 +622,8 @@ def run_learned(args):
         "plain_spp_equivalent": equiv,
         "iteration_ratio_at_plain_1000spp_error": None,
         "learned_reaches_plain_1000spp_error": learned[16] <= plain[1000],
-        "train": {"data_s": t_data, "train_s": t_train, "loss_first": losses[0], "loss_last": losses[-1]},
+        "train": {"data_s": t_data, "train_s": t_train, "separate_networks": bool(args.learned_separate),
+                  "loss_first_last": {str(k): v for k, v in losses.items()}},
         "fallback": {"bound": args.learned_bound, "frames": min(32, n_test), "fallbacks": fallbacks,
                      "correlation_with_true_l1": est_corr, "estimate_vs_true_l1": est_err[:8]},
         "gpu_launches": None,
@@ -647,6 +658,7 @@ def main():
     ap.add_argument("--learned-bound", type=float, default=0.02)
     ap.add_argument("--learned-spp", default="16,32,64,128", help="input sample counts the denoiser trains on")
     ap.add_argument("--learned-save", default="", help="write the trained parameters (.npy) here")
+    ap.add_argument("--learned-separate", action="store_true", help="one network per input level")
     ap.add_argument("--workload", default="frame1080", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     select_workload(args.workload)

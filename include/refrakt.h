@@ -351,6 +351,8 @@ typedef struct {
 RF_API int rf_denoiser_create(const rf_denoiser_desc* d, rf_denoiser** out);
 RF_API int rf_denoiser_destroy(rf_denoiser* d);
 RF_API int rf_denoiser_set_stream(rf_denoiser* d, void* stream);
+/* Waits for the denoiser's stream (infer returns without waiting). */
+RF_API int rf_denoiser_sync(rf_denoiser* d);
 RF_API int rf_denoiser_num_layers(const rf_denoiser* d);
 RF_API int rf_denoiser_layer(const rf_denoiser* d, int i, rf_denoiser_layer_info* out);
 /* Parameters in layer order, each layer its weights [out][tap][in_a + in_b] then its bias. */

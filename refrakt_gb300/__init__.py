@@ -158,6 +158,7 @@ _SIGS = {
     "rf_denoiser_create": ([ctypes.POINTER(DenoiserDesc), ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "rf_denoiser_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "rf_denoiser_set_stream": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rf_denoiser_sync": ([ctypes.c_void_p], ctypes.c_int),
     "rf_denoiser_num_layers": ([ctypes.c_void_p], ctypes.c_int),
     "rf_denoiser_layer": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(DenoiserLayer)], ctypes.c_int),
     "rf_denoiser_num_params": ([ctypes.c_void_p], ctypes.c_size_t),
@@ -618,9 +619,13 @@ class Denoiser:
         _check(library().rf_denoiser_gradients(self._h, a.ctypes.data_as(ctypes.c_void_p), a.size))
         return a
 
-    def infer(self, feats, out):
+    def infer(self, feats, out, sync=True):
+        """out = clamp(base + net(feats)); runs on the denoiser's stream and, with sync, waits
+        for it (the caller's stream may read `out` only after that)."""
         n, h, w = feats.shape[:3]
         _check(library().rf_denoiser_infer(self._h, _ptr(feats), n, h, w, _ptr(out)))
+        if sync:
+            _check(library().rf_denoiser_sync(self._h))
 
     def train_step(self, feats, target, lr):
         n, h, w = feats.shape[:3]

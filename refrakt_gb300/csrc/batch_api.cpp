@@ -409,6 +409,8 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
     }
     if (int rc = build_tables(b, b->slots, b->unit_passes, 0, n)) return bail(rc);
     if (d->use_graph) {
+        e = density_prepare();
+        if (e != cudaSuccess) return bail(cuda_err(e, "density estimation set-up"));
         e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return bail(cuda_err(e, "graph capture"));
         int rc = enqueue(b);

@@ -425,6 +425,14 @@ int rf_denoiser_set_stream(rf_denoiser* D, void* stream) {
     return RF_OK;
 }
 
+int rf_denoiser_sync(rf_denoiser* D) {
+    if (!D) return fail(RF_ERR_INVALID_ARG, "rf_denoiser_sync: null");
+    cudaSetDevice(D->device);
+    cudaError_t e = cudaStreamSynchronize(D->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "rf_denoiser_sync");
+    return RF_OK;
+}
+
 int rf_denoiser_num_layers(const rf_denoiser* D) { return D ? (int)D->convs.size() : -1; }
 
 int rf_denoiser_layer(const rf_denoiser* D, int i, rf_denoiser_layer_info* out) {

@@ -4,9 +4,10 @@
 // The reference does density estimation as a GL point-sprite raster pass with additive
 // blending (src/main.cpp:490-515, shaders/density_vert.glsl:26-63, density_frag.glsl:9-18):
 // every non-empty bin becomes a sprite of radius r = max(min, min(R, int(R / a^curve))) whose
-// fragments add color * (1 - d^2) * (2/pi) / r^2.  Here each CTA owns an output tile in shared
-// memory and every non-empty bin of the tile and its halo adds its disc's part inside the tile
-// (radii above 12 gather from global memory).  The disc is the symmetric restatement
+// fragments add color * (1 - d^2) * (2/pi) / r^2.  Here each CTA owns an output tile and gathers
+// it from the tile and its halo staged in shared memory, walking either the whole box of the
+// tile's largest radius or only its large discs, whichever is less work for that tile (radii
+// above 12 gather from global memory).  The disc is the symmetric restatement
 // 4 (dx^2 + dy^2) <= (2r + 1)^2 with
 // d^2 = (dx^2 + dy^2) / (r + 0.5)^2 (the GL sprite's sub-pixel centring depends on point
 // rasterisation rules).  Radii come from thresholds on a, computed on the host in FP64, and
@@ -52,56 +53,159 @@ __global__ void de_radius_kernel(const float4* __restrict__ in, size_t n, const 
     }
 }
 
-// pass 2: a CTA owns a 64 x 16 output tile in shared memory; every
-// non-empty bin of the tile and its R halo adds its disc's part inside the tile with shared-
-// memory atomics — the GL sprite pass restricted to one tile.  Work follows the sprites' area
-// (mostly radius 0 and 1 at converged sample counts) instead of the tile's largest radius.
+// pass 2: a CTA owns a 64 x 16 output tile.  It stages the colours and radii of the tile and
+// its R halo in shared memory and forms each output bin as a gather in one of two ways, chosen
+// per tile by their work:
+//   box  — sum the bins within the tile's largest radius rmax whose disc covers the output:
+//          (2 rmax + 1)^2 taps per output;
+//   list — the discs of radius 0 and 1 from the 3 x 3 neighbourhood, plus a compact list of the
+//          tile's larger discs (those reaching the tile), which every thread walks in the same
+//          order (shared-memory broadcasts): 9 + list-length taps per output.
+// Dense regions (radius 0 and 1 at converged sample counts, a few sparse bins) take the list;
+// sparse fringes full of large discs take the box.  The sum is deterministic either way.
 constexpr int kDsX = 64, kDsY = 16, kDsThreads = 256;
 
 template <int R>
-__global__ void __launch_bounds__(kDsThreads) de_scatter_kernel(
+__host__ __device__ constexpr size_t de_tile_smem() {
+    return (size_t)(kDsX + 2 * R) * (kDsY + 2 * R) * (16 + 4 + 1) + 16 + 64;
+}
+
+template <int R>
+__global__ void __launch_bounds__(kDsThreads) de_tile_kernel(
     const float4* __restrict__ in, const uint8_t* __restrict__ rad, uint32_t w, uint32_t h,
     const float* __restrict__ weights, const DeTables T, float4* __restrict__ out) {
-    constexpr int SW = kDsX + 2 * R, SH = kDsY + 2 * R;
-    __shared__ float s_acc[4][kDsY][kDsX];
-    float* acc = &s_acc[0][0][0];
-    for (int i = threadIdx.x; i < 4 * kDsY * kDsX; i += kDsThreads) acc[i] = 0.0f;
-    __syncthreads();
+    constexpr int SW = kDsX + 2 * R, SH = kDsY + 2 * R, NS = SW * SH, NO = kDsX * kDsY;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4* s_c = reinterpret_cast<float4*>(smem);                  // NS colours
+    int* s_list = reinterpret_cast<int*>(s_c + NS);                 // indices of discs of radius >= 2
+    uint8_t* s_r = reinterpret_cast<uint8_t*>(s_list + NS);         // NS radii (255: empty)
+    int* s_stat = reinterpret_cast<int*>(s_r + ((NS + 15) & ~15));  // [0] rmax, [1..8] per-warp counts
     const int tx0 = blockIdx.x * kDsX, ty0 = blockIdx.y * kDsY;
-    for (int i = threadIdx.x; i < SW * SH; i += kDsThreads) {
-        const int gx = tx0 - R + i % SW, gy = ty0 - R + i / SW;
-        if (gx < 0 || gy < 0 || gx >= (int)w || gy >= (int)h) continue;
-        const size_t gi = (size_t)gy * w + gx;
-        const int r = rad[gi];
-        if (r == 255) continue;
-        // the disc's bounding box inside the tile
-        const int xa = max(gx - r, tx0), xb = min(gx + r, min(tx0 + kDsX, (int)w) - 1);
-        const int ya = max(gy - r, ty0), yb = min(gy + r, min(ty0 + kDsY, (int)h) - 1);
-        if (xa > xb || ya > yb) continue;
-        const float4 v = in[gi];
-        const int lim = (2 * r + 1) * (2 * r + 1);
-        const float* wr = weights + T.wbase[r];
-        for (int oy = ya; oy <= yb; oy++) {
-            const int ay = oy > gy ? oy - gy : gy - oy;
-            for (int ox = xa; ox <= xb; ox++) {
-                const int ax = ox > gx ? ox - gx : gx - ox;
-                if (4 * (ax * ax + ay * ay) > lim) continue;
-                const float wt = r == 0 ? 1.0f : wr[ay * (r + 1) + ax];
-                const int o = (oy - ty0) * kDsX + (ox - tx0);
-                atomicAdd(acc + o, v.x * wt);
-                atomicAdd(acc + kDsY * kDsX + o, v.y * wt);
-                atomicAdd(acc + 2 * kDsY * kDsX + o, v.z * wt);
-                atomicAdd(acc + 3 * kDsY * kDsX + o, v.w * wt);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_stat[0] = 0;
+    int rmax = 0, nl = 0;
+    // stage the tile + halo; list the large discs that reach the tile in source order (a
+    // ballot-and-prefix compaction, so the list and the sums are the same on every run)
+    for (int i0 = 0; i0 < NS; i0 += kDsThreads) {
+        const int i = i0 + (int)threadIdx.x;
+        bool big = false;
+        if (i < NS) {
+            const int gx = tx0 - R + i % SW, gy = ty0 - R + i / SW;
+            uint8_t r = 255;
+            float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (gx >= 0 && gy >= 0 && gx < (int)w && gy < (int)h) {
+                const size_t gi = (size_t)gy * w + gx;
+                r = rad[gi];
+                if (r != 255) v = in[gi];
+            }
+            s_r[i] = r;
+            s_c[i] = v;
+            if (r != 255 && gx - r <= tx0 + kDsX - 1 && gx + r >= tx0 && gy - r <= ty0 + kDsY - 1 && gy + r >= ty0) {
+                rmax = max(rmax, (int)r);
+                big = r >= 2;
             }
         }
+        const unsigned m = __ballot_sync(0xffffffffu, big);
+        if (lane == 0) s_stat[1 + warp] = __popc(m);
+        __syncthreads();
+        int off = nl, tot = 0;
+        for (int q = 0; q < kDsThreads / 32; q++) {
+            const int c = s_stat[1 + q];
+            if (q < warp) off += c;
+            tot += c;
+        }
+        if (big) s_list[off + __popc(m & ((1u << lane) - 1u))] = i;
+        nl += tot;
+        __syncthreads();
     }
+    atomicMax(&s_stat[0], rmax);
     __syncthreads();
-    for (int i = threadIdx.x; i < kDsY * kDsX; i += kDsThreads) {
-        const int ox = tx0 + i % kDsX, oy = ty0 + i / kDsX;
-        if (ox < (int)w && oy < (int)h)
-            out[(size_t)oy * w + ox] = make_float4(acc[i], acc[kDsY * kDsX + i], acc[2 * kDsY * kDsX + i],
-                                                   acc[3 * kDsY * kDsX + i]);
+    const int rm = s_stat[0];
+    const bool use_list = 9 + nl < (2 * rm + 1) * (2 * rm + 1);
+    for (int o = threadIdx.x; o < NO; o += kDsThreads) {
+        const int ox = o % kDsX, oy = o / kDsX;
+        float4 a4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (use_list) {
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    const int si = (oy + R + dy) * SW + ox + R + dx;
+                    const int r = s_r[si];
+                    if (r > 1 || (r == 0 && (dx | dy))) continue;  // r = 255 (empty) fails r > 1
+                    const float wt = r == 0 ? 1.0f : weights[T.wbase[1] + (dy ? 1 : 0) * 2 + (dx ? 1 : 0)];
+                    const float4 v = s_c[si];
+                    a4.x = fmaf(v.x, wt, a4.x);
+                    a4.y = fmaf(v.y, wt, a4.y);
+                    a4.z = fmaf(v.z, wt, a4.z);
+                    a4.w = fmaf(v.w, wt, a4.w);
+                }
+            for (int k = 0; k < nl; k++) {
+                const int si = s_list[k];
+                const int r = s_r[si];
+                const int ax = abs(ox + R - si % SW), ay = abs(oy + R - si / SW);
+                if (4 * (ax * ax + ay * ay) > (2 * r + 1) * (2 * r + 1)) continue;
+                const float wt = weights[T.wbase[r] + ay * (r + 1) + ax];
+                const float4 v = s_c[si];
+                a4.x = fmaf(v.x, wt, a4.x);
+                a4.y = fmaf(v.y, wt, a4.y);
+                a4.z = fmaf(v.z, wt, a4.z);
+                a4.w = fmaf(v.w, wt, a4.w);
+            }
+        } else {
+            for (int dy = -rm; dy <= rm; dy++) {
+                const int ay = dy < 0 ? -dy : dy;
+                for (int dx = -rm; dx <= rm; dx++) {
+                    const int si = (oy + R + dy) * SW + ox + R + dx;
+                    const int r = s_r[si];
+                    const int ax = dx < 0 ? -dx : dx;
+                    if (r == 255 || ax > r || ay > r) continue;
+                    float wt = 1.0f;
+                    if (r > 0) {
+                        if (4 * (ax * ax + ay * ay) > (2 * r + 1) * (2 * r + 1)) continue;
+                        wt = weights[T.wbase[r] + ay * (r + 1) + ax];
+                    }
+                    const float4 v = s_c[si];
+                    a4.x = fmaf(v.x, wt, a4.x);
+                    a4.y = fmaf(v.y, wt, a4.y);
+                    a4.z = fmaf(v.z, wt, a4.z);
+                    a4.w = fmaf(v.w, wt, a4.w);
+                }
+            }
+        }
+        const int gx = tx0 + ox, gy = ty0 + oy;
+        if (gx < (int)w && gy < (int)h) out[(size_t)gy * w + gx] = a4;
     }
+}
+
+template <int R>
+static cudaError_t set_de_tile_smem() {
+    return cudaFuncSetAttribute(de_tile_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)de_tile_smem<R>());
+}
+
+// the DE kernels' shared-memory limits, set once per device before any launch (also before a
+// stream capture that contains DE)
+cudaError_t density_prepare() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    static bool done[64] = {};
+    if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+    e = set_de_tile_smem<3>();
+    if (e == cudaSuccess) e = set_de_tile_smem<6>();
+    if (e == cudaSuccess) e = set_de_tile_smem<9>();
+    if (e == cudaSuccess) e = set_de_tile_smem<kDeMaxSmemR>();
+    if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
+    return e;
+}
+
+template <int R>
+static cudaError_t launch_de_tile(const float4* in, const uint8_t* rad, uint32_t w, uint32_t h, const float* dw,
+                                  const DeTables& T, float4* out, cudaStream_t st) {
+    const size_t smem = de_tile_smem<R>();
+    cudaError_t e = density_prepare();
+    if (e != cudaSuccess) return e;
+    const dim3 grid((w + kDsX - 1) / kDsX, (h + kDsY - 1) / kDsY);
+    de_tile_kernel<R><<<grid, kDsThreads, smem, st>>>(in, rad, w, h, dw, T, out);
+    return cudaGetLastError();
 }
 
 // large radii: the gather straight from global memory
@@ -287,11 +391,10 @@ static cudaError_t launch_density_passes(const float4* in, uint32_t w, uint32_t 
     const size_t n = (size_t)w * h;
     de_radius_kernel<<<1024, 256, 0, st>>>(in, n, T, rad);
     const int rmax = T.R > T.min_r ? T.R : T.min_r;
-    const dim3 grid((w + kDsX - 1) / kDsX, (h + kDsY - 1) / kDsY);
-    if (rmax <= 3) de_scatter_kernel<3><<<grid, kDsThreads, 0, st>>>(in, rad, w, h, dw, T, out);
-    else if (rmax <= 6) de_scatter_kernel<6><<<grid, kDsThreads, 0, st>>>(in, rad, w, h, dw, T, out);
-    else if (rmax <= 9) de_scatter_kernel<9><<<grid, kDsThreads, 0, st>>>(in, rad, w, h, dw, T, out);
-    else if (rmax <= kDeMaxSmemR) de_scatter_kernel<kDeMaxSmemR><<<grid, kDsThreads, 0, st>>>(in, rad, w, h, dw, T, out);
+    if (rmax <= 3) return launch_de_tile<3>(in, rad, w, h, dw, T, out, st);
+    if (rmax <= 6) return launch_de_tile<6>(in, rad, w, h, dw, T, out, st);
+    if (rmax <= 9) return launch_de_tile<9>(in, rad, w, h, dw, T, out, st);
+    if (rmax <= kDeMaxSmemR) return launch_de_tile<kDeMaxSmemR>(in, rad, w, h, dw, T, out, st);
     else de_gather_global_kernel<<<dim3((w + 127) / 128, h), 128, 0, st>>>(in, rad, w, h, dw, T, out);
     return cudaGetLastError();
 }

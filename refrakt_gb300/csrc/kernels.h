@@ -35,6 +35,7 @@ cudaError_t launch_density_scratch(const float4* in, uint32_t w, uint32_t h, int
 // device (`dw`) and a byte of radius scratch per bin (`rad`) — no allocation and no host copy,
 // so the passes can be captured in a CUDA graph and replayed.
 void density_weights(int radius, int min_radius, std::vector<float>& out);
+cudaError_t density_prepare();  // per-device kernel attributes; call before capturing DE in a graph
 cudaError_t launch_density_resident(const float4* in, uint32_t w, uint32_t h, int radius, int min_radius,
                                     float curve, float4* out, uint8_t* radius_scratch, const float* weights,
                                     cudaStream_t st);

@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 
 def test_small_pipeline(rk, compiler):
     from refrakt_gb300 import learned as LD
-    S, n = 64, 24
+    S, n = 128, 32
     seeds = list(range(1000, 1000 + n))
     fl = [LD.genome(rk, compiler, s, S, S) for s in seeds]
     feats = torch.empty(n, S, S, 8, dtype=torch.bfloat16, device="cuda")
