@@ -55,7 +55,6 @@ struct rf_denoiser {
     cudaStream_t stream = nullptr;
     std::vector<Conv> convs;
     std::vector<Act> acts;          // acts[i] = output of convs[i]; pools appended after
-    std::vector<int> pool_of;       // pool activation index feeding each level 1..3 (-1 at 0)
     int out_conv = -1;
     uint64_t P0 = 0;                // pixels at level 0 (max)
     uint32_t H = 0, W = 0, N = 0;   // current shape
@@ -68,7 +67,6 @@ struct rf_denoiser {
     float* z = nullptr;             // [P0 x 3] output head
     __nv_bfloat16 *dpred = nullptr, *dpred_t = nullptr;
     double* loss = nullptr;
-    size_t col_elems = 0, dx_elems = 0;
     uint32_t step = 0;
     std::vector<void*> allocs;
 };
@@ -115,16 +113,13 @@ void build_graph(rf_denoiser* D) {
     int prev = -1;
     uint32_t cin = kIn;
     std::vector<int> skip(4, -1);
-    std::vector<int> pools;
     for (int l = 0; l < 4; l++) {
         int a = conv(cin, 0, kCh[l], l, prev, -1, 0, 9, 1);
         int b = conv(kCh[l], 0, kCh[l], l, a, -1, 0, 9, 1);
         skip[l] = b;
         prev = b;
         cin = kCh[l];
-        if (l < 3) pools.push_back(b);  // pooled into level l + 1 (activation appended below)
     }
-    // pool activations: index = acts.size() + i, filled after the convs are known
     // decoder
     int low = skip[3];
     for (int l = 2; l >= 0; l--) {
@@ -134,20 +129,16 @@ void build_graph(rf_denoiser* D) {
     }
     D->out_conv = conv(kCh[0], 0, 3, 0, low, -1, 0, 1, 0);
     // pooled activations: the input of encoder conv 'a' at levels 1..3
-    D->pool_of.assign(4, -1);
     for (int l = 1; l < 4; l++) {
         Act p{};
         p.c = kCh[l - 1];
         p.level = l;
         D->acts.push_back(p);
         const int pi = (int)D->acts.size() - 1;
-        D->pool_of[l] = pi;
         // encoder conv 'a' of level l is convs[2 l]; its input is the pool of level l - 1's output
         D->convs[2 * l].src_a = pi;
     }
 }
-
-uint32_t act_src_c(const rf_denoiser* D, int idx) { return idx < 0 ? kIn : D->acts[idx].c; }
 
 // ---- forward ---------------------------------------------------------------------------------
 int forward(rf_denoiser* D, const __nv_bfloat16* input, bool need_out) {
@@ -390,8 +381,6 @@ int rf_denoiser_create(const rf_denoiser_desc* desc, rf_denoiser** out) {
         dx = std::max<size_t>(dx, P * (c.ca + c.cb));
         dz = std::max<size_t>(dz, P * std::max<uint32_t>(c.cout, 8));
     }
-    D->col_elems = col;
-    D->dx_elems = dx;
     if (e == cudaSuccess) e = dalloc(D, &D->col, col);
     if (e == cudaSuccess) e = dalloc(D, &D->colt, col);
     if (e == cudaSuccess) e = dalloc(D, &D->dz, dz);

@@ -118,7 +118,6 @@ void emit_xform(std::ostringstream& o, const std::vector<uint32_t>& prog, uint32
 struct Spec {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t kernel = nullptr;
-    size_t smem_set = 0;
 };
 
 std::mutex g_mu;
