@@ -53,7 +53,7 @@ __global__ void de_radius_kernel(const float4* __restrict__ in, size_t n, const 
     }
 }
 
-// pass 2: a CTA owns a 64 x 16 output tile.  It stages the colours and radii of the tile and
+// pass 2: a CTA owns a 32 x 8 output tile.  It stages the colours and radii of the tile and
 // its R halo in shared memory and forms each output bin as a gather in one of two ways, chosen
 // per tile by their work:
 //   box  — sum the bins within the tile's largest radius rmax whose disc covers the output:
@@ -63,7 +63,7 @@ __global__ void de_radius_kernel(const float4* __restrict__ in, size_t n, const 
 //          order (shared-memory broadcasts): 9 + list-length taps per output.
 // Dense regions (radius 0 and 1 at converged sample counts, a few sparse bins) take the list;
 // sparse fringes full of large discs take the box.  The sum is deterministic either way.
-constexpr int kDsX = 64, kDsY = 16, kDsThreads = 256;
+constexpr int kDsX = 32, kDsY = 8, kDsThreads = 256;
 
 template <int R>
 __host__ __device__ constexpr size_t de_tile_smem() {
