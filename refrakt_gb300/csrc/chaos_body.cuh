@@ -25,18 +25,6 @@
 
 namespace rfk {
 
-// Slot of thread `tid` within each consecutive block of THREADS slots.  Warp w runs on scheduler
-// w % 4 (SMSP), so warps w, w + 4, w + 8, ... are given consecutive 32-slot runs: at any moment
-// the warps of one scheduler serve the same 256-slot group and so the same xform — one code path
-// in that scheduler's instruction cache instead of up to four.  Which thread serves which slot
-// changes nothing else: RNG states, walkers and xform draws belong to slots.
-template <int THREADS>
-__device__ __forceinline__ uint32_t slot_lane(int tid) {
-    constexpr int kWarpsPerSmsp = THREADS / 128;
-    const int w = tid >> 5;
-    return (uint32_t)((((w & 3) * kWarpsPerSmsp) + (w >> 2)) * 32 + (tid & 31));
-}
-
 struct InterpEval {
     static __device__ __forceinline__ void apply(const uint32_t* prog, int xi, uint32_t final_off, float& x, float& y,
                                                  float& c, float& op, bool first_run, Jsf& rng) {
@@ -60,7 +48,7 @@ __host__ __device__ inline size_t chaos_smem_bytes(int slots, uint32_t prog_word
 
 // One CTA of THREADS threads owns SLOTS = THREADS * SPT walker slots — the walker shuffle's mixing
 // domain — for the launch's passes.  Every slot's walker and JSF32 state live in shared memory;
-// each thread serves SPT slots per pass (slots k * THREADS + rt, in SPT different 256-slot
+// each thread serves SPT slots per pass (slots k * THREADS + tid, in SPT different 256-slot
 // groups, so a warp's work per pass averages over SPT xforms).  64 registers per thread:
 // 1024 threads x 1, 512 x 2 or 256 x 4 CTAs per SM.
 template <int THREADS, int SPT, class Eval>
@@ -76,7 +64,6 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
     uint32_t* s_perm = reinterpret_cast<uint32_t*>(s_xid + 2 * G);
 
     const int tid = threadIdx.x;
-    const uint32_t rt = slot_lane<THREADS>(tid);  // this thread's slot within each block of THREADS slots
     const uint32_t chunk = blockIdx.x;  // mixing domain
     const uint32_t ts = chunk / A.chunks_per_ts;
     const uint32_t gid0 = (chunk - ts * A.chunks_per_ts) * SLOTS;  // first slot within the temporal sample
@@ -93,7 +80,7 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
     // sample (pass 0 of a warmup reads the start points instead, flame.glsl:58-61)
     const uint64_t gkey = derive_key(A.seed, A.pass0, ts, TAG_GLOBAL);
     for (int k = 0; k < SPT; k++) {
-        const uint32_t ls = k * THREADS + rt;
+        const uint32_t ls = k * THREADS + tid;
         s_rng[ls] = A.rng[ts_base + gid0 + ls];
         const uint32_t src = feistel(gid0 + ls, A.ppts, gkey);
         float4 w;
@@ -110,7 +97,7 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
 
     const uint32_t foff = s_prog[H_FINAL];
     const bool has_final = A.draw && foff != 0;
-    const bool lane0 = (rt % kGroup) == 0;
+    const bool lane0 = (tid % kGroup) == 0;
     const float W = (float)A.W, H = (float)A.H;
     uint32_t drawn = 0, emitted = 0;
 
@@ -120,11 +107,11 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
         uint32_t src[SPT];
 #pragma unroll
         for (int k = 0; k < SPT; k++)
-            src[k] = (s == 0) ? (uint32_t)(k * THREADS + rt) : (uint32_t)A.table[(size_t)s_perm[s] * SLOTS + k * THREADS + rt];
+            src[k] = (s == 0) ? (uint32_t)(k * THREADS + tid) : (uint32_t)A.table[(size_t)s_perm[s] * SLOTS + k * THREADS + tid];
         if (lane0) {  // flame.glsl:51-53: the group's first slot draws the group's xform
 #pragma unroll 1
             for (int k = 0; k < SPT; k++) {
-                const uint32_t ls = k * THREADS + rt;
+                const uint32_t ls = k * THREADS + tid;
                 const uint4 r4 = s_rng[ls];
                 Jsf rng{r4.x, r4.y, r4.z, r4.w};
                 const int xi = select_xform(s_prog, randf(rng));
@@ -137,7 +124,7 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
         __syncthreads();
 #pragma unroll 1
         for (int k = 0; k < SPT; k++) {
-            const uint32_t ls = k * THREADS + rt;
+            const uint32_t ls = k * THREADS + tid;
             uint32_t j = src[0];
 #pragma unroll
             for (int q = 1; q < SPT; q++)
@@ -192,7 +179,7 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
     // each slot's final walker and state were written by the thread that owns the slot
     const int out_buf = A.steps & 1;
     for (int k = 0; k < SPT; k++) {
-        const uint32_t ls = k * THREADS + rt;
+        const uint32_t ls = k * THREADS + tid;
         A.walk_out[ts_base + gid0 + ls] = s_w[out_buf * SLOTS + ls];
         A.rng[ts_base + gid0 + ls] = s_rng[ls];
     }
