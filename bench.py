@@ -434,6 +434,7 @@ def run_batch(args):
     n_img = len(items)
     b = R.Batch(items, fuse_passes=FUSE, density_estimation=True, device=local)
     info = b.info()
+    spec_groups = len({items[i][0].kernel_source() for i, sp in enumerate(info["specialized"]) if sp})
 
     def barrier():
         if ws > 1:
@@ -490,7 +491,9 @@ def run_batch(args):
         "frames_per_s": n_img / (ms_step * 1e-3),
         "binned_fraction": st["binned"] / st["points"],
         "wall_ms_per_step": wall / args.steps,
-        "gpu_launches": (1 + sum(5 for _ in items)) * args.steps,
+        # per batch: the persistent chaos launches (one per specialised structure group + the
+        # interpreted one) and per image DE radius + DE gather + FP64 stats + tonemap
+        "gpu_launches": (spec_groups + (1 if 0 in info["specialized"] else 0) + 4 * n_img) * args.steps,
         "e2e": {"value": replica_throughput(st["points"], statistics.median(e2e_ms)), "unit": "Gpoints/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "frames_per_s": n_img / (e2e_step * 1e-3),
                 "includes": "genome parse + compile + upload + autotune + graph capture + run + image readback"},
@@ -541,7 +544,8 @@ def run_learned(args):
         log("training data: %d genomes x input levels %s" % (n_train, grp))
         net = R.Denoiser(4 * S * S, seed=7 + gi)
         t0 = time.perf_counter()
-        ls = LD.train(net, feats, targets, args.learned_steps, batch=4, lr=1e-3, log=log)
+        ls = LD.train(net, feats, targets, args.learned_steps, batch=args.learned_batch, lr=1e-3, log=log,
+                      crop=args.learned_crop)
         torch.cuda.synchronize()
         t_train += time.perf_counter() - t0
         for spp in grp:
@@ -613,7 +617,8 @@ def run_learned(args):
         "dtype": "bf16", "data": "synthetic genomes rendered by the library (seeds 1000-2999 train, 3000-%d test)" %
                                   (3000 + n_test - 1),
         "config": {"workload": CONFIG_NAME, "train_genomes": n_train, "test_genomes": n_test,
-                   "train_steps": args.learned_steps, "batch": 4, "resolution": [S, S],
+                   "train_steps": args.learned_steps, "batch": args.learned_batch, "crop": args.learned_crop,
+                   "resolution": [S, S],
                    "params": net.num_params(), "input_spp": levels, "target_spp": 1000, "reference_spp": 4000,
                    "frame_spp_learned": spp_fast},
         "plain_s_per_frame": times["plain"],
@@ -659,6 +664,8 @@ def main():
     ap.add_argument("--learned-spp", default="16,32,64,128", help="input sample counts the denoiser trains on")
     ap.add_argument("--learned-save", default="", help="write the trained parameters (.npy) here")
     ap.add_argument("--learned-separate", action="store_true", help="one network per input level")
+    ap.add_argument("--learned-batch", type=int, default=4)
+    ap.add_argument("--learned-crop", type=int, default=0, help="random crops of this size (0: whole images)")
     ap.add_argument("--workload", default="frame1080", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     select_workload(args.workload)

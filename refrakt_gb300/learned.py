@@ -69,20 +69,27 @@ def l1(a, b):
     return (a - b).abs().flatten(1).mean(1)
 
 
-def train(net, feats, targets, steps, batch=4, lr=1e-3, seed=0, log=None):
-    """Adam on random minibatches of whole images; cosine learning-rate decay to lr / 20.
-    `feats` is one [n, h, w, 8] tensor or a list of them (one per input sample count, each
-    against the same targets): every minibatch image draws its sample count at random."""
+def train(net, feats, targets, steps, batch=4, lr=1e-3, seed=0, log=None, crop=0):
+    """Adam on random minibatches; cosine learning-rate decay to lr / 20.  `feats` is one
+    [n, h, w, 8] tensor or a list of them (one per input sample count, each against the same
+    targets): every minibatch image draws its sample count at random.  With `crop` (a multiple
+    of 8) each minibatch entry is a random crop of that size, so one step sees more genomes."""
     import torch
     g = torch.Generator().manual_seed(seed)
     levels = feats if isinstance(feats, (list, tuple)) else [feats]
-    n = levels[0].shape[0]
+    n, H, W = levels[0].shape[:3]
     losses = []
     for s in range(steps):
         idx = torch.randint(0, n, (batch,), generator=g).tolist()
         lv = torch.randint(0, len(levels), (batch,), generator=g).tolist()
-        f = torch.stack([levels[l][i] for l, i in zip(lv, idx)])
-        t = torch.stack([targets[i] for i in idx])
+        if crop:
+            ys = (torch.randint(0, (H - crop) // 8 + 1, (batch,), generator=g) * 8).tolist()
+            xs = (torch.randint(0, (W - crop) // 8 + 1, (batch,), generator=g) * 8).tolist()
+            f = torch.stack([levels[l][i, y:y + crop, x:x + crop] for l, i, y, x in zip(lv, idx, ys, xs)])
+            t = torch.stack([targets[i, y:y + crop, x:x + crop] for i, y, x in zip(idx, ys, xs)])
+        else:
+            f = torch.stack([levels[l][i] for l, i in zip(lv, idx)])
+            t = torch.stack([targets[i] for i in idx])
         # random flips keep the attractors' orientation statistics symmetric
         if s % 2:
             f, t = f.flip(2).contiguous(), t.flip(2).contiguous()
