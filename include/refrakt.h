@@ -183,6 +183,12 @@ enum rf_splat { RF_SPLAT_AUTO = 0, RF_SPLAT_GLOBAL = 1, RF_SPLAT_WARP = 2 };
    every walker, drawing into caller-owned device bins.  bins_hits may be NULL.  When `drawn`
    is non-NULL the call synchronises and stores the number of points binned (the reference's
    return value); when NULL it returns without synchronising. */
+/* Bin layout of the drawing passes: the caller's planes directly (DIRECT), or interleaved 32-byte
+   records {RGBA, count} in a library buffer merged into the caller's planes at the end of each
+   draw call (INTERLEAVED: one DRAM sector per point instead of two; pays for itself when the bins
+   exceed L2).  AUTO: INTERLEAVED when a count plane is given and the planes exceed 256 MB. */
+enum rf_bin_layout { RF_BINS_AUTO = 0, RF_BINS_DIRECT = 1, RF_BINS_INTERLEAVED = 2 };
+RF_API int  rf_set_bin_layout(rf_sim* s, int layout);
 RF_API int  rf_draw_to_bins(rf_sim* s, rf_flame* f, float* bins_rgba, uint32_t* bins_hits,
                      uint32_t width, uint32_t height, uint32_t num_iter, uint64_t* drawn);
 RF_API int  rf_set_splat(rf_sim* s, int splat);

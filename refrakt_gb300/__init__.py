@@ -16,7 +16,7 @@ import os
 __all__ = ["RefraktError", "FlameCompiler", "Flame", "Sim", "library", "build", "density_estimate",
            "tonemap", "hist_stats", "shuffle_generate", "probe_xform", "write_png", "render",
            "SYNTH_SMALL", "SYNTH_RANDOM", "SYNTH_CONTRACT", "SYNTH_SPACEFILL",
-           "SPLAT_AUTO", "SPLAT_GLOBAL", "SPLAT_WARP", "Batch", "Denoiser", "denoiser_features", "gemm_bf16",
+           "SPLAT_AUTO", "SPLAT_GLOBAL", "SPLAT_WARP", "BINS_AUTO", "BINS_DIRECT", "BINS_INTERLEAVED", "Batch", "Denoiser", "denoiser_features", "gemm_bf16",
            "GEMM_STORE_F32", "GEMM_STORE_BF16", "GEMM_ATOMIC_F32"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "librefrakt_gb300.so")
 
 SYNTH_SMALL, SYNTH_RANDOM, SYNTH_CONTRACT, SYNTH_SPACEFILL = 0, 1, 2, 3
 SPLAT_AUTO, SPLAT_GLOBAL, SPLAT_WARP = 0, 1, 2
+BINS_AUTO, BINS_DIRECT, BINS_INTERLEAVED = 0, 1, 2
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "PARSE", 3: "UNKNOWN_NAME", 4: "UNSUPPORTED", 5: "CAPACITY",
           6: "CUDA", 7: "NEEDS_WARMUP", 8: "IO", 9: "NO_DEVICE"}
@@ -126,6 +127,7 @@ _SIGS = {
     "rf_draw_to_bins": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                          ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "rf_set_splat": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rf_set_bin_layout": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rf_sim_counters": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "rf_density_estimate": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
                              ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
@@ -429,6 +431,10 @@ class Sim:
 
     def set_splat(self, splat):
         _check(library().rf_set_splat(self._h, splat))
+
+    def set_bin_layout(self, layout):
+        """BINS_AUTO, BINS_DIRECT or BINS_INTERLEAVED (rf_set_bin_layout)."""
+        _check(library().rf_set_bin_layout(self._h, layout))
 
     def draw_to_bins(self, flame, bins_rgba, bins_hits, width, height, num_iter, sync=True):
         drawn = ctypes.c_uint64(0)

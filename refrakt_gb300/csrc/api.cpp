@@ -44,6 +44,8 @@ using namespace rfk;
 
 namespace {
 
+constexpr size_t kInterleaveMinBytes = 256ull << 20;  // bins + counts above ~2x L2: interleave
+
 int set_device(const rf_sim* s) {
     cudaError_t e = cudaSetDevice(s->device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
@@ -82,6 +84,8 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.first_run = (first_run && done == 0) ? 1 : 0;
         a.draw = draw ? 1 : 0;
         a.splat = s->splat == RF_SPLAT_WARP ? 1 : (s->splat == RF_SPLAT_GLOBAL ? 0 : 2);
+        a.rgba_shift = s->rgba_shift;
+        a.count_shift = s->count_shift;
         if (ss) memcpy(a.ss, ss, sizeof(a.ss));
         a.W = W;
         a.H = H;
@@ -101,6 +105,33 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         s->pass += steps;
         done += steps;
     }
+    return RF_OK;
+}
+
+// The drawing passes into the caller's planes, or — for histograms well above L2 with a count
+// plane — into interleaved 32-byte records (RGBA and count in one DRAM sector) merged into the
+// caller's planes afterwards.
+int draw_passes(rf_sim* s, uint32_t passes, float4* bins, uint32_t* hits, uint32_t W, uint32_t H, const float ss[6]) {
+    const size_t nb = (size_t)W * H;
+    bool il = s->bin_layout == RF_BINS_INTERLEAVED;
+    if (s->bin_layout == RF_BINS_AUTO) il = hits != nullptr && nb * 20 > kInterleaveMinBytes;
+    if (!il) return launch_passes(s, passes, false, true, bins, hits, W, H, ss);
+    if (s->rec_n < nb) {
+        cudaFree(s->rec);
+        s->rec = nullptr;
+        s->rec_n = 0;
+        RF_CUDA(cudaMalloc((void**)&s->rec, nb * 32));
+        RF_CUDA(cudaMemsetAsync(s->rec, 0, nb * 32, s->stream));
+        s->rec_n = nb;
+    }
+    s->rgba_shift = 1;
+    s->count_shift = 3;
+    const int rc = launch_passes(s, passes, false, true, s->rec, hits ? reinterpret_cast<uint32_t*>(s->rec) + 4 : nullptr,
+                                 W, H, ss);
+    s->rgba_shift = 0;
+    s->count_shift = 0;
+    if (rc) return rc;
+    RF_CUDA(launch_merge_records(s->rec, nb, bins, hits, s->stream));
     return RF_OK;
 }
 
@@ -371,7 +402,7 @@ int rf_sim_destroy(rf_sim* s) {
     if (!s) return RF_OK;
     cudaSetDevice(s->device);
     cudaStreamSynchronize(s->stream);
-    void* ptrs[] = {s->walk[0], s->walk[1], s->rng, s->table, s->base_prog, s->progs, s->palette, s->counters,
+    void* ptrs[] = {s->rec, s->walk[0], s->walk[1], s->rng, s->table, s->base_prog, s->progs, s->palette, s->counters,
                     s->trace, s->r_bins, s->r_hits, s->r_de, s->r_img, s->r_stats};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -468,6 +499,12 @@ int rf_flame_kernel_compile(const rf_flame* f, uint32_t cta_threads, uint32_t ct
     return RF_OK;
 }
 
+int rf_set_bin_layout(rf_sim* s, int layout) {
+    if (!s || layout < RF_BINS_AUTO || layout > RF_BINS_INTERLEAVED) return fail(RF_ERR_INVALID_ARG, "rf_set_bin_layout: bad arguments");
+    s->bin_layout = layout;
+    return RF_OK;
+}
+
 int rf_set_splat(rf_sim* s, int splat) {
     if (!s) return fail(RF_ERR_INVALID_ARG, "rf_set_splat: null sim");
     s->splat = splat;
@@ -487,7 +524,7 @@ int rf_draw_to_bins(rf_sim* s, rf_flame* f, float* bins_rgba, uint32_t* bins_hit
     genome_screen_affine(f->g, W, H, ss);
     // [0] drawn, [1] emitted count this call
     RF_CUDA(cudaMemsetAsync(s->counters, 0, 2 * sizeof(unsigned long long), s->stream));
-    if (int rc = launch_passes(s, num_iter, false, true, (float4*)bins_rgba, bins_hits, W, H, ss)) return rc;
+    if (int rc = draw_passes(s, num_iter, (float4*)bins_rgba, bins_hits, W, H, ss)) return rc;
     if (drawn) {
         unsigned long long c[1];
         RF_CUDA(cudaStreamSynchronize(s->stream));
@@ -623,7 +660,7 @@ int rf_render(rf_sim* s, rf_flame* f, const rf_render_desc* d, uint8_t* out, dou
     if (e == cudaSuccess) e = cudaMemsetAsync(s->r_hits, 0, nb * sizeof(uint32_t), s->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s->counters, 0, 2 * sizeof(unsigned long long), s->stream);
     if (e != cudaSuccess) return done(cuda_fail(e, "rf_render clear"));
-    if (int rc = launch_passes(s, (uint32_t)passes, false, true, s->r_bins, s->r_hits, W, H, ssa)) return done(rc);
+    if (int rc = draw_passes(s, (uint32_t)passes, s->r_bins, s->r_hits, W, H, ssa)) return done(rc);
     const float4* src = s->r_bins;
     if (d->density_estimation && (f->g.est_radius > 0 || f->g.est_min > 0)) {
         const int R = std::min(100, f->g.est_radius), mn = std::min(100, f->g.est_min);

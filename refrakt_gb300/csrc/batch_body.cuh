@@ -133,8 +133,9 @@ __device__ __forceinline__ void batch_body(const BatchArgs& A) {
                         val = make_float4(col.x, col.y, col.z, op);
                         drawn++;
                     }
-                    if (I.splat) splat_warp(I.bins, I.hits, bin, val);
-                    else splat_global(I.bins, I.hits, bin, val);
+                    const BinTarget t{I.bins, I.hits, 0u, 0u};
+                    if (I.splat) splat_warp(t, bin, val);
+                    else splat_global(t, bin, val);
                 }
             }
         }

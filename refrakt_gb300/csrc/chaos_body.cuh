@@ -170,9 +170,10 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
                     val = make_float4(col.x, col.y, col.z, op);
                     drawn++;
                 }
-                if (A.splat == 1) splat_warp(A.bins, A.hits, bin, val);
-                else if (A.splat == 2) splat_adaptive(A.bins, A.hits, bin, val);
-                else splat_global(A.bins, A.hits, bin, val);
+                const BinTarget t{A.bins, A.hits, A.rgba_shift, A.count_shift};
+                if (A.splat == 1) splat_warp(t, bin, val);
+                else if (A.splat == 2) splat_adaptive(t, bin, val);
+                else splat_global(t, bin, val);
             }
         }
     }

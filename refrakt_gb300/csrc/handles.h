@@ -37,6 +37,10 @@ struct rf_sim {
     uint32_t pass = 0;
     int splat = RF_SPLAT_AUTO;
     const void* spec = nullptr;  // genome-specialised kernel of the warmed flame (specialize.cpp)
+    int bin_layout = RF_BINS_AUTO;
+    uint32_t rgba_shift = 0, count_shift = 0;  // BinTarget addressing of the next launches
+    float4* rec = nullptr;       // interleaved bin records (32 B per bin), all zero between calls
+    size_t rec_n = 0;
     // rf_render scratch
     float4* r_bins = nullptr;
     uint32_t* r_hits = nullptr;

@@ -13,6 +13,31 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) chaos_kernel(const Ch
     chaos_body<THREADS, SPT, InterpEval>(A);
 }
 
+// Interleaved bin records (32 bytes: float4 RGBA, uint32 count, pad) added into the caller's
+// planes, then cleared for the next call.
+__global__ void merge_records_kernel(float4* __restrict__ rec, size_t n, float4* __restrict__ bins,
+                                     uint32_t* __restrict__ hits) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 v = rec[2 * i];
+        const uint32_t c = reinterpret_cast<const uint32_t*>(rec + 2 * i + 1)[0];
+        if (v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f) {
+            float4 b = bins[i];
+            b.x += v.x; b.y += v.y; b.z += v.z; b.w += v.w;
+            bins[i] = b;
+            rec[2 * i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        if (c) {
+            if (hits) hits[i] += c;
+            rec[2 * i + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
+}
+
+cudaError_t launch_merge_records(float4* rec, size_t n, float4* bins, uint32_t* hits, cudaStream_t st) {
+    merge_records_kernel<<<152 * 16, 256, 0, st>>>(rec, n, bins, hits);
+    return cudaGetLastError();
+}
+
 // src/flame.cpp:138-141 — slot i seeded with warmup_ctx(i + seed * N)
 __global__ void init_rng_kernel(uint4* rng, uint64_t n, uint64_t seed) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;

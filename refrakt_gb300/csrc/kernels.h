@@ -16,6 +16,7 @@ namespace rfk {
 size_t chaos_smem(int slots, uint32_t prog_words, uint32_t steps);
 bool chaos_shape_supported(int threads, int slots);
 cudaError_t launch_chaos(int threads, int slots, const ChaosArgs& a, uint32_t grid, cudaStream_t st);
+cudaError_t launch_merge_records(float4* rec, size_t n, float4* bins, uint32_t* hits, cudaStream_t st);
 cudaError_t launch_init_rng(uint4* rng, uint64_t n, uint64_t seed, cudaStream_t st);
 cudaError_t launch_shuffle_table(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed, cudaStream_t st);
 cudaError_t launch_animate(const uint32_t* base, uint32_t words, uint32_t T, float tss, uint32_t* out,

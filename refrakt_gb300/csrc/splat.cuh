@@ -22,6 +22,18 @@ namespace rfk {
 
 constexpr uint32_t kNoBin = 0xffffffffu;
 
+// Where a bin's RGBA sums and count live: rgba + (bin << rs) (float4 units) and
+// count + (bin << cs) (uint32 units).  The caller's planes: rs = cs = 0.  The interleaved
+// 32-byte record {RGBA, count, pad} of histograms larger than L2: rs = 1, cs = 3, count = the
+// record base + 4 -- one DRAM sector per point instead of two.
+struct BinTarget {
+    float4* rgba;
+    uint32_t* count;  // may be null
+    uint32_t rs, cs;
+    __device__ __forceinline__ float4* at_rgba(uint32_t bin) const { return rgba + ((size_t)bin << rs); }
+    __device__ __forceinline__ uint32_t* at_count(uint32_t bin) const { return count + ((size_t)bin << cs); }
+};
+
 __device__ __forceinline__ void red_add_f32x4(float4* p, float a, float b, float c, float d) {
     asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
                  : "memory");
@@ -30,18 +42,18 @@ __device__ __forceinline__ void red_add_u32x1(uint32_t* p, uint32_t v) {
     asm volatile("red.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-__device__ __forceinline__ void splat_global(float4* bins, uint32_t* hits, uint32_t bin, float4 v) {
+__device__ __forceinline__ void splat_global(const BinTarget& t, uint32_t bin, float4 v) {
     if (bin == kNoBin) return;
-    red_add_f32x4(bins + bin, v.x, v.y, v.z, v.w);
-    if (hits) red_add_u32x1(hits + bin, 1u);
+    red_add_f32x4(t.at_rgba(bin), v.x, v.y, v.z, v.w);
+    if (t.count) red_add_u32x1(t.at_count(bin), 1u);
 }
 
 // Every lane of the warp must call this (bin = kNoBin for lanes without a point).
-__device__ __forceinline__ void splat_warp(float4* bins, uint32_t* hits, uint32_t bin, float4 v) {
+__device__ __forceinline__ void splat_warp(const BinTarget& t, uint32_t bin, float4 v) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned peers = __match_any_sync(0xffffffffu, bin);
     if (__all_sync(0xffffffffu, peers == (1u << lane))) {  // no two lanes share a bin
-        splat_global(bins, hits, bin, v);
+        splat_global(t, bin, v);
         return;
     }
     unsigned rank = __popc(peers & ((1u << lane) - 1u));
@@ -63,16 +75,16 @@ __device__ __forceinline__ void splat_warp(float4* bins, uint32_t* hits, uint32_
         rank >>= 1;
     }
     if (bin != kNoBin && (peers & ((1u << lane) - 1u)) == 0u) {  // lowest lane of its set
-        red_add_f32x4(bins + bin, v.x, v.y, v.z, v.w);
-        if (hits) red_add_u32x1(hits + bin, (uint32_t)__popc(peers));
+        red_add_f32x4(t.at_rgba(bin), v.x, v.y, v.z, v.w);
+        if (t.count) red_add_u32x1(t.at_count(bin), (uint32_t)__popc(peers));
     }
 }
 
 // Every lane of the warp must call this.
-__device__ __forceinline__ void splat_adaptive(float4* bins, uint32_t* hits, uint32_t bin, float4 v) {
+__device__ __forceinline__ void splat_adaptive(const BinTarget& t, uint32_t bin, float4 v) {
     const uint32_t other = __shfl_xor_sync(0xffffffffu, bin, 1);
-    if (__any_sync(0xffffffffu, bin != kNoBin && bin == other)) splat_warp(bins, hits, bin, v);
-    else splat_global(bins, hits, bin, v);
+    if (__any_sync(0xffffffffu, bin != kNoBin && bin == other)) splat_warp(t, bin, v);
+    else splat_global(t, bin, v);
 }
 
 }  // namespace rfk

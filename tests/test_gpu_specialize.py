@@ -53,3 +53,25 @@ def test_nonlinear_genomes_match_interpreter(rk, compiler, kind, seed, nx):
     la, floor = _l1(a["hits"], b["hits"]), _l1(b["hits"], c["hits"])
     print("identical=%s L1 spec-vs-interp %.4g, interp two-seed %.4g" % (same, la, floor))
     assert same or la <= 1.5 * floor
+
+
+@pytest.mark.parametrize("kind", [0, 3])
+def test_interleaved_bin_records_equal_direct_planes(rk, compiler, kind):
+    """Drawing through interleaved 32-byte records (merged into the caller's planes after each
+    call) gives the direct planes' counts exactly, over two consecutive draw calls."""
+    W = H = 256
+    f = rk.Flame.synthesize(compiler, kind, 5, W, H)
+    out = []
+    for layout in (rk.BINS_DIRECT, rk.BINS_INTERLEAVED):
+        sim = rk.Sim(8192, seed=4)
+        sim.set_bin_layout(layout)
+        sim.warmup(f, 19)
+        bins, hits = _bins(W, H)
+        sim.draw_to_bins(f, bins, hits, W, H, 20)
+        sim.draw_to_bins(f, bins, hits, W, H, 20)
+        out.append((bins.cpu().numpy(), hits.cpu().numpy()))
+        sim.close()
+    (b0, h0), (b1, h1) = out
+    assert int(h0.sum()) > 0
+    assert np.array_equal(h0, h1)
+    assert np.allclose(b0, b1, rtol=1e-4, atol=1e-3)
