@@ -12,11 +12,10 @@ denoised, and half the mean absolute difference of the two outputs estimates the
 average.  Frames whose estimate exceeds the bound are rendered on the plain path instead.
 """
 import math
-import time
 
 import numpy as np
 
-from . import Batch, Denoiser, SYNTH_RANDOM, Flame
+from . import Batch, SYNTH_RANDOM, Flame
 
 DE = (9, 0, 0.4)  # adaptive DE of the plain path: max radius, min radius, curve
 
