@@ -310,6 +310,8 @@ def run_native(args):
         t1.record(stream)
         barrier()
     ms = t0.elapsed_time(t1)
+    cnt = sim.counters()  # the last frame's draw call: points binned (in frame, opacity > 0)
+    binned_fraction = cnt["drawn"] / float(passes * walkers)
     draw_ms = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
     image_passes = None
     if WL["image"]:
@@ -377,6 +379,7 @@ def run_native(args):
                    "parallelism": "replicas" if ws > 1 else "single"},
         "s_per_frame": ms_step / 1e3,
         "draw_ms_per_frame": draw_ms,
+        "binned_fraction": binned_fraction,
         "image_passes": image_passes,
         "gpu_launches": (launches + (FUSE + args.steps_per_launch - 1) // args.steps_per_launch + 4) * args.steps,
         "e2e": {"value": e2e_value, "unit": "Gpoints/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
