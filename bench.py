@@ -603,16 +603,25 @@ def run_learned(args):
                 fn()
                 ts.append(time.perf_counter() - t)
             times[name] = statistics.median(ts)
-    # the fallback policy on the held-out set: split estimates from two short runs
+    # the fallback policy on held-out frames: split estimates from two short runs, calibrated
+    # (scale = sum of true errors / sum of estimates) on the first half, applied to the second
+    # with the plain path's 1000-spp error as the bound
+    n_cal = min(32, n_test // 2)
     lr_ = LD.LearnedRenderer(net, spp=spp_fast, bound=args.learned_bound)
-    fallbacks, est_err = 0, []
-    for k in range(min(32, n_test)):
+    est_err = []
+    for k in range(n_cal):
         out, est, pest = lr_.estimate(te[k], S, S, seed=te_seeds[k] * 7 + 40)
-        fallbacks += int(est > args.learned_bound)
         est_err.append((est, pest, float((out - ref[k]).abs().mean())))
     true_e = np.array([x[2] for x in est_err])
     est_corr = {"learned_split": float(np.corrcoef([x[0] for x in est_err], true_e)[0, 1]),
                 "plain_split": float(np.corrcoef([x[1] for x in est_err], true_e)[0, 1])}
+    scale = float(true_e.sum() / max(1e-12, sum(x[0] for x in est_err)))
+    policy = LD.LearnedRenderer(net, spp=spp_fast, bound=plain[1000], scale=scale)
+    fallbacks, errs, learned_only = 0, [], []
+    for k in range(n_cal, 2 * n_cal):
+        out, e, fb = policy.render(te[k], S, S, seed=te_seeds[k] * 7 + 50)
+        fallbacks += int(fb)
+        errs.append(float((out - ref[k]).abs().mean()))
     line = {
         "metric": "s per 1080p frame at fixed L1 err, learned vs plain DE", "value": times["learned"],
         "unit": "s/frame", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -632,8 +641,10 @@ def run_learned(args):
         "learned_reaches_plain_1000spp_error": learned[16] <= plain[1000],
         "train": {"data_s": t_data, "train_s": t_train, "separate_networks": bool(args.learned_separate),
                   "loss_first_last": {str(k): v for k, v in losses.items()}},
-        "fallback": {"bound": args.learned_bound, "frames": min(32, n_test), "fallbacks": fallbacks,
-                     "correlation_with_true_l1": est_corr, "estimate_vs_true_l1": est_err[:8]},
+        "fallback": {"calibration_frames": n_cal, "scale": scale, "bound": plain[1000],
+                     "correlation_with_true_l1": est_corr, "estimate_vs_true_l1": est_err[:6],
+                     "policy_frames": n_cal, "policy_fallbacks": fallbacks,
+                     "policy_mean_l1": float(np.mean(errs)) if errs else None},
         "gpu_launches": None,
         "e2e": {"value": times["learned"], "unit": "s/frame", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "clocks": clk.summary(),

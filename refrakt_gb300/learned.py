@@ -116,11 +116,12 @@ class LearnedRenderer:
     pixel are denoised; the error estimate is half the mean absolute difference of the two
     denoised outputs plus `plain_weight` times that of the two plain images (the sampling noise
     the network has to remove); above `bound` the frame is rendered on the plain path
-    (`plain_spp`, adaptive DE) instead."""
+    (`plain_spp`, adaptive DE) instead.  `scale` calibrates the estimate against held-out
+    frames' true errors (the split estimate sees only the variance of the two runs)."""
 
-    def __init__(self, net, spp=16, bound=0.02, plain_spp=1000, plain_weight=0.0, device=0):
+    def __init__(self, net, spp=16, bound=0.02, plain_spp=1000, plain_weight=0.0, scale=1.0, device=0):
         self.net, self.spp, self.bound, self.plain_spp, self.device = net, spp, bound, plain_spp, device
-        self.plain_weight = plain_weight
+        self.plain_weight, self.scale = plain_weight, scale
 
     def estimate(self, flame, w, h, seed=0):
         """(denoised average, learned split estimate, plain split estimate) of two short runs."""
@@ -137,7 +138,7 @@ class LearnedRenderer:
         """(image, error estimate, fell back)."""
         import torch
         img, est, plain = self.estimate(flame, w, h, seed)
-        e = est + self.plain_weight * plain
+        e = self.scale * (est + self.plain_weight * plain)
         if e <= self.bound:
             return img, e, False
         full = torch.empty(1, h, w, 3, device="cuda")
