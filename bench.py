@@ -553,6 +553,8 @@ def run_learned(args):
         t_train += time.perf_counter() - t0
         for spp in grp:
             nets[spp], losses[spp] = net, (ls[0], ls[-1])
+        if args.learned_save:  # right after training, so a later failure keeps the weights
+            np.save(args.learned_save.replace(".npy", "") + "_%s.npy" % "-".join(map(str, grp)), net.params())
         del feats
     del targets
 
@@ -617,7 +619,7 @@ def run_learned(args):
                 "plain_split": float(np.corrcoef([x[1] for x in est_err], true_e)[0, 1])}
     scale = float(true_e.sum() / max(1e-12, sum(x[0] for x in est_err)))
     policy = LD.LearnedRenderer(net, spp=spp_fast, bound=plain[1000], scale=scale)
-    fallbacks, errs, learned_only = 0, [], []
+    fallbacks, errs = 0, []
     for k in range(n_cal, 2 * n_cal):
         out, e, fb = policy.render(te[k], S, S, seed=te_seeds[k] * 7 + 50)
         fallbacks += int(fb)
@@ -638,7 +640,6 @@ def run_learned(args):
         "l1_plain_by_spp": plain, "l1_learned_by_input_spp": learned,
         "plain_spp_equivalent": equiv,
         "iteration_ratio_at_plain_1000spp_error": None,
-        "learned_reaches_plain_1000spp_error": learned[16] <= plain[1000],
         "train": {"data_s": t_data, "train_s": t_train, "separate_networks": bool(args.learned_separate),
                   "loss_first_last": {str(k): v for k, v in losses.items()}},
         "fallback": {"calibration_frames": n_cal, "scale": scale, "bound": plain[1000],
@@ -651,8 +652,6 @@ def run_learned(args):
     }
     line["iteration_ratio_at_plain_1000spp_error"] = (1000.0 / spp_fast) if meets else None
     line["learned_reaches_plain_1000spp_error"] = bool(meets)
-    if args.learned_save:
-        np.save(args.learned_save, net.params())
     print(json.dumps(line))
     return 0
 
