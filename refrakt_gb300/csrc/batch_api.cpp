@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <map>
 #include <string>
 #include <cstring>
@@ -49,8 +51,9 @@ struct Item {
 
 constexpr uint64_t kUnitSeedStride = 0x9e3779b97f4a7c15ull;  // unit u of an item: seed + u * stride
 constexpr uint64_t kTableSeed = 0x5eed;                      // shared table: keyed by kTableSeed + slots
-constexpr size_t kMaxSpecGroups = 4;       // specialised launches per batch
-constexpr uint32_t kSpecMinUnitsPerSM = 2;  // a structure gets its own launch from 2 units per SM
+constexpr uint32_t kSpecMinUnitsPerSM = 2;  // a structure gets a persistent launch from 2 units per SM
+constexpr int kAuxStreams = 8;              // concurrent launches of the smaller structures
+constexpr unsigned kCompileThreads = 16;    // run-time compilations in parallel
 constexpr double kCompactShare = 16.0;  // probe points sharing a point's bin above this: compact attractor
 
 // Histogram L1 noise of a mixing domain relative to the reference's global shuffle, measured on
@@ -64,13 +67,16 @@ double mixing_efficiency(uint32_t slots) {
 
 struct SpecGroup {  // units of one genome structure, drawn by its specialised kernel
     const void* kernel = nullptr;
-    int grid = 0;
-    uint32_t first = 0, count = 0;
+    int grid = 0;       // CTAs: persistent (every SM) for a big group, one per unit up to that
+    bool big = false;   // big groups run one after another on the batch's stream; small ones
+    uint32_t first = 0, count = 0;  // concurrently on the auxiliary streams
 };
 
 struct rf_batch {
     int device = 0;
     std::vector<SpecGroup> groups;
+    std::vector<cudaStream_t> aux;    // concurrent launches of small specialised groups
+    std::vector<cudaEvent_t> aux_ev;  // [0] fork, [1 + k] join of aux[k]
     uint32_t interp_first = 0, interp_count = 0;
     cudaStream_t stream = nullptr;
     rf_batch_desc d{};
@@ -105,6 +111,8 @@ void destroy_batch(rf_batch* b) {
     }
     void* ptrs[] = {b->table, b->dinst, b->dunits, b->queue, b->counters, b->stats};
     for (void* p : ptrs) if (p) cudaFree(p);
+    for (cudaStream_t s : b->aux) cudaStreamDestroy(s);
+    for (cudaEvent_t ev : b->aux_ev) cudaEventDestroy(ev);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -216,15 +224,33 @@ int enqueue(rf_batch* b) {
         if (e == cudaSuccess) e = cudaMemsetAsync(it.hits, 0, nb * sizeof(uint32_t), st);
     }
     if (e != cudaSuccess) return cuda_err(e, "batch clear");
+    // small specialised groups: forked onto the auxiliary streams, joined before the image passes
+    bool forked = false;
+    for (size_t g = 0, k = 0; g < b->groups.size() && e == cudaSuccess; g++) {
+        const SpecGroup& G = b->groups[g];
+        if (G.big || !G.count) continue;
+        if (!forked) {
+            e = cudaEventRecord(b->aux_ev[0], st);
+            for (size_t a = 0; a < b->aux.size() && e == cudaSuccess; a++) e = cudaStreamWaitEvent(b->aux[a], b->aux_ev[0], 0);
+            forked = true;
+        }
+        if (e == cudaSuccess)
+            e = launch_batch_spec(G.kernel, (int)b->threads, (int)b->slots, G.grid,
+                                  args_for(b, G.first, G.count, (uint32_t)g), b->aux[k++ % b->aux.size()]);
+    }
     for (size_t g = 0; g < b->groups.size() && e == cudaSuccess; g++) {
         const SpecGroup& G = b->groups[g];
-        if (G.count)
+        if (G.big && G.count)
             e = launch_batch_spec(G.kernel, (int)b->threads, (int)b->slots, G.grid,
                                   args_for(b, G.first, G.count, (uint32_t)g), st);
     }
     if (e == cudaSuccess && b->interp_count)
         e = launch_batch((int)b->threads, (int)b->slots,
                          args_for(b, b->interp_first, b->interp_count, (uint32_t)b->groups.size()), st, nullptr);
+    for (size_t a = 0; forked && a < b->aux.size() && e == cudaSuccess; a++) {
+        e = cudaEventRecord(b->aux_ev[1 + a], b->aux[a]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, b->aux_ev[1 + a], 0);
+    }
     if (e != cudaSuccess) return cuda_err(e, "batch kernel");
     for (size_t i = 0; i < b->items.size(); i++) {
         Item& it = b->items[i];
@@ -308,7 +334,7 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
         b->max_prog_words = std::max(b->max_prog_words, (uint32_t)it.prog.size());
         b->points += items[i].points;
     }
-    e = cudaMalloc((void**)&b->queue, (kMaxSpecGroups + 1) * sizeof(unsigned int));
+    e = cudaMalloc((void**)&b->queue, ((size_t)n + 1) * sizeof(unsigned int));  // a counter per group (<= items)
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->counters, 3 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->stats, 3 * sizeof(double) * n);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
@@ -374,38 +400,61 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
     per = std::max<uint64_t>(per, d->unit_passes ? 1 : 20ull * b->fuse);
     per = std::min<uint64_t>(per, 1u << 20);
     b->unit_passes = (uint32_t)per;
-    // --- genome-specialised kernels for structures that fill the GPU on their own (animation
-    // frames); the rest stays on the interpreted kernel
+    // --- genome-specialised kernels, one per genome structure, compiled in parallel (cached
+    // across batches).  A structure with >= 2 units per SM gets a persistent launch of its own;
+    // the others run concurrently on auxiliary streams, a CTA per unit.  Structures whose kernel
+    // does not compile stay on the interpreted launch.
     if (d->specialize >= 0) {
         std::map<std::string, uint64_t> units_of;
+        std::map<std::string, const Item*> rep;
         for (auto& it : b->items) {
             it.structure = spec_structure(it.prog);
             units_of[it.structure] += std::max<uint64_t>(1, ((it.desc.points + b->slots - 1) / b->slots + per - 1) / per);
+            rep.emplace(it.structure, &it);
         }
-        std::vector<std::pair<uint64_t, std::string>> big;
-        for (auto& kv : units_of)
-            if (kv.second >= (uint64_t)kSpecMinUnitsPerSM * sms) big.push_back({kv.second, kv.first});
-        std::sort(big.rbegin(), big.rend());
-        if (big.size() > kMaxSpecGroups) big.resize(kMaxSpecGroups);
-        for (auto& bg : big) {
-            const Item* rep = nullptr;
-            for (auto& it : b->items)
-                if (it.structure == bg.second) { rep = &it; break; }
-            const void* k = nullptr;
-            int rc = spec_kernel(rep->prog, (int)b->threads, (int)b->slots, b->device, &k, SpecKind::Batch);
-            int grid = rc == RF_OK ? batch_spec_grid(k, (int)b->threads, (int)b->slots, b->max_prog_words) : 0;
-            if (rc == RF_OK && grid == 0) rc = fail(RF_ERR_CUDA, "specialised batch kernel: no resident CTA");
-            if (rc != RF_OK) {
-                if (d->specialize > 0) return bail(rc);
+        std::vector<std::pair<uint64_t, std::string>> order;
+        for (auto& kv : units_of) order.push_back({kv.second, kv.first});
+        std::sort(order.rbegin(), order.rend());
+        std::vector<const void*> kern(order.size(), nullptr);
+        std::vector<int> rcs(order.size(), RF_OK);
+        std::atomic<size_t> next{0};
+        auto worker = [&]() {
+            for (size_t j; (j = next++) < order.size();)
+                rcs[j] = spec_kernel(rep[order[j].second]->prog, (int)b->threads, (int)b->slots, b->device, &kern[j],
+                                     SpecKind::Batch);
+        };
+        const unsigned nt = std::max(1u, std::min<unsigned>(kCompileThreads, (unsigned)order.size()));
+        std::vector<std::thread> pool;
+        for (unsigned t = 1; t < nt; t++) pool.emplace_back(worker);
+        worker();
+        for (auto& t : pool) t.join();
+        cudaSetDevice(b->device);
+        for (size_t j = 0; j < order.size(); j++) {
+            int grid = rcs[j] == RF_OK ? batch_spec_grid(kern[j], (int)b->threads, (int)b->slots, b->max_prog_words) : 0;
+            if (rcs[j] != RF_OK || grid == 0) {
+                if (d->specialize > 0)
+                    return bail(rcs[j] != RF_OK ? rcs[j] : fail(RF_ERR_CUDA, "specialised batch kernel: no resident CTA"));
                 continue;
             }
             SpecGroup G;
-            G.kernel = k;
-            G.grid = grid;
+            G.kernel = kern[j];
+            G.big = order[j].first >= (uint64_t)kSpecMinUnitsPerSM * sms;
+            G.grid = G.big ? grid : (int)std::min<uint64_t>(order[j].first, (uint64_t)grid);
             b->groups.push_back(G);
             for (auto& it : b->items)
-                if (it.structure == bg.second) it.group = (int)b->groups.size() - 1;
+                if (it.structure == order[j].second) it.group = (int)b->groups.size() - 1;
         }
+        for (int a = 0; a < kAuxStreams && e == cudaSuccess; a++) {
+            cudaStream_t s = nullptr;
+            e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+            if (e == cudaSuccess) b->aux.push_back(s);
+        }
+        for (int a = 0; a <= kAuxStreams && e == cudaSuccess; a++) {
+            cudaEvent_t ev = nullptr;
+            e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+            if (e == cudaSuccess) b->aux_ev.push_back(ev);
+        }
+        if (e != cudaSuccess) return bail(cuda_err(e, "batch streams"));
     }
     if (int rc = build_tables(b, b->slots, b->unit_passes, 0, n)) return bail(rc);
     if (d->use_graph) {

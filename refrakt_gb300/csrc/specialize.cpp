@@ -201,21 +201,26 @@ int spec_kernel(const std::vector<uint32_t>& prog, int threads, int slots, int d
         return fail(RF_ERR_INVALID_ARG, "spec_kernel: not a compiled genome");
     const std::string src = spec_source(prog, threads, slots / threads, kind);
     const std::string key = std::to_string(device) + "\n" + src;
-    std::lock_guard<std::mutex> lk(g_mu);
-    auto it = g_cache.find(key);
-    if (it != g_cache.end()) {
-        *out = reinterpret_cast<const void*>(it->second->kernel);
-        return RF_OK;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_cache.find(key);
+        if (it != g_cache.end()) {
+            *out = reinterpret_cast<const void*>(it->second->kernel);
+            return RF_OK;
+        }
     }
+    // compile and load outside the lock, so several structures compile in parallel
     std::vector<char> cubin;
     if (int rc = spec_compile(src, cubin)) return rc;
     auto spec = std::make_unique<Spec>();
-    cudaError_t e = cudaLibraryLoadData(&spec->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaLibraryLoadData(&spec->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
     if (e == cudaSuccess)
         e = cudaLibraryGetKernel(&spec->kernel, spec->lib, kind == SpecKind::Batch ? "rfk_batch_spec" : "rfk_chaos_spec");
     if (e != cudaSuccess) return fail(RF_ERR_CUDA, std::string("loading the specialised kernel: ") + cudaGetErrorString(e));
-    *out = reinterpret_cast<const void*>(spec->kernel);
-    g_cache.emplace(key, std::move(spec));
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto ins = g_cache.emplace(key, std::move(spec));  // a concurrent compile of the same source keeps the first
+    *out = reinterpret_cast<const void*>(ins.first->second->kernel);
     return RF_OK;
 }
 
