@@ -57,7 +57,8 @@ __global__ void de_radius_kernel(const float4* __restrict__ in, size_t n, const 
 // its R halo in shared memory and forms each output bin as a gather in one of two ways, chosen
 // per tile by their work:
 //   box  — sum the bins within the tile's largest radius rmax whose disc covers the output:
-//          (2 rmax + 1)^2 taps per output;
+//          up to (2 rmax + 1)^2 taps per output, rows whose largest disc cannot reach the output
+//          skipped and each row's span cut to its largest radius;
 //   list — the discs of radius 0 and 1 from the 3 x 3 neighbourhood, plus a compact list of the
 //          tile's larger discs (those reaching the tile), which every thread walks in the same
 //          order (shared-memory broadcasts): 9 + list-length taps per output.
@@ -67,7 +68,7 @@ constexpr int kDsX = 32, kDsY = 8, kDsThreads = 256;
 
 template <int R>
 __host__ __device__ constexpr size_t de_tile_smem() {
-    return (size_t)(kDsX + 2 * R) * (kDsY + 2 * R) * (16 + 4 + 1) + 16 + 64;
+    return (size_t)(kDsX + 2 * R) * (kDsY + 2 * R) * (16 + 4 + 1) + 16 + 64 + 4 * (kDsY + 2 * R);
 }
 
 template <int R>
@@ -80,9 +81,12 @@ __global__ void __launch_bounds__(kDsThreads) de_tile_kernel(
     int* s_list = reinterpret_cast<int*>(s_c + NS);                 // indices of discs of radius >= 2
     uint8_t* s_r = reinterpret_cast<uint8_t*>(s_list + NS);         // NS radii (255: empty)
     int* s_stat = reinterpret_cast<int*>(s_r + ((NS + 15) & ~15));  // [0] rmax, [1..8] per-warp counts
+    int* s_rowmax = s_stat + 16;                                     // SH: largest radius per staged row
     const int tx0 = blockIdx.x * kDsX, ty0 = blockIdx.y * kDsY;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_stat[0] = 0;
+    for (int i = threadIdx.x; i < SH; i += kDsThreads) s_rowmax[i] = -1;
+    __syncthreads();
     int rmax = 0, nl = 0;
     // stage the tile + halo; list the large discs that reach the tile in source order (a
     // ballot-and-prefix compaction, so the list and the sums are the same on every run)
@@ -100,6 +104,7 @@ __global__ void __launch_bounds__(kDsThreads) de_tile_kernel(
             }
             s_r[i] = r;
             s_c[i] = v;
+            if (r != 255) atomicMax(&s_rowmax[i / SW], (int)r);
             if (r != 255 && gx - r <= tx0 + kDsX - 1 && gx + r >= tx0 && gy - r <= ty0 + kDsY - 1 && gy + r >= ty0) {
                 rmax = max(rmax, (int)r);
                 big = r >= 2;
@@ -153,7 +158,9 @@ __global__ void __launch_bounds__(kDsThreads) de_tile_kernel(
         } else {
             for (int dy = -rm; dy <= rm; dy++) {
                 const int ay = dy < 0 ? -dy : dy;
-                for (int dx = -rm; dx <= rm; dx++) {
+                const int rr = min(rm, s_rowmax[oy + R + dy]);  // no disc of this row reaches |dy| rows
+                if (rr < ay) continue;
+                for (int dx = -rr; dx <= rr; dx++) {
                     const int si = (oy + R + dy) * SW + ox + R + dx;
                     const int r = s_r[si];
                     const int ax = dx < 0 ? -dx : dx;
