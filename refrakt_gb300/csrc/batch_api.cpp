@@ -52,7 +52,7 @@ struct Item {
 constexpr uint64_t kUnitSeedStride = 0x9e3779b97f4a7c15ull;  // unit u of an item: seed + u * stride
 constexpr uint64_t kTableSeed = 0x5eed;                      // shared table: keyed by kTableSeed + slots
 constexpr uint32_t kSpecMinUnitsPerSM = 2;  // a structure gets a persistent launch from 2 units per SM
-constexpr int kAuxStreams = 8;              // concurrent launches of the smaller structures
+constexpr int kAuxStreams = 32;             // concurrent launches of the smaller structures
 constexpr unsigned kCompileThreads = 16;    // run-time compilations in parallel
 constexpr double kCompactShare = 16.0;  // probe points sharing a point's bin above this: compact attractor
 
