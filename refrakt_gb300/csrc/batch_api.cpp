@@ -447,12 +447,14 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
             for (auto& it : b->items)
                 if (it.structure == order[j].second) it.group = (int)b->groups.size() - 1;
         }
-        for (int a = 0; a < kAuxStreams && e == cudaSuccess; a++) {
+        bool small = false;
+        for (const auto& G : b->groups) small = small || !G.big;
+        for (int a = 0; small && a < kAuxStreams && e == cudaSuccess; a++) {
             cudaStream_t s = nullptr;
             e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
             if (e == cudaSuccess) b->aux.push_back(s);
         }
-        for (int a = 0; a <= kAuxStreams && e == cudaSuccess; a++) {
+        for (int a = 0; small && a <= kAuxStreams && e == cudaSuccess; a++) {
             cudaEvent_t ev = nullptr;
             e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
             if (e == cudaSuccess) b->aux_ev.push_back(ev);
