@@ -52,7 +52,6 @@ struct Item {
 constexpr uint64_t kUnitSeedStride = 0x9e3779b97f4a7c15ull;  // unit u of an item: seed + u * stride
 constexpr uint64_t kTableSeed = 0x5eed;                      // shared table: keyed by kTableSeed + slots
 constexpr uint32_t kSpecMinUnitsPerSM = 2;  // a structure gets a persistent launch from 2 units per SM
-constexpr int kAuxStreams = 32;             // concurrent launches of the smaller structures
 constexpr unsigned kCompileThreads = 16;    // run-time compilations in parallel
 constexpr double kCompactShare = 16.0;  // probe points sharing a point's bin above this: compact attractor
 
@@ -65,18 +64,15 @@ double mixing_efficiency(uint32_t slots) {
 
 }  // namespace
 
-struct SpecGroup {  // units of one genome structure, drawn by its specialised kernel
+struct SpecGroup {  // units of one genome structure, drawn by its specialised persistent kernel
     const void* kernel = nullptr;
-    int grid = 0;       // CTAs: persistent (every SM) for a big group, one per unit up to that
-    bool big = false;   // big groups run one after another on the batch's stream; small ones
-    uint32_t first = 0, count = 0;  // concurrently on the auxiliary streams
+    int grid = 0;
+    uint32_t first = 0, count = 0;
 };
 
 struct rf_batch {
     int device = 0;
     std::vector<SpecGroup> groups;
-    std::vector<cudaStream_t> aux;    // concurrent launches of small specialised groups
-    std::vector<cudaEvent_t> aux_ev;  // [0] fork, [1 + k] join of aux[k]
     uint32_t interp_first = 0, interp_count = 0;
     cudaStream_t stream = nullptr;
     rf_batch_desc d{};
@@ -111,8 +107,6 @@ void destroy_batch(rf_batch* b) {
     }
     void* ptrs[] = {b->table, b->dinst, b->dunits, b->queue, b->counters, b->stats};
     for (void* p : ptrs) if (p) cudaFree(p);
-    for (cudaStream_t s : b->aux) cudaStreamDestroy(s);
-    for (cudaEvent_t ev : b->aux_ev) cudaEventDestroy(ev);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -224,33 +218,15 @@ int enqueue(rf_batch* b) {
         if (e == cudaSuccess) e = cudaMemsetAsync(it.hits, 0, nb * sizeof(uint32_t), st);
     }
     if (e != cudaSuccess) return cuda_err(e, "batch clear");
-    // small specialised groups: forked onto the auxiliary streams, joined before the image passes
-    bool forked = false;
-    for (size_t g = 0, k = 0; g < b->groups.size() && e == cudaSuccess; g++) {
-        const SpecGroup& G = b->groups[g];
-        if (G.big || !G.count) continue;
-        if (!forked) {
-            e = cudaEventRecord(b->aux_ev[0], st);
-            for (size_t a = 0; a < b->aux.size() && e == cudaSuccess; a++) e = cudaStreamWaitEvent(b->aux[a], b->aux_ev[0], 0);
-            forked = true;
-        }
-        if (e == cudaSuccess)
-            e = launch_batch_spec(G.kernel, (int)b->threads, (int)b->slots, G.grid,
-                                  args_for(b, G.first, G.count, (uint32_t)g), b->aux[k++ % b->aux.size()]);
-    }
     for (size_t g = 0; g < b->groups.size() && e == cudaSuccess; g++) {
         const SpecGroup& G = b->groups[g];
-        if (G.big && G.count)
+        if (G.count)
             e = launch_batch_spec(G.kernel, (int)b->threads, (int)b->slots, G.grid,
                                   args_for(b, G.first, G.count, (uint32_t)g), st);
     }
     if (e == cudaSuccess && b->interp_count)
         e = launch_batch((int)b->threads, (int)b->slots,
                          args_for(b, b->interp_first, b->interp_count, (uint32_t)b->groups.size()), st, nullptr);
-    for (size_t a = 0; forked && a < b->aux.size() && e == cudaSuccess; a++) {
-        e = cudaEventRecord(b->aux_ev[1 + a], b->aux[a]);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, b->aux_ev[1 + a], 0);
-    }
     if (e != cudaSuccess) return cuda_err(e, "batch kernel");
     for (size_t i = 0; i < b->items.size(); i++) {
         Item& it = b->items[i];
@@ -441,25 +417,11 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
             }
             SpecGroup G;
             G.kernel = kern[j];
-            G.big = order[j].first >= (uint64_t)kSpecMinUnitsPerSM * sms;
-            G.grid = G.big ? grid : (int)std::min<uint64_t>(order[j].first, (uint64_t)grid);
+            G.grid = grid;
             b->groups.push_back(G);
             for (auto& it : b->items)
                 if (it.structure == order[j].second) it.group = (int)b->groups.size() - 1;
         }
-        bool small = false;
-        for (const auto& G : b->groups) small = small || !G.big;
-        for (int a = 0; small && a < kAuxStreams && e == cudaSuccess; a++) {
-            cudaStream_t s = nullptr;
-            e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-            if (e == cudaSuccess) b->aux.push_back(s);
-        }
-        for (int a = 0; small && a <= kAuxStreams && e == cudaSuccess; a++) {
-            cudaEvent_t ev = nullptr;
-            e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-            if (e == cudaSuccess) b->aux_ev.push_back(ev);
-        }
-        if (e != cudaSuccess) return bail(cuda_err(e, "batch streams"));
     }
     if (int rc = build_tables(b, b->slots, b->unit_passes, 0, n)) return bail(rc);
     if (d->use_graph) {
