@@ -533,9 +533,18 @@ def run_learned(args):
     levels = [int(x) for x in args.learned_spp.split(",")]
     # one network over all input levels, or (separate) one network per level
     groups = [[l] for l in levels] if args.learned_separate else [levels]
-    targets = torch.empty(n_train, S, S, 3, device="cuda")
-    LD.render_images(tr, S, S, 1000, [s * 7 + 2 for s in tr_seeds], targets)
     nets, losses, t_train = {}, {}, 0.0
+    loads = args.learned_load.split(",") if args.learned_load else []
+    if loads:  # evaluate trained weights (one file per group) instead of training
+        for grp, path in zip(groups, loads):
+            net = R.Denoiser(4 * S * S, seed=0)
+            net.set_params(np.load(path))
+            for spp in grp:
+                nets[spp], losses[spp] = net, None
+        groups = []
+    else:
+        targets = torch.empty(n_train, S, S, 3, device="cuda")
+        LD.render_images(tr, S, S, 1000, [s * 7 + 2 for s in tr_seeds], targets)
     t_data = time.perf_counter() - t0
     for gi, grp in enumerate(groups):
         t0 = time.perf_counter()
@@ -556,11 +565,12 @@ def run_learned(args):
         if args.learned_save:  # right after training, so a later failure keeps the weights
             np.save(args.learned_save.replace(".npy", "") + "_%s.npy" % "-".join(map(str, grp)), net.params())
         del feats
-    del targets
+    if not loads:
+        del targets
 
-    # held-out evaluation against a 4000-spp adaptive-DE reference
+    # held-out evaluation against a converged adaptive-DE reference (args.learned_ref_spp)
     ref = torch.empty(n_test, S, S, 3, device="cuda")
-    LD.render_images(te, S, S, 4000, [s * 7 + 3 for s in te_seeds], ref)
+    LD.render_images(te, S, S, args.learned_ref_spp, [s * 7 + 3 for s in te_seeds], ref)
     spps = [16, 32, 64, 125, 250, 500, 1000]
     img = torch.empty(n_test, S, S, 3, device="cuda")
     plain = {}
@@ -633,7 +643,8 @@ def run_learned(args):
         "config": {"workload": CONFIG_NAME, "train_genomes": n_train, "test_genomes": n_test,
                    "train_steps": args.learned_steps, "batch": args.learned_batch, "crop": args.learned_crop,
                    "resolution": [S, S],
-                   "params": net.num_params(), "input_spp": levels, "target_spp": 1000, "reference_spp": 4000,
+                   "params": net.num_params(), "input_spp": levels, "target_spp": 1000, "reference_spp": args.learned_ref_spp,
+                   "weights": "loaded" if loads else "trained in this run",
                    "frame_spp_learned": spp_fast},
         "plain_s_per_frame": times["plain"],
         "speedup_vs_plain": times["plain"] / times["learned"],
@@ -641,7 +652,7 @@ def run_learned(args):
         "plain_spp_equivalent": equiv,
         "iteration_ratio_at_plain_1000spp_error": None,
         "train": {"data_s": t_data, "train_s": t_train, "separate_networks": bool(args.learned_separate),
-                  "loss_first_last": {str(k): v for k, v in losses.items()}},
+                  "loss_first_last": {str(k): v for k, v in losses.items() if v is not None}},
         "fallback": {"calibration_frames": n_cal, "scale": scale, "bound": plain[1000],
                      "correlation_with_true_l1": est_corr, "estimate_vs_true_l1": est_err[:6],
                      "policy_frames": n_cal, "policy_fallbacks": fallbacks,
@@ -679,6 +690,9 @@ def main():
     ap.add_argument("--learned-separate", action="store_true", help="one network per input level")
     ap.add_argument("--learned-batch", type=int, default=4)
     ap.add_argument("--learned-crop", type=int, default=0, help="random crops of this size (0: whole images)")
+    ap.add_argument("--learned-load", default="", help="evaluate these trained parameter files (.npy, one per "
+                                                       "network) instead of training")
+    ap.add_argument("--learned-ref-spp", type=int, default=16000, help="samples per pixel of the reference images")
     ap.add_argument("--workload", default="frame1080", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     select_workload(args.workload)
