@@ -107,6 +107,36 @@ typedef struct {
 } rf_synth_desc;
 RF_API int  rf_flame_synthesize(const rf_synth_desc* d, const rf_compiler* c, rf_flame** out);
 
+/* A genome from plain C structures (no XML), for FFI callers that build genomes in code: the
+   fields of flame.hpp:21-61 with variations and parameters by name.  The result is validated
+   like a loaded genome (flame.cpp:160-226): unknown names, missing parameters and variations
+   the reference cannot compile are errors. */
+typedef struct {
+    float weight, color, color_speed, opacity;
+    float coefs[6];             /* flam3 coefs order: c00 c01 c10 c11 c20 c21 */
+    int32_t has_post;
+    float post[6];
+    uint32_t n_vars;            /* variations: names and weights */
+    const char* const* var_names;
+    const float* var_weights;
+    uint32_t n_params;          /* parameters of those variations: names and values */
+    const char* const* param_names;
+    const float* param_values;
+} rf_xform_desc;
+typedef struct {
+    uint32_t size[2];
+    float center[2];
+    float scale, rotate;
+    int32_t estimator_radius, estimator_min;
+    float estimator_curve;
+    float gamma, vibrancy, brightness;
+    const float* palette_rgb;   /* 256 x 3 floats in [0, 1] */
+    uint32_t n_xforms;
+    const rf_xform_desc* xforms;
+    const rf_xform_desc* final_xform;  /* may be NULL */
+} rf_genome_desc;
+RF_API int  rf_flame_from_struct(const rf_genome_desc* d, const rf_compiler* c, rf_flame** out);
+
 /* Genome at t in [0, 1] between a and b (animation frames; the reference only rotates affines
    over time, main.cpp:383-395).  The shorter genome's missing xforms are padded with zero
    selection weight; affines, post, weights, colours, variation weights (0 where absent) and shared

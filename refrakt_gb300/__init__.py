@@ -52,6 +52,23 @@ class FlameInfo(ctypes.Structure):
                 ("total_params", ctypes.c_uint32)]
 
 
+class XformDesc(ctypes.Structure):
+    _fields_ = [("weight", ctypes.c_float), ("color", ctypes.c_float), ("color_speed", ctypes.c_float),
+                ("opacity", ctypes.c_float), ("coefs", ctypes.c_float * 6), ("has_post", ctypes.c_int32),
+                ("post", ctypes.c_float * 6), ("n_vars", ctypes.c_uint32), ("var_names", ctypes.POINTER(ctypes.c_char_p)),
+                ("var_weights", ctypes.POINTER(ctypes.c_float)), ("n_params", ctypes.c_uint32),
+                ("param_names", ctypes.POINTER(ctypes.c_char_p)), ("param_values", ctypes.POINTER(ctypes.c_float))]
+
+
+class GenomeDesc(ctypes.Structure):
+    _fields_ = [("size", ctypes.c_uint32 * 2), ("center", ctypes.c_float * 2), ("scale", ctypes.c_float),
+                ("rotate", ctypes.c_float), ("estimator_radius", ctypes.c_int32), ("estimator_min", ctypes.c_int32),
+                ("estimator_curve", ctypes.c_float), ("gamma", ctypes.c_float), ("vibrancy", ctypes.c_float),
+                ("brightness", ctypes.c_float), ("palette_rgb", ctypes.POINTER(ctypes.c_float)),
+                ("n_xforms", ctypes.c_uint32), ("xforms", ctypes.POINTER(XformDesc)),
+                ("final_xform", ctypes.POINTER(XformDesc))]
+
+
 class SimDesc(ctypes.Structure):
     _fields_ = [("walkers", ctypes.c_uint64), ("temporal_samples", ctypes.c_uint32),
                 ("shuffle_count", ctypes.c_uint32), ("seed", ctypes.c_uint64), ("cta_slots", ctypes.c_uint32),
@@ -107,6 +124,8 @@ _SIGS = {
     "rf_flame_free": ([ctypes.c_void_p], None),
     "rf_flame_to_xml": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "rf_flame_synthesize": ([ctypes.POINTER(SynthDesc), ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rf_flame_from_struct": ([ctypes.POINTER(GenomeDesc), ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)],
+                             ctypes.c_int),
     "rf_flame_get_info": ([ctypes.c_void_p, ctypes.POINTER(FlameInfo)], ctypes.c_int),
     "rf_flame_interpolate": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "rf_flame_set_view": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_float, ctypes.c_float], ctypes.c_int),
@@ -310,6 +329,37 @@ class Flame:
     def from_xml(cls, xml, compiler):
         h = ctypes.c_void_p()
         _check(library().rf_flame_load_xml(xml.encode() if isinstance(xml, str) else xml, compiler._h, ctypes.byref(h)))
+        return cls(h, compiler)
+
+    @classmethod
+    def from_struct(cls, compiler, genome):
+        """A genome from a dict (rf_flame_from_struct): size, center, scale, rotate, estimator
+        (radius, min, curve), gamma, vibrancy, brightness, palette (256 x 3), xforms and an optional
+        final_xform, each {weight, color, color_speed, opacity, coefs, post?, vars: {name: weight},
+        params: {name: value}}."""
+        keep = []
+
+        def xf(x):
+            names = [n.encode() for n in x["vars"]]
+            pn = [n.encode() for n in x.get("params", {})]
+            vn = (ctypes.c_char_p * max(1, len(names)))(*names)
+            vw = (ctypes.c_float * max(1, len(names)))(*x["vars"].values())
+            pk = (ctypes.c_char_p * max(1, len(pn)))(*pn)
+            pv = (ctypes.c_float * max(1, len(pn)))(*x.get("params", {}).values())
+            keep.extend([vn, vw, pk, pv])
+            post = x.get("post")
+            return XformDesc(x["weight"], x.get("color", 0.0), x.get("color_speed", 0.5), x.get("opacity", 1.0),
+                             (ctypes.c_float * 6)(*x["coefs"]), int(post is not None),
+                             (ctypes.c_float * 6)(*(post or [1, 0, 0, 1, 0, 0])), len(names), vn, vw, len(pn), pk, pv)
+        xs = (XformDesc * len(genome["xforms"]))(*[xf(x) for x in genome["xforms"]])
+        fin = ctypes.pointer(xf(genome["final_xform"])) if genome.get("final_xform") else None
+        pal = (ctypes.c_float * 768)(*[c for rgb in genome["palette"] for c in rgb])
+        est = genome.get("estimator", (9, 0, 0.4))
+        d = GenomeDesc((ctypes.c_uint32 * 2)(*genome["size"]), (ctypes.c_float * 2)(*genome.get("center", (0, 0))),
+                       genome["scale"], genome.get("rotate", 0.0), est[0], est[1], est[2], genome.get("gamma", 2.2),
+                       genome.get("vibrancy", 1.0), genome.get("brightness", 4.0), pal, len(genome["xforms"]), xs, fin)
+        h = ctypes.c_void_p()
+        _check(library().rf_flame_from_struct(ctypes.byref(d), compiler._h, ctypes.byref(h)))
         return cls(h, compiler)
 
     @classmethod

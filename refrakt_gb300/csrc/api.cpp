@@ -240,6 +240,61 @@ int rf_flame_synthesize(const rf_synth_desc* d, const rf_compiler* c, rf_flame**
     return new_flame(std::move(g), c, out);
 }
 
+int rf_flame_from_struct(const rf_genome_desc* d, const rf_compiler* c, rf_flame** out) {
+    if (!d || !c || !out || (d->n_xforms && !d->xforms) || !d->palette_rgb)
+        return fail(RF_ERR_INVALID_ARG, "rf_flame_from_struct: null argument");
+    *out = nullptr;
+    Genome g;
+    g.size[0] = d->size[0];
+    g.size[1] = d->size[1];
+    g.center[0] = d->center[0];
+    g.center[1] = d->center[1];
+    g.scale = d->scale;
+    g.rotate = d->rotate;
+    g.est_radius = d->estimator_radius;
+    g.est_min = d->estimator_min;
+    g.est_curve = d->estimator_curve;
+    g.gamma = d->gamma;
+    g.vibrancy = d->vibrancy;
+    g.brightness = d->brightness;
+    for (int i = 0; i < 256; i++) {
+        for (int k = 0; k < 3; k++) g.palette[i][k] = d->palette_rgb[3 * i + k];
+        g.palette[i][3] = 1.0f;
+    }
+    const Registry& reg = *c->reg;
+    auto xform = [&](const rf_xform_desc& s, Xform& x) -> int {
+        x.weight = s.weight;
+        x.color = s.color;
+        x.color_speed = s.color_speed;
+        x.opacity = s.opacity;
+        for (int k = 0; k < 6; k++) x.affine[k] = s.coefs[k];
+        x.has_post = s.has_post != 0;
+        for (int k = 0; k < 6; k++) x.post[k] = x.has_post ? s.post[k] : (k == 0 || k == 3 ? 1.0f : 0.0f);
+        if ((s.n_vars && (!s.var_names || !s.var_weights)) || (s.n_params && (!s.param_names || !s.param_values)))
+            return fail(RF_ERR_INVALID_ARG, "rf_flame_from_struct: null name or value array");
+        for (uint32_t k = 0; k < s.n_vars; k++) {
+            if (!s.var_names[k] || !reg.vars.count(s.var_names[k]))
+                return fail(RF_ERR_UNKNOWN_NAME, std::string("unknown variation ") + (s.var_names[k] ? s.var_names[k] : "(null)"));
+            x.vars[s.var_names[k]] = s.var_weights[k];
+        }
+        for (uint32_t k = 0; k < s.n_params; k++) {
+            if (!s.param_names[k] || !reg.param_owner.count(s.param_names[k]))
+                return fail(RF_ERR_UNKNOWN_NAME, std::string("unknown parameter ") + (s.param_names[k] ? s.param_names[k] : "(null)"));
+            x.params[s.param_names[k]] = s.param_values[k];
+        }
+        return RF_OK;
+    };
+    g.xforms.resize(d->n_xforms);
+    for (uint32_t i = 0; i < d->n_xforms; i++)
+        if (int rc = xform(d->xforms[i], g.xforms[i])) return rc;
+    if (d->final_xform) {
+        g.has_final = true;
+        if (int rc = xform(*d->final_xform, g.final_xf)) return rc;
+    }
+    if (int rc = genome_validate(g, reg)) return rc;
+    return new_flame(std::move(g), c, out);
+}
+
 int rf_flame_interpolate(const rf_flame* a, const rf_flame* b, float t, rf_flame** out) {
     if (!a || !b || !out) return fail(RF_ERR_INVALID_ARG, "rf_flame_interpolate: null argument");
     *out = nullptr;

@@ -298,3 +298,34 @@ def test_specialised_kernel_source_and_compile(rk, compiler):
     assert g.kernel_source(512, 2048).count("case ") == 2  # 3 xforms: cases 0, 1 and default
     assert f.kernel_compile(1024, 4096) > 10000
     assert g.kernel_compile(256, 256) > 10000
+
+
+def test_genome_from_struct_equals_xml(rk, compiler):
+    """rf_flame_from_struct builds the same genome (parameter buffer) as the flam3 loader."""
+    xml = ('<flame size="256 192" center="0.1 -0.2" scale="50" rotate="10" gamma="2.2" brightness="4" '
+           'vibrancy="1" estimator_radius="9" estimator_minimum="0" estimator_curve="0.4">'
+           '<xform weight="0.5" color="0.2" color_speed="0.5" opacity="1" coefs="0.5 0.1 -0.1 0.5 0.2 0" '
+           'linear="0.7" julian="0.3" julian_power="3" julian_dist="1"/>'
+           '<xform weight="0.5" color="0.8" color_speed="0.4" opacity="0.9" coefs="-0.4 0 0.2 0.6 0 0.3" '
+           'post="1 0 0 1 0.1 0" spherical="1"/>'
+           '<finalxform color="0" color_speed="0" opacity="1" coefs="1 0 0 1 0 0" sinusoidal="1"/>'
+           + "".join('<color index="%d" rgb="%d %d %d"/>' % (i, i, (3 * i) % 256, 255 - i) for i in range(256))
+           + '</flame>')
+    a = rk.Flame.from_xml(xml, compiler)
+    pal = [(i / 256.0, ((3 * i) % 256) / 256.0, (255 - i) / 256.0) for i in range(256)]
+    b = rk.Flame.from_struct(compiler, {
+        "size": (256, 192), "center": (0.1, -0.2), "scale": 50, "rotate": 10, "estimator": (9, 0, 0.4),
+        "gamma": 2.2, "vibrancy": 1, "brightness": 4, "palette": pal,
+        "xforms": [
+            {"weight": 0.5, "color": 0.2, "color_speed": 0.5, "opacity": 1, "coefs": (0.5, 0.1, -0.1, 0.5, 0.2, 0),
+             "vars": {"linear": 0.7, "julian": 0.3}, "params": {"julian_power": 3, "julian_dist": 1}},
+            {"weight": 0.5, "color": 0.8, "color_speed": 0.4, "opacity": 0.9, "coefs": (-0.4, 0, 0.2, 0.6, 0, 0.3),
+             "post": (1, 0, 0, 1, 0.1, 0), "vars": {"spherical": 1}}],
+        "final_xform": {"weight": 0, "color": 0, "color_speed": 0, "opacity": 1, "coefs": (1, 0, 0, 1, 0, 0),
+                        "vars": {"sinusoidal": 1}}})
+    assert np.array_equal(a.param_buffer(), b.param_buffer())
+    assert a.param_layout() == b.param_layout()
+    assert a.kernel_source() == b.kernel_source()
+    with pytest.raises(rk.RefraktError):
+        rk.Flame.from_struct(compiler, {"size": (8, 8), "scale": 1, "palette": pal,
+                                        "xforms": [{"weight": 1, "coefs": (1, 0, 0, 1, 0, 0), "vars": {"nope": 1}}]})
