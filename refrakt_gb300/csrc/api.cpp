@@ -409,8 +409,8 @@ int rf_sim_create(const rf_sim_desc* d, rf_sim** out) {
     const uint32_t threads = d->cta_threads ? d->cta_threads : std::min<uint32_t>(slots, 1024);
     const uint32_t T = d->temporal_samples ? d->temporal_samples : 1;
     if (!chaos_shape_supported((int)threads, (int)slots))
-        return fail(RF_ERR_INVALID_ARG, "cta_slots / cta_threads: 256x256, 512x512, 1024, 2048 or 4096 slots on 512 "
-                                        "threads, 1024, 2048 or 4096 slots on 1024 threads");
+        return fail(RF_ERR_INVALID_ARG, "cta_slots / cta_threads: 256x256, 512x512, 1024 or 2048 slots on 512 threads, "
+                                        "1024, 2048 or 4096 slots on 1024 threads");
     if (d->walkers == 0 || d->walkers % T) return fail(RF_ERR_INVALID_ARG, "walkers must be a positive multiple of temporal_samples");
     const uint64_t ppts = d->walkers / T;
     if (ppts % slots) return fail(RF_ERR_INVALID_ARG, "walkers per temporal sample must be a multiple of cta_slots");

@@ -110,25 +110,23 @@ static cudaError_t launch_chaos_t(const ChaosArgs& a, uint32_t grid, cudaStream_
 }
 
 bool chaos_shape_supported(int threads, int slots) {
-    if (threads <= 0 || slots % threads) return false;
-    switch (threads * 16 + slots / threads) {
-    case 256 * 16 + 1: case 512 * 16 + 1: case 512 * 16 + 2: case 512 * 16 + 4: case 512 * 16 + 8:
-    case 1024 * 16 + 1: case 1024 * 16 + 2: case 1024 * 16 + 4: return true;
+    switch (threads * 8 + slots / threads) {
+    case 256 * 8 + 1: case 512 * 8 + 1: case 512 * 8 + 2: case 512 * 8 + 4:
+    case 1024 * 8 + 1: case 1024 * 8 + 2: case 1024 * 8 + 4: return slots % threads == 0;
     default: return false;
     }
 }
 
 cudaError_t launch_chaos(int threads, int slots, const ChaosArgs& a, uint32_t grid, cudaStream_t st) {
     if (!chaos_shape_supported(threads, slots)) return cudaErrorInvalidValue;
-    switch (threads * 16 + slots / threads) {
-    case 256 * 16 + 1: return launch_chaos_t<256, 1>(a, grid, st);
-    case 512 * 16 + 1: return launch_chaos_t<512, 1>(a, grid, st);
-    case 512 * 16 + 2: return launch_chaos_t<512, 2>(a, grid, st);
-    case 512 * 16 + 4: return launch_chaos_t<512, 4>(a, grid, st);
-    case 512 * 16 + 8: return launch_chaos_t<512, 8>(a, grid, st);
-    case 1024 * 16 + 1: return launch_chaos_t<1024, 1>(a, grid, st);
-    case 1024 * 16 + 2: return launch_chaos_t<1024, 2>(a, grid, st);
-    case 1024 * 16 + 4: return launch_chaos_t<1024, 4>(a, grid, st);
+    switch (threads * 8 + slots / threads) {
+    case 256 * 8 + 1: return launch_chaos_t<256, 1>(a, grid, st);
+    case 512 * 8 + 1: return launch_chaos_t<512, 1>(a, grid, st);
+    case 512 * 8 + 2: return launch_chaos_t<512, 2>(a, grid, st);
+    case 512 * 8 + 4: return launch_chaos_t<512, 4>(a, grid, st);
+    case 1024 * 8 + 1: return launch_chaos_t<1024, 1>(a, grid, st);
+    case 1024 * 8 + 2: return launch_chaos_t<1024, 2>(a, grid, st);
+    case 1024 * 8 + 4: return launch_chaos_t<1024, 4>(a, grid, st);
     default: return cudaErrorInvalidValue;
     }
 }

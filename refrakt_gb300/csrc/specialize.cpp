@@ -125,10 +125,7 @@ std::map<std::string, std::unique_ptr<Spec>> g_cache;  // key: device + source
 
 }  // namespace
 
-// struct GenEval: one inlined evaluator per xform of this genome's structure; apply() for one
-// walker, apply_wide() for kWide walkers of one group at once (chaos_wide.cuh)
-constexpr int kWide = 4;
-
+// struct GenEval: one inlined evaluator per xform of this genome's structure
 static std::string gen_eval(const std::vector<uint32_t>& prog) {
     std::ostringstream o;
     o << "namespace rfk {\n"
@@ -145,44 +142,19 @@ static std::string gen_eval(const std::vector<uint32_t>& prog) {
         emit_xform(o, prog, prog[H_FINAL], true);
         o << "      break; }\n";
     }
-    o << "    }\n  }\n";
-    // the same bodies over kWide walkers: the loops unroll into one straight-line run per xform
-    o << "  static __device__ __forceinline__ void apply_wide(const uint32_t* __restrict__ prog, int xi, float (&X)["
-      << kWide << "], float (&Y)[" << kWide << "], float (&C)[" << kWide << "], float (&OP)[" << kWide
-      << "], bool first_run, Jsf (&R)[" << kWide << "]) {\n    switch (xi) {\n";
-    auto wide_case = [&](uint32_t off, bool fin) {
-        o << "#pragma unroll\n      for (int q = 0; q < " << kWide << "; q++) {\n"
-          << "  float& x = X[q]; float& y = Y[q]; float& c = C[q]; float& op = OP[q]; Jsf& rng = R[q];\n";
-        emit_xform(o, prog, off, fin);
-        o << "      }\n      break; }\n";
-    };
-    for (uint32_t k = 0; k < nx; k++) {
-        o << (k + 1 == nx ? "    default: {\n" : "    case " + std::to_string(k) + ": {\n");
-        wide_case(prog[H_XOFF + k], false);
-    }
-    if (prog[H_HASFINAL] && prog[H_FINAL]) {
-        o << "    case -1: {\n";
-        wide_case(prog[H_FINAL], true);
-    }
     o << "    }\n  }\n};\n}  // namespace rfk\n";
     return o.str();
 }
 
 std::string spec_source(const std::vector<uint32_t>& prog, int threads, int spt, SpecKind kind) {
     std::ostringstream o;
-    // 512 threads x 8 slots: the wide body (kWide slots of one group per evaluation)
-    const bool wide = kind == SpecKind::Chaos && threads == 512 && spt == 8;
     o << "// generated: genome-specialised " << (kind == SpecKind::Batch ? "batch" : "chaos") << " kernel\n"
-      << (kind == SpecKind::Batch ? "#include \"batch_body.cuh\"\n"
-                                  : (wide ? "#include \"chaos_wide.cuh\"\n" : "#include \"chaos_body.cuh\"\n"))
+      << (kind == SpecKind::Batch ? "#include \"batch_body.cuh\"\n" : "#include \"chaos_body.cuh\"\n")
       << gen_eval(prog);
     if (kind == SpecKind::Batch)
         o << "extern \"C\" __global__ void __launch_bounds__(" << threads << ", " << 1024 / threads
           << ") rfk_batch_spec(const rfk::BatchArgs A) {\n  rfk::batch_body<" << threads << ", " << spt
           << ", rfk::GenEval>(A);\n}\n";
-    else if (wide)
-        o << "extern \"C\" __global__ void __launch_bounds__(512, 1) rfk_chaos_spec(const rfk::ChaosArgs A) {\n"
-          << "  rfk::chaos_body_wide<512, 8, " << kWide << ", rfk::GenEval>(A);\n}\n";
     else
         o << "extern \"C\" __global__ void __launch_bounds__(" << threads << ", " << 1024 / threads
           << ") rfk_chaos_spec(const rfk::ChaosArgs A) {\n  rfk::chaos_body<" << threads << ", " << spt

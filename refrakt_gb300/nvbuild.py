@@ -21,7 +21,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 
 # device headers the run-time compiler sees (specialize.cpp), embedded into the library
 RTC_HEADERS = ["rtc_types.h", "program.h", "device.cuh", "variations.cuh", "splat.cuh", "chaos_args.h",
-               "chaos_body.cuh", "chaos_wide.cuh", "batch_args.h", "batch_body.cuh"]
+               "chaos_body.cuh", "batch_args.h", "batch_body.cuh"]
 
 
 def _rtc_headers_source():
