@@ -7,6 +7,44 @@
 
 #include "device.cuh"
 
+#ifdef RFK_RTC
+// Genome-specialised kernels (compiled at run time) inline every xform's variations.  The FP32
+// library functions with long argument-reduction paths stay out of line there: one shared copy
+// each instead of one per call site keeps the kernel's code within the instruction caches.  The
+// same functions are called, so the results are unchanged.
+namespace rfk {
+static __device__ __noinline__ float m_sinf(float x) { return sinf(x); }
+static __device__ __noinline__ float m_cosf(float x) { return cosf(x); }
+static __device__ __noinline__ float m_tanf(float x) { return tanf(x); }
+static __device__ __noinline__ float m_expf(float x) { return expf(x); }
+static __device__ __noinline__ float m_logf(float x) { return logf(x); }
+static __device__ __noinline__ float m_sinhf(float x) { return sinhf(x); }
+static __device__ __noinline__ float m_coshf(float x) { return coshf(x); }
+static __device__ __noinline__ float m_powf(float x, float y) { return powf(x, y); }
+static __device__ __noinline__ float m_atan2f(float y, float x) { return atan2f(y, x); }
+static __device__ __noinline__ float2 m_sincosf(float x) {
+    float s, c;
+    sincosf(x, &s, &c);
+    return make_float2(s, c);
+}
+}  // namespace rfk
+#define sinf(a_) ::rfk::m_sinf(a_)
+#define cosf(a_) ::rfk::m_cosf(a_)
+#define tanf(a_) ::rfk::m_tanf(a_)
+#define expf(a_) ::rfk::m_expf(a_)
+#define logf(a_) ::rfk::m_logf(a_)
+#define sinhf(a_) ::rfk::m_sinhf(a_)
+#define coshf(a_) ::rfk::m_coshf(a_)
+#define powf(a_, b_) ::rfk::m_powf(a_, b_)
+#define atan2f(a_, b_) ::rfk::m_atan2f(a_, b_)
+#define sincosf(a_, s_, c_)                             \
+    do {                                                \
+        const float2 rfk_sc_ = ::rfk::m_sincosf(a_);    \
+        *(s_) = rfk_sc_.x;                              \
+        *(c_) = rfk_sc_.y;                              \
+    } while (0)
+#endif
+
 namespace rfk {
 
 constexpr float kPI = 3.14159265358979f;  // math.glsl:1, FP32
