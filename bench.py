@@ -47,6 +47,9 @@ WORKLOADS = {
                        "1024x768 + 64 random genomes (2-16 xforms) at 512x512 / 1024x768 / 1920x1080, 200 spp, "
                        "one persistent graph-captured launch",
                   genome=None, out=(1024, 768), ss=1, points=None, de=(9, 0, 0.4), image=True),
+    "gemm": dict(name="tcgen05 BF16 GEMM of the learned density estimator: 8192^3 (FP32 accumulation) and the "
+                      "U-Net's largest convolution GEMM (1,048,576 x 32 x 720)",
+                 genome=None, out=(512, 512), ss=1, points=None, de=None, image=False),
     "learned": dict(name="learned density estimation: U-Net (32-48-64-96, BF16 on tcgen05) trained on 2000 genomes "
                          "(seeds 1000-2999, 2-12 xforms) at 512x512, 16 spp -> 1000-spp adaptive-DE target; 200 "
                          "held-out genomes; 1080p frame time, learned vs plain",
@@ -515,6 +518,54 @@ def run_batch(args):
     return 0
 
 
+def run_gemm(args):
+    """Tensor-core GEMM throughput against the measured cuBLAS bf16 peak."""
+    import torch
+    import refrakt_gb300 as R
+    ws, rank, local = _dist()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    R.build()
+    g = torch.Generator(device="cuda").manual_seed(0)
+    res = {}
+    for name, (M, N, K) in (("square_8192", (8192, 8192, 8192)), ("unet_conv", (1048576, 32, 720)),
+                            ("unet_dw", (32, 720, 1048576))):
+        a = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+        b = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
+        c = torch.zeros(M, N, device="cuda")
+        splits = 64 if K > 65536 else 1
+        mode = R.GEMM_ATOMIC_F32 if splits > 1 else R.GEMM_STORE_F32
+        for _ in range(args.warmup):
+            R.gemm_bf16(a, b, c, mode=mode, splits=splits)
+        t = []
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            R.gemm_bf16(a, b, c, mode=mode, splits=splits)  # synchronises its stream
+            e1.record()
+            torch.cuda.synchronize()
+            t.append(e0.elapsed_time(e1))
+        ms = statistics.median(t)
+        res[name] = {"M": M, "N": N, "K": K, "ms": ms, "tflops": 2.0 * M * N * K / (ms * 1e-3) / 1e12}
+        del a, b, c
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, src = float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        peak, src = 1900.0, "fallback"
+    v = res["square_8192"]["tflops"]
+    print(json.dumps({
+        "metric": "TFLOP/s bf16 (tcgen05 GEMM)", "value": v, "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": res["square_8192"]["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16", "data": "random normal operands",
+        "config": {"workload": CONFIG_NAME}, "shapes": res,
+        "roofline": {"bound": "tensor", "achieved": v, "peak": peak, "unit": "TFLOP/s", "frac": v / peak,
+                     "traffic": None, "peak_source": src},
+        "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+    return 0
+
+
 def run_learned(args):
     import numpy as np
     import torch
@@ -707,6 +758,8 @@ def main():
         return run_batch(args)
     if args.workload == "learned":
         return run_learned(args)
+    if args.workload == "gemm":
+        return run_gemm(args)
     return run_native(args)
 
 
