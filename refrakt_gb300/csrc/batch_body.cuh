@@ -37,7 +37,7 @@ __device__ __forceinline__ void batch_body(const BatchArgs& A) {
     uint32_t* s_misc = reinterpret_cast<uint32_t*>(s_xid + 2 * G);  // [0] unit, [1..2] permutation ids
 
     const int tid = threadIdx.x;
-    const bool lane0 = (tid % kGroup) == 0;
+    const int dphase = draw_phase<THREADS, SPT>(tid);
     uint32_t drawn = 0, emitted = 0;
     unsigned long long steps = 0;
 
@@ -53,7 +53,7 @@ __device__ __forceinline__ void batch_body(const BatchArgs& A) {
         // seeds and start points of this unit's slots (flame.cpp:138-141, hammersley.cpp:29-48)
         const uint64_t gkey0 = derive_key(unit.seed, 0, 0, TAG_GLOBAL);
         for (int k = 0; k < SPT; k++) {
-            const uint32_t ls = k * THREADS + tid;
+            const uint32_t ls = phase_slot<THREADS>(k, tid);
             const Jsf r = jsf_seed((uint32_t)(ls + unit.seed * SLOTS));
             s_rng[ls] = make_uint4(r.a, r.b, r.c, r.d);
             float4 w;
@@ -73,22 +73,19 @@ __device__ __forceinline__ void batch_body(const BatchArgs& A) {
             const int buf = s & 1;
             const bool draw = s >= I.fuse;
             if (tid == 0) s_misc[1 + buf] = (uint32_t)(derive_key(unit.seed, s, 0, TAG_LOCAL) % A.table_size);
-            if (lane0) {
-#pragma unroll 1
-                for (int k = 0; k < SPT; k++) {
-                    const uint32_t ls = k * THREADS + tid;
-                    const uint4 r4 = s_rng[ls];
-                    Jsf rng{r4.x, r4.y, r4.z, r4.w};
-                    const int xi = select_xform(s_prog, randf(rng));
-                    s_rng[ls] = make_uint4(rng.a, rng.b, rng.c, rng.d);
-                    s_xid[buf * G + ls / kGroup] = xi;
-                }
+            if (dphase >= 0) {  // flame.glsl:51-53
+                const uint32_t ls = phase_slot<THREADS>(dphase, tid);
+                const uint4 r4 = s_rng[ls];
+                Jsf rng{r4.x, r4.y, r4.z, r4.w};
+                const int xi = select_xform(s_prog, randf(rng));
+                s_rng[ls] = make_uint4(rng.a, rng.b, rng.c, rng.d);
+                s_xid[buf * G + ls / kGroup] = xi;
             }
             __syncthreads();
             const uint32_t perm = s_misc[1 + buf];
 #pragma unroll 1
             for (int k = 0; k < SPT; k++) {
-                const uint32_t ls = k * THREADS + tid;
+                const uint32_t ls = phase_slot<THREADS>(k, tid);
                 const uint32_t j = (s == 0) ? ls
                                    : (s == I.fuse) ? feistel(ls, SLOTS, gkeyF)
                                                    : (uint32_t)A.table[(size_t)perm * SLOTS + ls];

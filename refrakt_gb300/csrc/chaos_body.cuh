@@ -32,6 +32,21 @@ struct InterpEval {
     }
 };
 
+// The slot a thread serves in phase k of a pass: phase k covers slots [k * THREADS, (k + 1) *
+// THREADS), and warps are permuted per phase (warp w serves warp w ^ k's 32 slots), so the 256-slot
+// groups' first slots fall to SPT * THREADS / 256 different warps, one per warp: the group xform
+// draws at the start of a pass run in parallel instead of SPT after another.
+template <int THREADS>
+__device__ __forceinline__ uint32_t phase_slot(int k, int tid) {
+    return (uint32_t)(k * THREADS + (tid ^ (32 * k)));
+}
+// the phase in which thread tid serves a group's first slot, or -1
+template <int THREADS, int SPT>
+__device__ __forceinline__ int draw_phase(int tid) {
+    const int k = (tid % kGroup) >> 5;
+    return ((tid & 31) == 0 && k < SPT) ? k : -1;
+}
+
 // Shared memory of a chaos CTA (dynamic, in this order):
 //   program words (prog_words), palette float4[256], walker exchange float4 [2][SLOTS],
 //   JSF32 states uint4[SLOTS], group xform ids int[2][SLOTS/256], per-pass permutation ids
@@ -48,8 +63,8 @@ __host__ __device__ inline size_t chaos_smem_bytes(int slots, uint32_t prog_word
 
 // One CTA of THREADS threads owns SLOTS = THREADS * SPT walker slots — the walker shuffle's mixing
 // domain — for the launch's passes.  Every slot's walker and JSF32 state live in shared memory;
-// each thread serves SPT slots per pass (slots k * THREADS + tid, in SPT different 256-slot
-// groups, so a warp's work per pass averages over SPT xforms).  64 registers per thread:
+// each thread serves SPT slots per pass (phase_slot(k, tid), in SPT different 256-slot groups, so
+// a warp's work per pass averages over SPT xforms).  64 registers per thread:
 // 1024 threads x 1, 512 x 2 or 256 x 4 CTAs per SM.
 template <int THREADS, int SPT, class Eval>
 __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
@@ -80,7 +95,7 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
     // sample (pass 0 of a warmup reads the start points instead, flame.glsl:58-61)
     const uint64_t gkey = derive_key(A.seed, A.pass0, ts, TAG_GLOBAL);
     for (int k = 0; k < SPT; k++) {
-        const uint32_t ls = k * THREADS + tid;
+        const uint32_t ls = phase_slot<THREADS>(k, tid);
         s_rng[ls] = A.rng[ts_base + gid0 + ls];
         const uint32_t src = feistel(gid0 + ls, A.ppts, gkey);
         float4 w;
@@ -97,7 +112,7 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
 
     const uint32_t foff = s_prog[H_FINAL];
     const bool has_final = A.draw && foff != 0;
-    const bool lane0 = (tid % kGroup) == 0;
+    const int dphase = draw_phase<THREADS, SPT>(tid);
     const float W = (float)A.W, H = (float)A.H;
     uint32_t drawn = 0, emitted = 0;
 
@@ -107,24 +122,21 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
         uint32_t src[SPT];
 #pragma unroll
         for (int k = 0; k < SPT; k++)
-            src[k] = (s == 0) ? (uint32_t)(k * THREADS + tid) : (uint32_t)A.table[(size_t)s_perm[s] * SLOTS + k * THREADS + tid];
-        if (lane0) {  // flame.glsl:51-53: the group's first slot draws the group's xform
-#pragma unroll 1
-            for (int k = 0; k < SPT; k++) {
-                const uint32_t ls = k * THREADS + tid;
-                const uint4 r4 = s_rng[ls];
-                Jsf rng{r4.x, r4.y, r4.z, r4.w};
-                const int xi = select_xform(s_prog, randf(rng));
-                s_rng[ls] = make_uint4(rng.a, rng.b, rng.c, rng.d);
-                s_xid[buf * G + ls / kGroup] = xi;
-                if (A.trace && A.pass0 + s < A.trace_passes)
-                    A.trace[(size_t)(A.pass0 + s) * A.n_groups + (ts_base + gid0 + ls) / kGroup] = (uint8_t)xi;
-            }
+            src[k] = (s == 0) ? phase_slot<THREADS>(k, tid) : (uint32_t)A.table[(size_t)s_perm[s] * SLOTS + phase_slot<THREADS>(k, tid)];
+        if (dphase >= 0) {  // flame.glsl:51-53: the group's first slot draws the group's xform
+            const uint32_t ls = phase_slot<THREADS>(dphase, tid);
+            const uint4 r4 = s_rng[ls];
+            Jsf rng{r4.x, r4.y, r4.z, r4.w};
+            const int xi = select_xform(s_prog, randf(rng));
+            s_rng[ls] = make_uint4(rng.a, rng.b, rng.c, rng.d);
+            s_xid[buf * G + ls / kGroup] = xi;
+            if (A.trace && A.pass0 + s < A.trace_passes)
+                A.trace[(size_t)(A.pass0 + s) * A.n_groups + (ts_base + gid0 + ls) / kGroup] = (uint8_t)xi;
         }
         __syncthreads();
 #pragma unroll 1
         for (int k = 0; k < SPT; k++) {
-            const uint32_t ls = k * THREADS + tid;
+            const uint32_t ls = phase_slot<THREADS>(k, tid);
             uint32_t j = src[0];
 #pragma unroll
             for (int q = 1; q < SPT; q++)
@@ -180,7 +192,7 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
     // each slot's final walker and state were written by the thread that owns the slot
     const int out_buf = A.steps & 1;
     for (int k = 0; k < SPT; k++) {
-        const uint32_t ls = k * THREADS + tid;
+        const uint32_t ls = phase_slot<THREADS>(k, tid);
         A.walk_out[ts_base + gid0 + ls] = s_w[out_buf * SLOTS + ls];
         A.rng[ts_base + gid0 + ls] = s_rng[ls];
     }
