@@ -50,6 +50,7 @@ __device__ __forceinline__ void batch_body(const BatchArgs& A) {
         const BatchInstance& I = A.inst[unit.instance];
         for (uint32_t i = tid; i < I.prog_words; i += THREADS) s_prog[i] = I.prog[i];
         for (int i = tid; i < 256; i += THREADS) s_pal[i] = I.palette[i];
+        const uint32_t passes = I.fuse + unit.draw;
         // seeds and start points of this unit's slots (flame.cpp:138-141, hammersley.cpp:29-48)
         const uint64_t gkey0 = derive_key(unit.seed, 0, 0, TAG_GLOBAL);
         for (int k = 0; k < SPT; k++) {
@@ -68,11 +69,19 @@ __device__ __forceinline__ void batch_body(const BatchArgs& A) {
         __syncthreads();
         const uint32_t foff = s_prog[H_FINAL];
         const float Wf = (float)I.W, Hf = (float)I.H;
-        const uint32_t passes = I.fuse + unit.draw;
         for (uint32_t s = 0; s < passes; s++) {
             const int buf = s & 1;
             const bool draw = s >= I.fuse;
-            if (tid == 0) s_misc[1 + buf] = (uint32_t)(derive_key(unit.seed, s, 0, TAG_LOCAL) % A.table_size);
+            // pass s + 1's permutation id; pass s's was written before the previous pass's barrier
+            if (tid == 0) s_misc[1 + (buf ^ 1)] = (uint32_t)(derive_key(unit.seed, s + 1, 0, TAG_LOCAL) % A.table_size);
+            // this pass's sources, loaded before the barrier
+            const uint32_t perm = s_misc[1 + buf];
+            uint32_t src[SPT];
+#pragma unroll
+            for (int k = 0; k < SPT; k++) {
+                const uint32_t ls = phase_slot<THREADS>(k, tid);
+                src[k] = (s == 0) ? ls : (s == I.fuse) ? feistel(ls, SLOTS, gkeyF) : (uint32_t)A.table[(size_t)perm * SLOTS + ls];
+            }
             if (dphase >= 0) {  // flame.glsl:51-53
                 const uint32_t ls = phase_slot<THREADS>(dphase, tid);
                 const uint4 r4 = s_rng[ls];
@@ -82,13 +91,13 @@ __device__ __forceinline__ void batch_body(const BatchArgs& A) {
                 s_xid[buf * G + ls / kGroup] = xi;
             }
             __syncthreads();
-            const uint32_t perm = s_misc[1 + buf];
 #pragma unroll 1
             for (int k = 0; k < SPT; k++) {
                 const uint32_t ls = phase_slot<THREADS>(k, tid);
-                const uint32_t j = (s == 0) ? ls
-                                   : (s == I.fuse) ? feistel(ls, SLOTS, gkeyF)
-                                                   : (uint32_t)A.table[(size_t)perm * SLOTS + ls];
+                uint32_t j = src[0];
+#pragma unroll
+                for (int q = 1; q < SPT; q++)
+                    if (q == k) j = src[q];
                 const float4 v = s_w[buf * SLOTS + j];
                 float x = v.x, y = v.y, c = v.z;
                 const uint4 r4 = s_rng[ls];
