@@ -48,7 +48,7 @@ WORKLOADS = {
                        "one persistent graph-captured launch",
                   genome=None, out=(1024, 768), ss=1, points=None, de=(9, 0, 0.4), image=True),
     "gemm": dict(name="tcgen05 BF16 GEMM of the learned density estimator: 8192^3 (FP32 accumulation) and the "
-                      "U-Net's largest convolution GEMM (1,048,576 x 32 x 720)",
+                      "U-Net's largest convolution (1,048,576 x 32 x 720) as a GEMM and as an implicit GEMM",
                  genome=None, out=(512, 512), ss=1, points=None, de=None, image=False),
     "learned": dict(name="learned density estimation: U-Net (32-48-64-96, BF16 on tcgen05) trained on 2000 genomes "
                          "(seeds 1000-2999, 2-12 xforms) at 512x512, 16 spp -> 1000-spp adaptive-DE target; 200 "
@@ -529,6 +529,20 @@ def run_gemm(args):
     R.build()
     g = torch.Generator(device="cuda").manual_seed(0)
     res = {}
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        t = []
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()  # launches on the current stream and synchronises it
+            e1.record()
+            torch.cuda.synchronize()
+            t.append(e0.elapsed_time(e1))
+        return statistics.median(t)
+
     for name, (M, N, K) in (("square_8192", (8192, 8192, 8192)), ("unet_conv", (1048576, 32, 720)),
                             ("unet_dw", (32, 720, 1048576))):
         a = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
@@ -536,19 +550,22 @@ def run_gemm(args):
         c = torch.zeros(M, N, device="cuda")
         splits = 64 if K > 65536 else 1
         mode = R.GEMM_ATOMIC_F32 if splits > 1 else R.GEMM_STORE_F32
-        for _ in range(args.warmup):
-            R.gemm_bf16(a, b, c, mode=mode, splits=splits)
-        t = []
-        for _ in range(args.steps):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            R.gemm_bf16(a, b, c, mode=mode, splits=splits)  # synchronises its stream
-            e1.record()
-            torch.cuda.synchronize()
-            t.append(e0.elapsed_time(e1))
-        ms = statistics.median(t)
+        ms = timed(lambda: R.gemm_bf16(a, b, c, mode=mode, splits=splits))
         res[name] = {"M": M, "N": N, "K": K, "ms": ms, "tflops": 2.0 * M * N * K / (ms * 1e-3) / 1e12}
         del a, b, c
+    # the same U-Net level-0 decoder convolution as an implicit GEMM: 48 channels upsampled from
+    # 512 x 512 and 32 skip channels at 1024 x 1024, 32 outputs, BF16 + bias + ReLU as in the network
+    xa = torch.randn(1, 512, 512, 48, device="cuda", generator=g).to(torch.bfloat16)
+    xb = torch.randn(1, 1024, 1024, 32, device="cuda", generator=g).to(torch.bfloat16)
+    wt = torch.randn(32, 720, device="cuda", generator=g).to(torch.bfloat16)
+    bias = torch.zeros(32, device="cuda")
+    c = torch.zeros(1048576, 32, device="cuda", dtype=torch.bfloat16)
+    ms = timed(lambda: R.conv3x3_bf16(xa, wt, c, xb=xb, up=True, mode=R.GEMM_STORE_BF16, bias=bias, relu=True))
+    hbm = (xa.numel() + xb.numel() + wt.numel() + c.numel()) * 2
+    res["unet_conv_implicit"] = {"M": 1048576, "N": 32, "K": 720, "ms": ms,
+                                 "tflops": 2.0 * 1048576 * 32 * 720 / (ms * 1e-3) / 1e12,
+                                 "hbm_bytes": hbm, "gbs": hbm / (ms * 1e-3) / 1e9}
+    del xa, xb, wt, c
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             peak, src = float(json.load(f)["bf16_tflops"]), "measured"

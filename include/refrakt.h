@@ -361,6 +361,16 @@ enum rf_gemm_mode { RF_GEMM_STORE_F32 = 0, RF_GEMM_STORE_BF16 = 1, RF_GEMM_ATOMI
 RF_API int rf_gemm_bf16(const void* A, const void* B, void* C, uint32_t M, uint32_t N, uint32_t K, uint32_t lda,
                         uint32_t ldb, uint32_t ldc, int mode, const float* bias, int relu, uint32_t splits,
                         void* stream);
+/* 3x3 convolution (stride 1, zero padding 1) as an implicit GEMM on the same tensor cores: the
+ * GEMM gathers its im2col rows from the inputs instead of reading a materialised matrix.
+ * Inputs are NHWC bf16: xa [n, h/2, w/2, ca] when up (nearest-neighbour upsampled to h x w) else
+ * [n, h, w, ca]; xb [n, h, w, cb] (channel-concatenated after xa; NULL when cb = 0); ca, cb
+ * multiples of 8.  B holds the weights as [N x 9 (ca + cb)] bf16 (row stride ldb), column
+ * k = tap * (ca + cb) + c with tap = (dy + 1) * 3 + (dx + 1).  C [n h w x N] (row stride ldc),
+ * mode and bias / relu as rf_gemm_bf16 (one split).  Synchronises the stream. */
+RF_API int rf_conv3x3_bf16(const void* xa, uint32_t ca, int up, const void* xb, uint32_t cb, uint32_t n, uint32_t h,
+                           uint32_t w, const void* B, uint32_t N, uint32_t ldb, void* C, uint32_t ldc, int mode,
+                           const float* bias, int relu, void* stream);
 
 /* ------------------------------------------------------------------------------------------
  * Learned density estimation (no reference counterpart).  A U-Net maps the features of a

@@ -176,6 +176,9 @@ _SIGS = {
     "rf_batch_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "rf_gemm_bf16": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_uint32] * 6 +
                      [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),
+    "rf_conv3x3_bf16": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_void_p] + [ctypes.c_uint32] * 4 +
+                        [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
+                         ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
     "rf_denoiser_create": ([ctypes.POINTER(DenoiserDesc), ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "rf_denoiser_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "rf_denoiser_set_stream": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
@@ -625,6 +628,21 @@ def gemm_bf16(a, b, c, mode=GEMM_STORE_F32, bias=None, relu=False, splits=1, str
     N = b.shape[0]
     _check(library().rf_gemm_bf16(_rows_ptr(a), _rows_ptr(b), _rows_ptr(c), M, N, K, a.stride(0), b.stride(0),
                                   c.stride(0), mode, _ptr(bias), int(relu), splits, _stream(stream)))
+
+
+def conv3x3_bf16(xa, w, c, xb=None, up=False, mode=GEMM_STORE_F32, bias=None, relu=False, stream=None):
+    """c (+)= conv3x3(concat(upsample(xa) if up else xa, xb)) · w as an implicit GEMM on the tensor
+    cores.  xa [n, h, w, ca] (or [n, h/2, w/2, ca] with up) and xb [n, h, w, cb] contiguous NHWC
+    bf16; w [N, 9 (ca + cb)] bf16, column k = tap (ca + cb) + channel, tap = (dy + 1) 3 + (dx + 1);
+    c [n h w, N] with contiguous rows."""
+    n, ha, wa, ca = xa.shape
+    h, wd = (2 * ha, 2 * wa) if up else (ha, wa)
+    cb = 0 if xb is None else xb.shape[3]
+    if w.shape[1] != 9 * (ca + cb):
+        raise ValueError("conv3x3_bf16: weights must have 9 (ca + cb) = %d columns" % (9 * (ca + cb)))
+    _check(library().rf_conv3x3_bf16(_ptr(xa), ca, int(up), _ptr(xb), cb, n, h, wd, _rows_ptr(w), w.shape[0],
+                                     w.stride(0), _rows_ptr(c), c.stride(0), mode, _ptr(bias), int(relu),
+                                     _stream(stream)))
 
 
 class Denoiser:

@@ -2,8 +2,9 @@
 // to the converged, tonemapped image.  Four levels of 32-48-64-96 channels, two 3x3 convolutions
 // + ReLU per level, 2x2 average pooling down, nearest-neighbour upsampling and channel-concatenated
 // skip connections up, a 1x1 output convolution to RGB.  Weights are FP32 masters with BF16 copies;
-// every convolution is an im2col + tcgen05 BF16 GEMM with FP32 accumulation (gemm.cu), and the
-// backward pass and the Adam update are the same GEMMs and hand-written kernels (denoise_ops.cu).
+// every 3x3 convolution is an implicit-im2col tcgen05 BF16 GEMM with FP32 accumulation (gemm.cu:
+// the GEMM gathers its operand rows from the NHWC activations), and the backward pass and the Adam
+// update are the same GEMMs and hand-written kernels (denoise_ops.cu).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -59,7 +60,6 @@ struct rf_denoiser {
     uint64_t P0 = 0;                // pixels at level 0 (max)
     uint32_t H = 0, W = 0, N = 0;   // current shape
     // scratch
-    __nv_bfloat16* col = nullptr;   // [P x K] im2col (also of dz)
     __nv_bfloat16* colt = nullptr;  // [K x P]
     __nv_bfloat16* dz = nullptr;    // [P x cout]
     __nv_bfloat16* dzt = nullptr;   // [cout x P]
@@ -159,11 +159,15 @@ int forward(rf_denoiser* D, const __nv_bfloat16* input, bool need_out) {
         const __nv_bfloat16* xa = c.src_a < 0 ? input : D->acts[c.src_a].x;
         const __nv_bfloat16* xb = c.src_b < 0 ? nullptr : D->acts[c.src_b].x;
         GemmArgs g{};
-        if (c.taps == 9) {
-            cudaError_t e = launch_im2col(xa, c.ca, c.up, xb, c.cb, n, hl, wl, D->col, st);
-            if (e != cudaSuccess) return cuda_fail(e, "im2col");
-            g.A = D->col;
-            g.lda = c.K();
+        if (c.taps == 9) {  // implicit convolution: the GEMM gathers its im2col rows from xa, xb
+            g.xa = xa;
+            g.xb = xb;
+            g.ca = c.ca;
+            g.cb = c.cb;
+            g.n = n;
+            g.h = hl;
+            g.w = wl;
+            g.up = c.up;
         } else {
             g.A = xa;
             g.lda = c.ca;
@@ -185,7 +189,7 @@ int forward(rf_denoiser* D, const __nv_bfloat16* input, bool need_out) {
             g.bias = c.b;
             g.relu = c.relu;
         }
-        cudaError_t e = launch_gemm(g, 1, st);
+        cudaError_t e = c.taps == 9 ? launch_gemm_conv(g, st) : launch_gemm(g, 1, st);
         if (e != cudaSuccess) return cuda_fail(e, "conv gemm");
     }
     return RF_OK;
@@ -258,11 +262,12 @@ int backward(rf_denoiser* D, const __nv_bfloat16* input, const float* target, fl
         if (c.src_a < 0) continue;  // first layer: no input gradient
         // input gradient: dX[P x Ctot] = conv(dz, flipped transposed weights)
         GemmArgs gx{};
-        if (c.taps == 9) {
-            e = launch_im2col(dzp, c.cout, 0, nullptr, 0, n, hl, wl, D->col, st);
-            if (e != cudaSuccess) return cuda_fail(e, "im2col of dz");
-            gx.A = D->col;
-            gx.lda = 9 * c.cout;
+        if (c.taps == 9) {  // implicit convolution of dz
+            gx.xa = dzp;
+            gx.ca = c.cout;
+            gx.n = n;
+            gx.h = hl;
+            gx.w = wl;
             gx.K = 9 * c.cout;
         } else {
             gx.A = dzp;
@@ -284,7 +289,7 @@ int backward(rf_denoiser* D, const __nv_bfloat16* input, const float* target, fl
             gx.ldc = c.ca + c.cb;
             gx.mode = kGemmStoreF32;
         }
-        e = launch_gemm(gx, 1, st);
+        e = c.taps == 9 ? launch_gemm_conv(gx, st) : launch_gemm(gx, 1, st);
         if (e != cudaSuccess) return cuda_fail(e, "input-gradient gemm");
         if (concat) {
             e = launch_split_concat_grad(D->dx, c.ca, c.cb, n, hl, wl, D->acts[c.src_a].dy, D->acts[c.src_b].dy, st);
@@ -369,7 +374,7 @@ int rf_denoiser_create(const rf_denoiser_desc* desc, rf_denoiser** out) {
         if (e != cudaSuccess) return bail(cuda_fail(e, "rf_denoiser_create: parameters"));
     }
     // activations and scratch at the maximum size
-    size_t col = 0, dx = 0, dz = 0;
+    size_t colt = 0, dx = 0, dz = 0;
     for (auto& a : D->acts) {
         const uint64_t P = D->P0 >> (2 * a.level);
         if (e == cudaSuccess) e = dalloc(D, &a.x, P * a.c);
@@ -377,12 +382,11 @@ int rf_denoiser_create(const rf_denoiser_desc* desc, rf_denoiser** out) {
     }
     for (auto& c : D->convs) {
         const uint64_t P = ((D->P0 >> (2 * c.level)) + 7) & ~7ull;
-        col = std::max<size_t>(col, P * std::max<uint32_t>(9 * (c.ca + c.cb), 9 * c.cout));
+        colt = std::max<size_t>(colt, P * c.K());
         dx = std::max<size_t>(dx, P * (c.ca + c.cb));
         dz = std::max<size_t>(dz, P * std::max<uint32_t>(c.cout, 8));
     }
-    if (e == cudaSuccess) e = dalloc(D, &D->col, col);
-    if (e == cudaSuccess) e = dalloc(D, &D->colt, col);
+    if (e == cudaSuccess) e = dalloc(D, &D->colt, colt);
     if (e == cudaSuccess) e = dalloc(D, &D->dz, dz);
     if (e == cudaSuccess) e = dalloc(D, &D->dzt, dz);
     if (e == cudaSuccess) e = dalloc(D, &D->dx, dx);

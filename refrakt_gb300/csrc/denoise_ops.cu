@@ -3,7 +3,9 @@
 // count a multiple of 8, so every pixel's channels are whole 16-byte vectors of bf16.
 //
 // A convolution's GEMM operand is its im2col matrix: row p = pixel, column k = tap * C + c with
-// tap = (dy + 1) * 3 + (dx + 1) — tap-major, so each tap's channels are one contiguous run.  A
+// tap = (dy + 1) * 3 + (dx + 1) — tap-major, so each tap's channels are one contiguous run.  The
+// forward and input-gradient GEMMs gather it on the fly (gemm.cu, launch_gemm_conv); the weight
+// gradient reads its transpose, materialised here.  A
 // decoder convolution reads two inputs, channel-concatenated: the coarser level upsampled by
 // nearest neighbour (first Ca channels) and the encoder's skip tensor (next Cb channels).
 #include <cuda_bf16.h>
@@ -16,34 +18,6 @@ namespace rfk {
 namespace {
 
 __device__ __forceinline__ uint4 zero16() { return make_uint4(0, 0, 0, 0); }
-
-// one thread per (pixel, tap, 8-channel chunk)
-__global__ void im2col_kernel(const __nv_bfloat16* __restrict__ xa, uint32_t ca, int up,
-                              const __nv_bfloat16* __restrict__ xb, uint32_t cb, uint32_t n, uint32_t h, uint32_t w,
-                              __nv_bfloat16* __restrict__ col) {
-    const uint32_t ct = ca + cb, chunks = ct / 8;
-    const uint64_t total = (uint64_t)n * h * w * 9 * chunks;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t q = (uint32_t)(i % chunks);
-        const uint64_t t = i / chunks;
-        const uint32_t tap = (uint32_t)(t % 9);
-        const uint64_t p = t / 9;
-        const uint32_t x = (uint32_t)(p % w), y = (uint32_t)((p / w) % h), b = (uint32_t)(p / ((uint64_t)w * h));
-        const int sy = (int)y + (int)(tap / 3) - 1, sx = (int)x + (int)(tap % 3) - 1;
-        uint4 v = zero16();
-        if (sy >= 0 && sx >= 0 && sy < (int)h && sx < (int)w) {
-            const uint32_t c = q * 8;
-            if (c < ca) {
-                const uint32_t ha = up ? h / 2 : h, wa = up ? w / 2 : w;
-                const uint32_t ay = up ? (uint32_t)sy / 2 : (uint32_t)sy, ax = up ? (uint32_t)sx / 2 : (uint32_t)sx;
-                v = *reinterpret_cast<const uint4*>(xa + (((uint64_t)b * ha + ay) * wa + ax) * ca + c);
-            } else {
-                v = *reinterpret_cast<const uint4*>(xb + (((uint64_t)b * h + sy) * w + sx) * cb + (c - ca));
-            }
-        }
-        *reinterpret_cast<uint4*>(col + p * (9ull * ct) + (uint64_t)tap * ct + q * 8) = v;
-    }
-}
 
 // transposed im2col for the weight gradient: colT[k][p], k = tap * C + c (C = ca + cb); with
 // taps = 1 only the centre tap (a plain transpose, for a 1x1 convolution)
@@ -266,13 +240,6 @@ unsigned grid_for(uint64_t n, unsigned threads) {
 }
 
 }  // namespace
-
-cudaError_t launch_im2col(const __nv_bfloat16* xa, uint32_t ca, int up, const __nv_bfloat16* xb, uint32_t cb,
-                          uint32_t n, uint32_t h, uint32_t w, __nv_bfloat16* col, cudaStream_t st) {
-    const uint64_t total = (uint64_t)n * h * w * 9 * ((ca + cb) / 8);
-    im2col_kernel<<<grid_for(total, 256), 256, 0, st>>>(xa, ca, up, xb, cb, n, h, w, col);
-    return cudaGetLastError();
-}
 
 cudaError_t launch_im2col_t(const __nv_bfloat16* xa, uint32_t ca, int up, const __nv_bfloat16* xb, uint32_t cb,
                             uint32_t taps, uint32_t n, uint32_t h, uint32_t w, __nv_bfloat16* colt, uint32_t ldp,

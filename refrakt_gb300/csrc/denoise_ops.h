@@ -8,8 +8,6 @@
 
 namespace rfk {
 
-cudaError_t launch_im2col(const __nv_bfloat16* xa, uint32_t ca, int up, const __nv_bfloat16* xb, uint32_t cb,
-                          uint32_t n, uint32_t h, uint32_t w, __nv_bfloat16* col, cudaStream_t st);
 cudaError_t launch_im2col_t(const __nv_bfloat16* xa, uint32_t ca, int up, const __nv_bfloat16* xb, uint32_t cb,
                             uint32_t taps, uint32_t n, uint32_t h, uint32_t w, __nv_bfloat16* colt, uint32_t ldp,
                             cudaStream_t st);

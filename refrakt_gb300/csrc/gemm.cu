@@ -8,7 +8,8 @@
 // no-swizzle core-matrix layout (umma.cuh) through a 3-stage ring; thread 0 issues four
 // M128 x N x K16 MMAs per stage and commits them to the stage's mbarrier, which releases the
 // stage for refilling.  The epilogue reads the accumulator with tcgen05.ld (warp w owns rows
-// 32w..32w+31) and applies one of: FP32 store, bias + ReLU + BF16 store, FP32 atomic add.
+// 32w..32w+31), stages 32 columns at a time in shared memory and writes whole row segments with
+// one of: FP32 store, bias + ReLU + BF16 store, FP32 atomic add.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -31,19 +32,72 @@ __host__ __device__ constexpr size_t gemm_smem() {
     return 1024 + (size_t)kStages * (kBM * 128 + BN * 128) + 64;
 }
 
-template <int BN>
-__device__ __forceinline__ void load_stage(const GemmArgs& g, uint32_t sA, uint32_t sB, uint32_t m0, uint32_t n0,
-                                           uint32_t kbase, uint32_t k1, int tid) {
+// The pixels of a thread's A rows in an implicit convolution: thread tid loads rows
+// 16 i + 8 (tid / 64) + tid % 8 (i = 0..7) of the tile at one K chunk per stage (load_stage's
+// mapping), so their coordinates are computed once per tile.
+struct ConvRows {
+    uint32_t p[kBM / 16];    // pixel index, or ~0u past M
+    uint32_t yx[kBM / 16];   // y << 16 | x
+    uint32_t img[kBM / 16];  // image index (read for an upsampled input only)
+};
+
+__device__ __forceinline__ ConvRows conv_rows(const GemmArgs& g, uint32_t m0, int tid) {
+    ConvRows cr;
+#pragma unroll
+    for (int i = 0; i < (int)(kBM / 16); i++) {
+        const uint32_t p = m0 + 16u * i + 8u * ((uint32_t)tid >> 6) + ((uint32_t)tid & 7u);
+        const uint32_t q = p / g.w, x = p - q * g.w, y = q % g.h;
+        cr.p[i] = p < g.M ? p : ~0u;
+        cr.yx[i] = (y << 16) | x;
+        cr.img[i] = q / g.h;
+    }
+    return cr;
+}
+
+template <int BN, bool CONV>
+__device__ __forceinline__ void load_stage(const GemmArgs& g, const ConvRows& cr, uint32_t sA, uint32_t sB, uint32_t m0,
+                                           uint32_t n0, uint32_t kbase, uint32_t k1, int tid) {
     // virtual warp v covers rows 8*(v/2) .. +7 and K chunks 4*(v%2) .. +3: 64 contiguous bytes of
     // 8 rows in global memory, four whole core matrices (512 contiguous bytes) in shared memory
+    if constexpr (CONV) {
+        // this thread's K chunk: one tap and 8 channels of one input
+        const uint32_t kc = 4u * (((uint32_t)tid >> 5) & 1u) + (((uint32_t)tid & 31u) >> 3);
+        const uint32_t k = kbase + kc * 8u, ct = g.ca + g.cb;
+        const uint32_t tap = k / ct, c = k - tap * ct;
+        const int dy = (int)(tap / 3u) - 1, dx = (int)(tap % 3u) - 1;
+        const bool kok = k < k1;
 #pragma unroll
-    for (int i = 0; i < (int)(kBM * 8 / kThreads); i++) {
-        const uint32_t idx = tid + kThreads * i, l = idx & 31u, v = idx >> 5;
-        const uint32_t r = 8u * (v >> 1) + (l & 7u), kc = 4u * (v & 1u) + (l >> 3);
-        const uint32_t row = m0 + r, k = kbase + kc * 8u;
-        const bool ok = row < g.M && k < k1;
-        const __nv_bfloat16* src = ok ? g.A + (size_t)row * g.lda + k : g.A;
-        umma::cp_async16(sA + umma::tile_offset(r, kc), src, ok ? 16u : 0u);
+        for (int i = 0; i < (int)(kBM / 16); i++) {
+            const uint32_t r = 16u * i + 8u * ((uint32_t)tid >> 6) + ((uint32_t)tid & 7u);
+            const int y = (int)(cr.yx[i] >> 16) + dy, x = (int)(cr.yx[i] & 0xFFFFu) + dx;
+            const bool ok = kok && cr.p[i] != ~0u && y >= 0 && x >= 0 && y < (int)g.h && x < (int)g.w;
+            const __nv_bfloat16* src = g.xb ? g.xb : g.xa;
+            if (ok) {
+                const uint32_t p = cr.p[i] + (uint32_t)(dy * (int)g.w + dx);  // same image: the row and column are in range
+                if (c < g.ca) {
+                    if (g.up) {
+                        const uint32_t hw = (g.h / 2u) * (g.w / 2u);
+                        src = g.xa +
+                              ((size_t)cr.img[i] * hw + (size_t)((uint32_t)y >> 1) * (g.w / 2u) + ((uint32_t)x >> 1)) * g.ca + c;
+                    } else {
+                        src = g.xa + (size_t)p * g.ca + c;
+                    }
+                } else {
+                    src = g.xb + (size_t)p * g.cb + (c - g.ca);
+                }
+            }
+            umma::cp_async16(sA + umma::tile_offset(r, kc), src, ok ? 16u : 0u);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < (int)(kBM * 8 / kThreads); i++) {
+            const uint32_t idx = tid + kThreads * i, l = idx & 31u, v = idx >> 5;
+            const uint32_t r = 8u * (v >> 1) + (l & 7u), kc = 4u * (v & 1u) + (l >> 3);
+            const uint32_t row = m0 + r, k = kbase + kc * 8u;
+            const bool ok = row < g.M && k < k1;
+            const __nv_bfloat16* src = ok ? g.A + (size_t)row * g.lda + k : g.A;
+            umma::cp_async16(sA + umma::tile_offset(r, kc), src, ok ? 16u : 0u);
+        }
     }
 #pragma unroll
     for (int i = 0; i < (int)(BN * 8 / kThreads); i++) {
@@ -56,7 +110,36 @@ __device__ __forceinline__ void load_stage(const GemmArgs& g, uint32_t sA, uint3
     }
 }
 
-template <int BN>
+constexpr uint32_t kStageLd = 36;  // floats per row of the epilogue's staging block (32 + 4 against bank conflicts)
+
+// writes columns n .. n + min(4, left) - 1 of one output row at element offset o
+__device__ __forceinline__ void store4(const GemmArgs& g, size_t o, uint32_t left, float4 v, bool vec) {
+    const float e[4] = {v.x, v.y, v.z, v.w};
+    if (g.mode == kGemmStoreF32) {
+        float* c = static_cast<float*>(g.C) + o;
+        if (vec && left >= 4) {
+            *reinterpret_cast<float4*>(c) = v;
+        } else {
+            for (uint32_t j = 0; j < 4 && j < left; j++) c[j] = e[j];
+        }
+    } else if (g.mode == kGemmAtomicF32) {
+        float* c = static_cast<float*>(g.C) + o;
+        for (uint32_t j = 0; j < 4 && j < left; j++) atomicAdd(c + j, e[j]);
+    } else {
+        __nv_bfloat16* c = static_cast<__nv_bfloat16*>(g.C) + o;
+        if (vec && left >= 4) {
+            const __nv_bfloat162 lo = __floats2bfloat162_rn(v.x, v.y), hi = __floats2bfloat162_rn(v.z, v.w);
+            uint2 u;
+            u.x = *reinterpret_cast<const uint32_t*>(&lo);
+            u.y = *reinterpret_cast<const uint32_t*>(&hi);
+            *reinterpret_cast<uint2*>(c) = u;
+        } else {
+            for (uint32_t j = 0; j < 4 && j < left; j++) c[j] = __float2bfloat16_rn(e[j]);
+        }
+    }
+}
+
+template <int BN, bool CONV>
 __global__ void __launch_bounds__(kThreads, 1) umma_gemm_kernel(const GemmArgs g) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned char* smem = smem_raw + ((1024u - (umma::smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -86,10 +169,12 @@ __global__ void __launch_bounds__(kThreads, 1) umma_gemm_kernel(const GemmArgs g
     umma::fence_after_sync();
     const uint32_t tmem = *s_tmem;
     const uint32_t idesc = umma::idesc_bf16_f32(kBM, n_tile);
+    ConvRows cr;
+    if constexpr (CONV) cr = conv_rows(g, m0, tid);
 
     for (int s = 0; s < kStages - 1; s++) {
-        if ((uint32_t)s < nk) load_stage<BN>(g, base + s * (kA + kB), base + s * (kA + kB) + kA, m0, n0,
-                                             k0 + s * umma::kTileK, k1, tid);
+        if ((uint32_t)s < nk) load_stage<BN, CONV>(g, cr, base + s * (kA + kB), base + s * (kA + kB) + kA, m0, n0,
+                                                   k0 + s * umma::kTileK, k1, tid);
         umma::cp_async_commit();
     }
     for (uint32_t kb = 0; kb < nk; kb++) {
@@ -117,8 +202,8 @@ __global__ void __launch_bounds__(kThreads, 1) umma_gemm_kernel(const GemmArgs g
                 }
             }
             const uint32_t ns = nxt % kStages;
-            load_stage<BN>(g, base + ns * (kA + kB), base + ns * (kA + kB) + kA, m0, n0, k0 + nxt * umma::kTileK,
-                           k1, tid);
+            load_stage<BN, CONV>(g, cr, base + ns * (kA + kB), base + ns * (kA + kB) + kA, m0, n0,
+                                 k0 + nxt * umma::kTileK, k1, tid);
         }
         umma::cp_async_commit();
     }
@@ -134,31 +219,44 @@ __global__ void __launch_bounds__(kThreads, 1) umma_gemm_kernel(const GemmArgs g
     umma::fence_after_sync();
 
     if (*s_fail == 0 && (nk > 0 || g.mode != kGemmAtomicF32)) {
-        const uint32_t m = m0 + 32u * warp + lane;
-        for (uint32_t c0 = 0; c0 < n_tile; c0 += 16) {
-            float v[16];
-            if (nk > 0) {
-                umma::tmem_ld16(tmem + ((32u * warp) << 16) + c0, v);
-            } else {
+        // 32 columns at a time: each warp moves its 32 accumulator rows through shared memory
+        // (the free operand stages), then the CTA writes whole row segments, 4 columns per thread
+        float* stage = reinterpret_cast<float*>(smem);  // [128][kStageLd]
+        const bool vec = ((reinterpret_cast<uintptr_t>(g.C) & 15u) == 0) && (g.ldc % 4u == 0);
+        for (uint32_t c0 = 0; c0 < n_tile; c0 += 32) {
 #pragma unroll
-                for (int j = 0; j < 16; j++) v[j] = 0.0f;
-            }
-            if (m >= g.M) continue;
-#pragma unroll
-            for (int j = 0; j < 16; j++) {
-                const uint32_t n = n0 + c0 + j;
-                if (n >= g.N) break;
-                const size_t o = (size_t)m * g.ldc + n;
-                if (g.mode == kGemmStoreF32) {
-                    static_cast<float*>(g.C)[o] = v[j];
-                } else if (g.mode == kGemmAtomicF32) {
-                    atomicAdd(static_cast<float*>(g.C) + o, v[j]);
+            for (uint32_t hh = 0; hh < 2; hh++) {
+                const uint32_t cc = c0 + 16u * hh;
+                if (cc >= n_tile) break;  // n_tile is a multiple of 16
+                float v[16];
+                if (nk > 0) {
+                    umma::tmem_ld16(tmem + ((32u * warp) << 16) + cc, v);
                 } else {
-                    float y = v[j] + (g.bias ? g.bias[n] : 0.0f);
-                    if (g.relu) y = fmaxf(y, 0.0f);
-                    static_cast<__nv_bfloat16*>(g.C)[o] = __float2bfloat16_rn(y);
+#pragma unroll
+                    for (int j = 0; j < 16; j++) v[j] = 0.0f;
                 }
+                if (g.mode == kGemmStoreBF16) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        const uint32_t n = n0 + cc + j;
+                        float y = v[j] + ((g.bias && n < g.N) ? g.bias[n] : 0.0f);
+                        v[j] = g.relu ? fmaxf(y, 0.0f) : y;
+                    }
+                }
+                float4* dst = reinterpret_cast<float4*>(stage + (32u * warp + lane) * kStageLd + 16u * hh);
+#pragma unroll
+                for (int q = 0; q < 4; q++) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
             }
+            __syncthreads();
+            const uint32_t pieces = (n_tile - c0 < 32u ? n_tile - c0 : 32u) / 4u;  // 4-column pieces per row
+            for (uint32_t idx = tid; idx < kBM * pieces; idx += kThreads) {
+                const uint32_t r = idx / pieces, pc = idx - r * pieces;
+                const uint32_t m = m0 + r, n = n0 + c0 + 4u * pc;
+                if (m >= g.M || n >= g.N) continue;
+                const float4 v = *reinterpret_cast<const float4*>(stage + r * kStageLd + 4u * pc);
+                store4(g, (size_t)m * g.ldc + n, g.N - n, v, vec);
+            }
+            __syncthreads();
         }
     }
     umma::fence_before_sync();
@@ -166,13 +264,14 @@ __global__ void __launch_bounds__(kThreads, 1) umma_gemm_kernel(const GemmArgs g
     if (warp == 0) umma::tmem_free(tmem, kCols);
 }
 
-template <int BN>
+template <int BN, bool CONV = false>
 cudaError_t launch_bn(const GemmArgs& g, uint32_t splits, cudaStream_t st) {
     const size_t smem = gemm_smem<BN>();
-    cudaError_t e = cudaFuncSetAttribute(umma_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(umma_gemm_kernel<BN, CONV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const dim3 grid((g.N + BN - 1) / BN, (g.M + kBM - 1) / kBM, splits);
-    umma_gemm_kernel<BN><<<grid, kThreads, smem, st>>>(g);
+    umma_gemm_kernel<BN, CONV><<<grid, kThreads, smem, st>>>(g);
     return cudaGetLastError();
 }
 
@@ -190,6 +289,20 @@ cudaError_t launch_gemm(GemmArgs g, uint32_t splits, cudaStream_t st) {
     if (g.N <= 64) return launch_bn<64>(g, splits, st);
     if (g.N <= 128) return launch_bn<128>(g, splits, st);
     return launch_bn<256>(g, splits, st);
+}
+
+cudaError_t launch_gemm_conv(GemmArgs g, cudaStream_t st) {
+    if (g.ca % 8 || g.cb % 8 || g.ca + g.cb == 0 || g.n == 0 || g.h == 0 || g.w == 0 || g.h > 65535 || g.w > 65535)
+        return cudaErrorInvalidValue;
+    if (!g.xa || (g.cb && !g.xb) || (uint64_t)g.n * g.h * g.w != g.M || g.K != 9u * (g.ca + g.cb) || g.ldb % 8 ||
+        g.N == 0 || ((uintptr_t)g.xa | (uintptr_t)g.xb | (uintptr_t)g.B) & 15)
+        return cudaErrorInvalidValue;
+    g.A = nullptr;
+    g.lda = 0;
+    g.k_per_split = (g.K + umma::kTileK - 1) / umma::kTileK * umma::kTileK;
+    if (g.N <= 64) return launch_bn<64, true>(g, 1, st);
+    if (g.N <= 128) return launch_bn<128, true>(g, 1, st);
+    return launch_bn<256, true>(g, 1, st);
 }
 
 cudaError_t gemm_error(int* out) {

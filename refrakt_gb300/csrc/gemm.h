@@ -19,10 +19,21 @@ struct GemmArgs {
     const float* bias;       // StoreBF16: per column n, may be null
     int relu;                // StoreBF16: max(0, .)
     uint32_t k_per_split;    // set by launch_gemm
+    // implicit 3x3 convolution (launch_gemm_conv): A is not read from memory as a matrix but
+    // gathered from NHWC inputs as their im2col matrix, row p = pixel (n x h x w), column
+    // k = tap * (ca + cb) + c, tap = (dy + 1) * 3 + (dx + 1); channels [0, ca) come from xa (at half
+    // resolution, nearest-neighbour upsampled, when up), [ca, ca + cb) from xb
+    const __nv_bfloat16* xa;
+    const __nv_bfloat16* xb;
+    uint32_t ca, cb, n, h, w;
+    int up;
 };
 
 // splits > 1 partitions K over grid.z and requires kGemmAtomicF32 (C accumulates)
 cudaError_t launch_gemm(GemmArgs g, uint32_t splits, cudaStream_t st);
+// C = im2col(xa, xb) * B^T without materialising the im2col matrix; M = n h w, K = 9 (ca + cb),
+// ca and cb multiples of 8, one split
+cudaError_t launch_gemm_conv(GemmArgs g, cudaStream_t st);
 // reads and clears the kernels' error word (0 = no bounded wait ran out)
 cudaError_t gemm_error(int* out);
 
