@@ -6,14 +6,15 @@
 // An autotuner picks the work-unit shape: the walkers per unit (1024, 2048 or 4096 — the walker
 // shuffle's mixing domain) by timing a short probe batch of the actual genomes on each shape and
 // weighting throughput by the shape's statistical efficiency, and the drawing passes per unit
-// so that the units outnumber the persistent CTAs eight times over while the fuse passes cost
-// at most 5 % of a unit.
+// that finish the batch first on the persistent CTAs (simulated longest-first), counting each
+// unit's fuse passes.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <atomic>
 #include <thread>
 #include <map>
+#include <queue>
 #include <string>
 #include <cstring>
 #include <vector>
@@ -115,6 +116,28 @@ void destroy_batch(rf_batch* b) {
 
 int cuda_err(cudaError_t e, const char* what) {
     return fail(RF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Passes until the last CTA finishes when unit_passes = per cuts every item's drawing passes
+// into equal units (as build_tables does), each also running the fuse passes, and `ctas`
+// persistent CTAs take them longest first (each the next unit when it finishes its own).
+double unit_makespan(const std::vector<uint64_t>& need, uint64_t per, uint32_t fuse, int ctas) {
+    std::vector<uint64_t> len;
+    for (uint64_t nd : need) {
+        const uint64_t nu = std::max<uint64_t>(1, (nd + per - 1) / per), u = (nd + nu - 1) / nu;
+        for (uint64_t i = 0; i < nu; i++) len.push_back(u + fuse);
+    }
+    std::sort(len.rbegin(), len.rend());
+    std::priority_queue<uint64_t, std::vector<uint64_t>, std::greater<uint64_t>> load;
+    for (int i = 0; i < std::max(1, ctas); i++) load.push(0);
+    uint64_t last = 0;
+    for (uint64_t l : len) {
+        const uint64_t t = load.top() + l;
+        load.pop();
+        load.push(t);
+        last = std::max(last, t);
+    }
+    return (double)last;
 }
 
 // Builds the instance and unit tables for a shape; `probe_passes` > 0 builds an autotuner probe
@@ -369,12 +392,31 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
     } else {
         for (auto& it : b->items) it.splat = d->splat == RF_SPLAT_WARP ? 1u : 0u;
     }
-    // --- drawing passes per unit: >= 8 units per persistent CTA, fuse <= 5 % of a unit
+    // --- drawing passes per unit: the candidate whose units, taken longest first by the
+    // persistent CTAs, finish first (a batch of few points wants one short unit per SM even at a
+    // large fuse share; a large batch several units per CTA for balance); within 2 % the longer
+    // units win (fewer fuse passes)
+    std::vector<uint64_t> need;
     uint64_t total_passes = 0;
-    for (auto& it : b->items) total_passes += (it.desc.points + b->slots - 1) / b->slots;
-    uint64_t per = d->unit_passes ? d->unit_passes : total_passes / (8ull * sms);
-    per = std::max<uint64_t>(per, d->unit_passes ? 1 : 20ull * b->fuse);
-    per = std::min<uint64_t>(per, 1u << 20);
+    for (auto& it : b->items) {
+        need.push_back((it.desc.points + b->slots - 1) / b->slots);
+        total_passes += need.back();
+    }
+    uint64_t per = d->unit_passes;
+    if (per == 0) {
+        std::vector<uint64_t> cands = {20ull * b->fuse};
+        for (uint64_t k : {1, 2, 3, 4, 6, 8, 12, 16}) cands.push_back((total_passes + k * sms - 1) / (k * sms));
+        double best_t = 0.0;
+        for (uint64_t c : cands) {
+            c = std::min<uint64_t>(std::max<uint64_t>(c, 1), 1u << 20);
+            const double t = unit_makespan(need, c, b->fuse, sms);
+            if (per == 0 || t < best_t * 0.98 || (t <= best_t * 1.02 && c > per)) {
+                if (per == 0 || t < best_t) best_t = t;
+                per = c;
+            }
+        }
+    }
+    per = std::min<uint64_t>(std::max<uint64_t>(per, 1), 1u << 20);
     b->unit_passes = (uint32_t)per;
     // --- genome-specialised kernels for the structures with >= 2 units per SM (animation frames
     // share one), compiled in parallel and cached across batches, each a persistent launch of its
@@ -391,8 +433,9 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
             rep.emplace(it.structure, &it);
         }
         std::vector<std::pair<uint64_t, std::string>> order;
-        for (auto& kv : units_of)
-            if (kv.second >= (uint64_t)kSpecMinUnitsPerSM * sms) order.push_back({kv.second, kv.first});
+        for (auto& kv : units_of)  // (a batch of one structure always: no other launch to balance against)
+            if (kv.second >= (uint64_t)kSpecMinUnitsPerSM * sms || units_of.size() == 1)
+                order.push_back({kv.second, kv.first});
         std::sort(order.rbegin(), order.rend());
         std::vector<const void*> kern(order.size(), nullptr);
         std::vector<int> rcs(order.size(), RF_OK);

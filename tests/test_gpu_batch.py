@@ -142,6 +142,19 @@ def test_splat_strategies_agree_and_autotune_picks_warp_for_compact(rk, compiler
         assert np.allclose(g[0], w[0], rtol=1e-4, atol=1e-3)
 
 
+def test_autotuned_units_fill_the_gpu(rk, compiler):
+    # a single short render is cut into about one unit per SM, not a few long ones
+    import torch
+    f = rk.Flame.synthesize(compiler, rk.SYNTH_RANDOM, 7, 1024, 1024, n_xforms=4)
+    b = rk.Batch([(f, 1024, 1024, 16 * 1024 * 1024, 1)], density_estimation=False)
+    info = b.info()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert info["units"] >= sms // 2, info
+    b.run()
+    assert b.sync()["points"] >= 16 * 1024 * 1024
+    b.close()
+
+
 def test_autotuned_shape_covers_points(rk, compiler):
     fl = [rk.Flame.synthesize(compiler, rk.SYNTH_RANDOM, s, 128, 128, n_xforms=2 + s % 8) for s in range(12)]
     pts = [(1 + s % 3) * 3_000_000 for s in range(12)]
