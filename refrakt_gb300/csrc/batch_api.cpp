@@ -14,6 +14,7 @@
 #include <atomic>
 #include <thread>
 #include <map>
+#include <mutex>
 #include <queue>
 #include <string>
 #include <cstring>
@@ -55,6 +56,10 @@ constexpr uint64_t kTableSeed = 0x5eed;                      // shared table: ke
 constexpr uint32_t kSpecMinUnitsPerSM = 2;  // a structure gets a persistent launch from 2 units per SM
 constexpr unsigned kCompileThreads = 16;    // run-time compilations in parallel
 constexpr double kCompactShare = 16.0;  // probe points sharing a point's bin above this: compact attractor
+
+// unit shape (walkers per unit) chosen per device and set of genome structures
+std::mutex g_shape_mu;
+std::map<std::string, uint32_t> g_shape_cache;
 
 // Histogram L1 noise of a mixing domain relative to the reference's global shuffle, measured on
 // the CPU oracle (tests/test_oracle_self.py): variance grows with its square.
@@ -342,9 +347,26 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
 
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-    // --- autotune the unit shape on a probe batch of the actual genomes
+    // --- autotune the unit shape on a probe batch of the actual genomes; the choice is kept per
+    // device and set of genome structures, so the frames of an animation probe once
+    for (auto& it : b->items) it.structure = spec_structure(it.prog);
+    std::string shape_key;
+    {
+        std::vector<std::string> st;
+        for (auto& it : b->items) st.push_back(it.structure);
+        std::sort(st.begin(), st.end());
+        st.erase(std::unique(st.begin(), st.end()), st.end());
+        shape_key = std::to_string(b->device);
+        for (auto& x : st) shape_key += "|" + x;
+    }
     std::vector<uint32_t> shapes = {1024, 2048, 4096};
-    if (d->cta_slots) shapes = {d->cta_slots};
+    if (d->cta_slots) {
+        shapes = {d->cta_slots};
+    } else {
+        std::lock_guard<std::mutex> lk(g_shape_mu);
+        auto hit = g_shape_cache.find(shape_key);
+        if (hit != g_shape_cache.end()) shapes = {hit->second};
+    }
     double best = -1.0;
     for (uint32_t slots : shapes) {
         if (shapes.size() == 1) { b->slots = slots; break; }
@@ -365,6 +387,10 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
         if (rate > best) { best = rate; b->slots = slots; }
     }
     b->threads = 1024;
+    if (!d->cta_slots) {
+        std::lock_guard<std::mutex> lk(g_shape_mu);
+        g_shape_cache[shape_key] = b->slots;
+    }
     if (int rc = make_table(b, b->slots)) return bail(rc);
     // --- splat strategy per genome: a compact attractor (its 16-pass probe unit's points share
     // their bins with many others) takes the warp-aggregated reductions
@@ -428,7 +454,6 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
         std::map<std::string, uint64_t> units_of;
         std::map<std::string, const Item*> rep;
         for (auto& it : b->items) {
-            it.structure = spec_structure(it.prog);
             units_of[it.structure] += std::max<uint64_t>(1, ((it.desc.points + b->slots - 1) / b->slots + per - 1) / per);
             rep.emplace(it.structure, &it);
         }
