@@ -10,6 +10,8 @@
 // stage for refilling.  The epilogue reads the accumulator with tcgen05.ld (warp w owns rows
 // 32w..32w+31), stages 32 columns at a time in shared memory and writes whole row segments with
 // one of: FP32 store, bias + ReLU + BF16 store, FP32 atomic add.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -139,6 +141,52 @@ __device__ __forceinline__ void store4(const GemmArgs& g, size_t o, uint32_t lef
     }
 }
 
+// The epilogue of one warp's 32 accumulator rows (TMEM lane quarter q: rows 32q .. 32q + 31 of
+// the 128 x n_tile tile).  32 columns at a time go through the warp's own 32 rows of a staging
+// block in shared memory (`stage`, [128][kStageLd] floats), then the warp writes whole row
+// segments, 4 columns per lane: no barrier beyond the warp, so a warp that gives up on a wait
+// cannot strand the others.
+__device__ __forceinline__ void warp_epilogue(const GemmArgs& g, float* stage, uint32_t tmem, uint32_t q, uint32_t lane,
+                                              uint32_t m0, uint32_t n0, uint32_t n_tile, bool have_acc) {
+    const bool vec = ((reinterpret_cast<uintptr_t>(g.C) & 15u) == 0) && (g.ldc % 4u == 0);
+    float* rows = stage + 32u * q * kStageLd;
+    for (uint32_t c0 = 0; c0 < n_tile; c0 += 32) {
+#pragma unroll
+        for (uint32_t hh = 0; hh < 2; hh++) {
+            const uint32_t cc = c0 + 16u * hh;
+            if (cc >= n_tile) break;  // n_tile is a multiple of 16
+            float v[16];
+            if (have_acc) {
+                umma::tmem_ld16(tmem + ((32u * q) << 16) + cc, v);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 16; j++) v[j] = 0.0f;
+            }
+            if (g.mode == kGemmStoreBF16) {
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const uint32_t n = n0 + cc + j;
+                    float y = v[j] + ((g.bias && n < g.N) ? g.bias[n] : 0.0f);
+                    v[j] = g.relu ? fmaxf(y, 0.0f) : y;
+                }
+            }
+            float4* dst = reinterpret_cast<float4*>(rows + lane * kStageLd + 16u * hh);
+#pragma unroll
+            for (int j = 0; j < 4; j++) dst[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+        }
+        __syncwarp();
+        const uint32_t pieces = (n_tile - c0 < 32u ? n_tile - c0 : 32u) / 4u;  // 4-column pieces per row
+        for (uint32_t idx = lane; idx < 32u * pieces; idx += 32u) {
+            const uint32_t r = idx / pieces, pc = idx - r * pieces;
+            const uint32_t m = m0 + 32u * q + r, n = n0 + c0 + 4u * pc;
+            if (m >= g.M || n >= g.N) continue;
+            const float4 v = *reinterpret_cast<const float4*>(rows + r * kStageLd + 4u * pc);
+            store4(g, (size_t)m * g.ldc + n, g.N - n, v, vec);
+        }
+        __syncwarp();
+    }
+}
+
 template <int BN, bool CONV>
 __global__ void __launch_bounds__(kThreads, 1) umma_gemm_kernel(const GemmArgs g) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -218,50 +266,167 @@ __global__ void __launch_bounds__(kThreads, 1) umma_gemm_kernel(const GemmArgs g
     __syncthreads();
     umma::fence_after_sync();
 
-    if (*s_fail == 0 && (nk > 0 || g.mode != kGemmAtomicF32)) {
-        // 32 columns at a time: each warp moves its 32 accumulator rows through shared memory
-        // (the free operand stages), then the CTA writes whole row segments, 4 columns per thread
-        float* stage = reinterpret_cast<float*>(smem);  // [128][kStageLd]
-        const bool vec = ((reinterpret_cast<uintptr_t>(g.C) & 15u) == 0) && (g.ldc % 4u == 0);
-        for (uint32_t c0 = 0; c0 < n_tile; c0 += 32) {
-#pragma unroll
-            for (uint32_t hh = 0; hh < 2; hh++) {
-                const uint32_t cc = c0 + 16u * hh;
-                if (cc >= n_tile) break;  // n_tile is a multiple of 16
-                float v[16];
-                if (nk > 0) {
-                    umma::tmem_ld16(tmem + ((32u * warp) << 16) + cc, v);
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 16; j++) v[j] = 0.0f;
-                }
-                if (g.mode == kGemmStoreBF16) {
-#pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        const uint32_t n = n0 + cc + j;
-                        float y = v[j] + ((g.bias && n < g.N) ? g.bias[n] : 0.0f);
-                        v[j] = g.relu ? fmaxf(y, 0.0f) : y;
-                    }
-                }
-                float4* dst = reinterpret_cast<float4*>(stage + (32u * warp + lane) * kStageLd + 16u * hh);
-#pragma unroll
-                for (int q = 0; q < 4; q++) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-            }
-            __syncthreads();
-            const uint32_t pieces = (n_tile - c0 < 32u ? n_tile - c0 : 32u) / 4u;  // 4-column pieces per row
-            for (uint32_t idx = tid; idx < kBM * pieces; idx += kThreads) {
-                const uint32_t r = idx / pieces, pc = idx - r * pieces;
-                const uint32_t m = m0 + r, n = n0 + c0 + 4u * pc;
-                if (m >= g.M || n >= g.N) continue;
-                const float4 v = *reinterpret_cast<const float4*>(stage + r * kStageLd + 4u * pc);
-                store4(g, (size_t)m * g.ldc + n, g.N - n, v, vec);
-            }
-            __syncthreads();
-        }
-    }
+    if (*s_fail == 0 && (nk > 0 || g.mode != kGemmAtomicF32))
+        warp_epilogue(g, reinterpret_cast<float*>(smem), tmem, (uint32_t)warp, (uint32_t)lane, m0, n0, n_tile, nk > 0);
     umma::fence_before_sync();
     __syncthreads();
     if (warp == 0) umma::tmem_free(tmem, kCols);
+}
+
+// ---- TMA pipeline ------------------------------------------------------------------------------
+// Warp-specialised: warp 0 (one lane) loads 64-wide K blocks of A and B with cp.async.bulk.tensor
+// into a ring of stages, completing each stage's `full` mbarrier by transaction bytes; warp 1 (one
+// lane) issues the four MMAs of a stage once it is full and commits them to the stage's `empty`
+// mbarrier (which frees it for the next load) and, after the last block, to `acc`; warps 2-5 run
+// the epilogue.  One TMA box per operand and stage: 64 K-elements (128 bytes) x R rows in the
+// 128-byte swizzled K-major layout (umma::smem_desc_sw128).  Rows and K past the matrix are
+// zero-filled by the TMA unit.
+constexpr int kTmaThreads = 192;
+
+template <int BN>
+__host__ __device__ constexpr int tma_stages() { return BN >= 256 ? 4 : (BN >= 128 ? 6 : 4); }  // 64: 2 CTAs per SM
+template <int BN>
+__host__ __device__ constexpr size_t tma_smem() {
+    return 1024 + (size_t)tma_stages<BN>() * (kBM * 128 + BN * 128) + 256;
+}
+
+__device__ __forceinline__ void gemm_fail(int* s_fail, int code) {
+    *reinterpret_cast<volatile int*>(s_fail) = 1;
+    atomicExch(&g_gemm_error, code);
+}
+
+template <int BN>
+__global__ void __launch_bounds__(kTmaThreads, 1)
+    umma_gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                         const GemmArgs g) {
+    constexpr int S = tma_stages<BN>();
+    constexpr uint32_t kA = kBM * 128, kB = BN * 128;  // bytes of one stage's A and B blocks
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned char* smem = smem_raw + ((1024u - (umma::smem_u32(smem_raw) & 1023u)) & 1023u);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * (kA + kB));
+    uint64_t* empty = full + S;
+    uint64_t* acc = empty + S;
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(acc + 1);
+    int* s_fail = reinterpret_cast<int*>(s_tmem + 1);
+    const uint32_t base = umma::smem_u32(smem);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t m0 = blockIdx.y * kBM, n0 = blockIdx.x * BN;
+    const uint32_t k0 = blockIdx.z * g.k_per_split;  // a multiple of 64: blocks never straddle splits
+    const uint32_t k1 = min(g.K, k0 + g.k_per_split);
+    const uint32_t nk = k1 > k0 ? (k1 - k0 + umma::kTileK - 1) / umma::kTileK : 0u;
+    const uint32_t n_rem = g.N - n0;
+    const uint32_t n_tile = ((n_rem < (uint32_t)BN ? n_rem : (uint32_t)BN) + 15u) & ~15u;
+    constexpr uint32_t kCols = BN < 32 ? 32 : BN;
+
+    if (warp == 1) umma::tmem_alloc(s_tmem, kCols);
+    if (tid == 0) {
+        for (int s = 0; s < S; s++) {
+            umma::mbar_init(&full[s], 1);
+            umma::mbar_init(&empty[s], 1);
+        }
+        umma::mbar_init(acc, 1);
+        *s_fail = 0;
+        umma::fence_mbar_init();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *s_tmem;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t issued = 0;
+            for (uint32_t kb = 0; kb < nk; kb++) {
+                const uint32_t st = kb % S, use = kb / S;
+                if (use > 0 && !umma::mbar_wait(&empty[st], (use - 1) & 1u, kWaitLimit)) {
+                    gemm_fail(s_fail, 1 + (int)st);
+                    break;
+                }
+                if (*reinterpret_cast<volatile int*>(s_fail)) break;
+                umma::mbar_arrive_expect_tx(&full[st], kA + kB);
+                const uint32_t a = base + st * (kA + kB), b = a + kA;
+                const int kx = (int)(k0 + kb * umma::kTileK);
+                umma::tma_load_2d(a, &tmA, kx, (int)m0, &full[st]);
+                umma::tma_load_2d(b, &tmB, kx, (int)n0, &full[st]);
+                issued = kb + 1;
+            }
+            if (*reinterpret_cast<volatile int*>(s_fail)) {  // let this thread's copies in flight land
+                for (uint32_t kb = issued > (uint32_t)S ? issued - S : 0u; kb < issued; kb++)
+                    umma::mbar_wait(&full[kb % S], (kb / S) & 1u, kWaitLimit);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = umma::idesc_bf16_f32(kBM, n_tile);
+            for (uint32_t kb = 0; kb < nk; kb++) {
+                const uint32_t st = kb % S;
+                if (!umma::mbar_wait(&full[st], (kb / S) & 1u, kWaitLimit)) {
+                    gemm_fail(s_fail, 1 + S + (int)st);
+                    break;
+                }
+                umma::fence_after_sync();
+                const uint32_t a = base + st * (kA + kB), b = a + kA;
+#pragma unroll
+                for (uint32_t kk = 0; kk < umma::kTileK / 16; kk++)
+                    umma::mma_bf16(tmem, umma::smem_desc_sw128(a + 32u * kk), umma::smem_desc_sw128(b + 32u * kk), idesc,
+                                   (kb | kk) != 0u);
+                umma::mma_commit(&empty[st]);
+            }
+            umma::mma_commit(acc);  // arrives once every MMA issued above has completed
+        }
+    } else {
+        const bool ok = umma::mbar_wait(acc, 0u, kWaitLimit);
+        if (!ok) gemm_fail(s_fail, 1 + 2 * S);
+        umma::fence_after_sync();
+        if (ok && !*reinterpret_cast<volatile int*>(s_fail) && (nk > 0 || g.mode != kGemmAtomicF32))
+            warp_epilogue(g, reinterpret_cast<float*>(smem), tmem, (uint32_t)warp & 3u, (uint32_t)lane, m0, n0, n_tile,
+                          nk > 0);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 1) umma::tmem_free(tmem, kCols);
+}
+
+// cuTensorMapEncodeTiled from the driver (no link-time dependency on libcuda); null when absent
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// a [rows x inner] bf16 matrix with row stride ld (elements), read in 128-byte swizzled boxes of
+// 64 x box_rows
+bool encode_operand(CUtensorMap* m, const __nv_bfloat16* p, uint32_t inner, uint32_t rows, uint32_t ld,
+                    uint32_t box_rows) {
+    const cuuint64_t dims[2] = {inner, rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2u};
+    const cuuint32_t box[2] = {umma::kTileK, box_rows};
+    const cuuint32_t estr[2] = {1u, 1u};
+    return tensor_map_encoder()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(p), dims, strides,
+                                box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// false (nothing launched) when a tensor map cannot be encoded for these operands
+template <int BN>
+bool launch_tma_bn(const GemmArgs& g, uint32_t splits, cudaStream_t st, cudaError_t* err) {
+    CUtensorMap ta, tb;
+    if (!encode_operand(&ta, g.A, g.K, g.M, g.lda, kBM) || !encode_operand(&tb, g.B, g.K, g.N, g.ldb, BN)) return false;
+    const size_t smem = tma_smem<BN>();
+    *err = cudaFuncSetAttribute(umma_gemm_tma_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (*err != cudaSuccess) return true;
+    const dim3 grid((g.N + BN - 1) / BN, (g.M + kBM - 1) / kBM, splits);
+    umma_gemm_tma_kernel<BN><<<grid, kTmaThreads, smem, st>>>(ta, tb, g);
+    *err = cudaGetLastError();
+    return true;
 }
 
 template <int BN, bool CONV = false>
@@ -286,6 +451,13 @@ cudaError_t launch_gemm(GemmArgs g, uint32_t splits, cudaStream_t st) {
     const uint32_t per = (kblocks + splits - 1) / splits;
     g.k_per_split = per * umma::kTileK;
     if (splits > 1 && g.mode != kGemmAtomicF32) return cudaErrorInvalidValue;
+    if (tensor_map_encoder() && g.K > 0 && g.M < (1u << 31) && g.K < (1u << 31)) {  // TMA pipeline
+        cudaError_t e = cudaSuccess;
+        const bool launched = g.N <= 64    ? launch_tma_bn<64>(g, splits, st, &e)
+                              : g.N <= 128 ? launch_tma_bn<128>(g, splits, st, &e)
+                                           : launch_tma_bn<256>(g, splits, st, &e);
+        if (launched) return e;
+    }
     if (g.N <= 64) return launch_bn<64>(g, splits, st);
     if (g.N <= 128) return launch_bn<128>(g, splits, st);
     return launch_bn<256>(g, splits, st);

@@ -33,6 +33,17 @@ __host__ __device__ constexpr uint64_t smem_desc(uint32_t saddr, uint32_t lbo, u
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
+// The same descriptor for a K-major tile in the 128-byte swizzled layout that a TMA load with
+// CU_TENSOR_MAP_SWIZZLE_128B writes: rows of 64 bf16 (128 bytes), 16-byte chunk j of row r
+// stored at chunk j ^ (r % 8), 8-row groups 1024 bytes apart (SBO); the leading offset is unused;
+// layout type 2 (128-byte swizzle) in bits 61-63.  The tile must start 1024-byte aligned; the
+// k-th 16-element step of a 64-wide block starts 32 * k bytes in (the swizzle is applied to the
+// computed addresses).
+__host__ __device__ constexpr uint64_t smem_desc_sw128(uint32_t saddr) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | (1ull << 16) | ((uint64_t)(1024u >> 4) << 32) | (1ull << 46) |
+           (2ull << 61);
+}
+
 // Instruction descriptor of kind::f16 (32 bit): D format F32 (bits 4-5 = 1), A and B BF16 (bits
 // 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22, M >> 4 in bits 24-28.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t m, uint32_t n) {
