@@ -99,7 +99,9 @@ def _conv_ref(xa, xb, wt, up, absolute=False):
 
 @pytest.mark.parametrize("n,h,w,ca,cb,N,up", [(2, 16, 24, 8, 0, 32, False), (1, 37, 53, 48, 0, 48, False),
                                               (2, 32, 48, 64, 48, 48, True), (1, 20, 20, 96, 64, 64, True),
-                                              (3, 9, 130, 32, 0, 96, False), (1, 40, 24, 16, 8, 200, False)])
+                                              (3, 9, 130, 32, 0, 96, False), (1, 40, 24, 16, 8, 200, False),
+                                              (1, 12, 20, 16, 0, 16, False), (2, 16, 300, 32, 32, 48, True),
+                                              (1, 8, 8, 96, 96, 96, False)])
 def test_conv3x3_store_f32(rk, n, h, w, ca, cb, N, up):
     xa, xb, wt = _conv_ops(n, h, w, ca, cb, N, up, n * 1000 + h * 10 + N)
     c = torch.full((n * h * w, N), float("nan"), device="cuda")
