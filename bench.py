@@ -229,7 +229,7 @@ def run_reference(args):
     line = {"metric": "Gpoints/s histogrammed", "value": v, "unit": "Gpoints/s", "impl": "reference",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": points / (v * 1e9) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic genome (seed 1), no dataset",
+            "data": "synthetic genome (seed %d); no dataset" % (GENOME["seed"] if GENOME else 2),
             "config": {"workload": CONFIG_NAME, "points_per_frame": points, "bins": [W, H], "genome": GENOME},
             "cpu_baseline": {"value": v, "unit": "Gpoints/s", "cores": last[0], "kind": "port", "sample": last[1]},
             "e2e": {"value": v, "unit": "Gpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -376,7 +376,7 @@ def run_native(args):
     line = {
         "metric": "Gpoints/s histogrammed", "value": value, "unit": "Gpoints/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic genome (seed 1); no dataset",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic genome (seed %d); no dataset" % GENOME["seed"],
         "config": {"workload": CONFIG_NAME, "points_per_frame": POINTS, "bins": [W, H], "output": [W_OUT, H_OUT],
                    "genome": GENOME, "walkers": walkers, "cta_slots": cta, "steps_per_launch": args.steps_per_launch,
                    "passes_per_frame": passes, "fuse_passes": FUSE, "splat": args.splat,
