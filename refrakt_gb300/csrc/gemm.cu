@@ -12,6 +12,8 @@
 // one of: FP32 store, bias + ReLU + BF16 store, FP32 atomic add.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+
+#include <algorithm>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -274,58 +276,84 @@ __global__ void __launch_bounds__(kThreads, 1) umma_gemm_kernel(const GemmArgs g
 }
 
 // ---- TMA pipeline ------------------------------------------------------------------------------
-// Warp-specialised: warp 0 (one lane) loads 64-wide K blocks of A and B with cp.async.bulk.tensor
-// into a ring of stages, completing each stage's `full` mbarrier by transaction bytes; warp 1 (one
-// lane) issues the four MMAs of a stage once it is full and commits them to the stage's `empty`
-// mbarrier (which frees it for the next load) and, after the last block, to `acc`; warps 2-5 run
-// the epilogue.  One TMA box per operand and stage: 64 K-elements (128 bytes) x R rows in the
-// 128-byte swizzled K-major layout (umma::smem_desc_sw128).  Rows and K past the matrix are
-// zero-filled by the TMA unit.
+// Persistent and warp-specialised.  Each CTA walks its share of the output tiles (grouped: 8
+// row tiles side by side, so co-resident CTAs share A rows and B columns in L2).  Warp 0 (one lane)
+// loads 64-wide K blocks of A and B with cp.async.bulk.tensor into a ring of stages that runs on
+// across tiles, completing each stage's `full` mbarrier by transaction bytes; warp 1 (one lane)
+// issues the four MMAs of a full stage and commits them to the stage's `empty` mbarrier (which
+// frees it for the next load).  Two tensor-memory accumulators alternate between tiles: the MMA
+// lane commits a finished tile to `acc_full[b]`, warps 2-5 drain it (each its TMEM lane quarter,
+// through its own rows of a staging block) and release it on `acc_empty[b]`, so a tile's epilogue
+// overlaps the next tile's loads and MMAs.  One TMA box per operand and stage: 64 K-elements
+// (128 bytes) x R rows in the 128-byte swizzled K-major layout (umma::smem_desc_sw128); rows and K
+// past the matrix are zero-filled by the TMA unit.
 constexpr int kTmaThreads = 192;
+constexpr uint32_t kGroupM = 8;  // row tiles per raster group
 
 template <int BN>
-__host__ __device__ constexpr int tma_stages() { return BN >= 256 ? 4 : (BN >= 128 ? 6 : 4); }  // 64: 2 CTAs per SM
+__host__ __device__ constexpr int tma_stages() { return BN >= 256 ? 4 : (BN >= 128 ? 6 : 8); }  // one CTA per SM
 template <int BN>
 __host__ __device__ constexpr size_t tma_smem() {
-    return 1024 + (size_t)tma_stages<BN>() * (kBM * 128 + BN * 128) + 256;
+    return 1024 + (size_t)tma_stages<BN>() * (kBM * 128 + BN * 128) + (size_t)kBM * kStageLd * 4 + 256;
 }
 
 __device__ __forceinline__ void gemm_fail(int* s_fail, int code) {
     *reinterpret_cast<volatile int*>(s_fail) = 1;
     atomicExch(&g_gemm_error, code);
 }
+__device__ __forceinline__ bool gemm_failed(const int* s_fail) { return *reinterpret_cast<const volatile int*>(s_fail) != 0; }
+
+// tile t of the grid (split-major; within a split, groups of kGroupM row tiles with the row tile
+// fastest) -> its origin and K range
+struct TileCoord {
+    uint32_t m0, n0, k0, nk;
+};
+__device__ __forceinline__ TileCoord tile_coord(const GemmArgs& g, uint32_t t, uint32_t tiles_m, uint32_t tiles_n,
+                                                uint32_t bn) {
+    const uint32_t per_split = tiles_m * tiles_n, split = t / per_split, r = t - split * per_split;
+    const uint32_t group = r / (kGroupM * tiles_n), first = group * kGroupM;
+    const uint32_t gm = min(kGroupM, tiles_m - first), within = r - group * kGroupM * tiles_n;
+    TileCoord c;
+    c.m0 = (first + within % gm) * kBM;
+    c.n0 = (within / gm) * bn;
+    c.k0 = split * g.k_per_split;  // a multiple of 64: blocks never straddle splits
+    const uint32_t k1 = min(g.K, c.k0 + g.k_per_split);
+    c.nk = k1 > c.k0 ? (k1 - c.k0 + umma::kTileK - 1) / umma::kTileK : 0u;
+    return c;
+}
 
 template <int BN>
 __global__ void __launch_bounds__(kTmaThreads, 1)
     umma_gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                         const GemmArgs g) {
+                         const GemmArgs g, uint32_t splits) {
     constexpr int S = tma_stages<BN>();
     constexpr uint32_t kA = kBM * 128, kB = BN * 128;  // bytes of one stage's A and B blocks
+    constexpr uint32_t kCols = BN < 32 ? 32 : BN;      // one accumulator; two are allocated
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned char* smem = smem_raw + ((1024u - (umma::smem_u32(smem_raw) & 1023u)) & 1023u);
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * (kA + kB));
+    float* stage_out = reinterpret_cast<float*>(smem + S * (kA + kB));
+    uint64_t* full = reinterpret_cast<uint64_t*>(stage_out + kBM * kStageLd);
     uint64_t* empty = full + S;
-    uint64_t* acc = empty + S;
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(acc + 1);
+    uint64_t* acc_full = empty + S;
+    uint64_t* acc_empty = acc_full + 2;
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(acc_empty + 2);
     int* s_fail = reinterpret_cast<int*>(s_tmem + 1);
     const uint32_t base = umma::smem_u32(smem);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t m0 = blockIdx.y * kBM, n0 = blockIdx.x * BN;
-    const uint32_t k0 = blockIdx.z * g.k_per_split;  // a multiple of 64: blocks never straddle splits
-    const uint32_t k1 = min(g.K, k0 + g.k_per_split);
-    const uint32_t nk = k1 > k0 ? (k1 - k0 + umma::kTileK - 1) / umma::kTileK : 0u;
-    const uint32_t n_rem = g.N - n0;
-    const uint32_t n_tile = ((n_rem < (uint32_t)BN ? n_rem : (uint32_t)BN) + 15u) & ~15u;
-    constexpr uint32_t kCols = BN < 32 ? 32 : BN;
+    const uint32_t tiles_m = (g.M + kBM - 1) / kBM, tiles_n = (g.N + BN - 1) / BN;
+    const uint32_t tiles = tiles_m * tiles_n * splits;
 
-    if (warp == 1) umma::tmem_alloc(s_tmem, kCols);
+    if (warp == 1) umma::tmem_alloc(s_tmem, 2 * kCols);
     if (tid == 0) {
         for (int s = 0; s < S; s++) {
             umma::mbar_init(&full[s], 1);
             umma::mbar_init(&empty[s], 1);
         }
-        umma::mbar_init(acc, 1);
+        for (int b = 0; b < 2; b++) {
+            umma::mbar_init(&acc_full[b], 1);
+            umma::mbar_init(&acc_empty[b], 4);  // one arrival per epilogue warp
+        }
         *s_fail = 0;
         umma::fence_mbar_init();
     }
@@ -336,56 +364,87 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
 
     if (warp == 0) {
         if (lane == 0) {
-            uint32_t issued = 0;
-            for (uint32_t kb = 0; kb < nk; kb++) {
-                const uint32_t st = kb % S, use = kb / S;
-                if (use > 0 && !umma::mbar_wait(&empty[st], (use - 1) & 1u, kWaitLimit)) {
-                    gemm_fail(s_fail, 1 + (int)st);
-                    break;
+            uint32_t it = 0;  // K blocks issued by this CTA
+            for (uint32_t t = blockIdx.x; t < tiles && !gemm_failed(s_fail); t += gridDim.x) {
+                const TileCoord c = tile_coord(g, t, tiles_m, tiles_n, BN);
+                for (uint32_t kb = 0; kb < c.nk; kb++, it++) {
+                    const uint32_t st = it % S, use = it / S;
+                    if (use > 0 && !umma::mbar_wait(&empty[st], (use - 1) & 1u, kWaitLimit)) {
+                        gemm_fail(s_fail, 1 + (int)st);
+                        break;
+                    }
+                    if (gemm_failed(s_fail)) break;
+                    umma::mbar_arrive_expect_tx(&full[st], kA + kB);
+                    const uint32_t a = base + st * (kA + kB), b = a + kA;
+                    const int kx = (int)(c.k0 + kb * umma::kTileK);
+                    umma::tma_load_2d(a, &tmA, kx, (int)c.m0, &full[st]);
+                    umma::tma_load_2d(b, &tmB, kx, (int)c.n0, &full[st]);
                 }
-                if (*reinterpret_cast<volatile int*>(s_fail)) break;
-                umma::mbar_arrive_expect_tx(&full[st], kA + kB);
-                const uint32_t a = base + st * (kA + kB), b = a + kA;
-                const int kx = (int)(k0 + kb * umma::kTileK);
-                umma::tma_load_2d(a, &tmA, kx, (int)m0, &full[st]);
-                umma::tma_load_2d(b, &tmB, kx, (int)n0, &full[st]);
-                issued = kb + 1;
             }
-            if (*reinterpret_cast<volatile int*>(s_fail)) {  // let this thread's copies in flight land
-                for (uint32_t kb = issued > (uint32_t)S ? issued - S : 0u; kb < issued; kb++)
-                    umma::mbar_wait(&full[kb % S], (kb / S) & 1u, kWaitLimit);
+            if (gemm_failed(s_fail)) {  // let this thread's copies in flight land
+                for (uint32_t k = it > (uint32_t)S ? it - S : 0u; k < it; k++)
+                    umma::mbar_wait(&full[k % S], (k / S) & 1u, kWaitLimit);
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            const uint32_t idesc = umma::idesc_bf16_f32(kBM, n_tile);
-            for (uint32_t kb = 0; kb < nk; kb++) {
-                const uint32_t st = kb % S;
-                if (!umma::mbar_wait(&full[st], (kb / S) & 1u, kWaitLimit)) {
-                    gemm_fail(s_fail, 1 + S + (int)st);
-                    break;
+            uint32_t it = 0, i = 0;  // K blocks consumed, tiles done by this CTA
+            for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x, i++) {
+                const TileCoord c = tile_coord(g, t, tiles_m, tiles_n, BN);
+                const uint32_t buf = i & 1u, u = i >> 1;
+                const uint32_t n_rem = g.N - c.n0;
+                const uint32_t n_tile = ((n_rem < (uint32_t)BN ? n_rem : (uint32_t)BN) + 15u) & ~15u;
+                const uint32_t idesc = umma::idesc_bf16_f32(kBM, n_tile);
+                bool ok = !gemm_failed(s_fail);
+                if (ok && u > 0 && !umma::mbar_wait(&acc_empty[buf], (u - 1) & 1u, kWaitLimit)) {
+                    gemm_fail(s_fail, 1 + 2 * S + (int)buf);
+                    ok = false;
                 }
                 umma::fence_after_sync();
-                const uint32_t a = base + st * (kA + kB), b = a + kA;
+                for (uint32_t kb = 0; ok && kb < c.nk; kb++, it++) {
+                    const uint32_t st = it % S;
+                    if (!umma::mbar_wait(&full[st], (it / S) & 1u, kWaitLimit)) {
+                        gemm_fail(s_fail, 1 + S + (int)st);
+                        ok = false;
+                        break;
+                    }
+                    umma::fence_after_sync();
+                    const uint32_t a = base + st * (kA + kB), b = a + kA;
 #pragma unroll
-                for (uint32_t kk = 0; kk < umma::kTileK / 16; kk++)
-                    umma::mma_bf16(tmem, umma::smem_desc_sw128(a + 32u * kk), umma::smem_desc_sw128(b + 32u * kk), idesc,
-                                   (kb | kk) != 0u);
-                umma::mma_commit(&empty[st]);
+                    for (uint32_t kk = 0; kk < umma::kTileK / 16; kk++)
+                        umma::mma_bf16(tmem + buf * kCols, umma::smem_desc_sw128(a + 32u * kk),
+                                       umma::smem_desc_sw128(b + 32u * kk), idesc, (kb | kk) != 0u);
+                    umma::mma_commit(&empty[st]);
+                }
+                umma::mma_commit(&acc_full[buf]);  // arrives once every MMA issued above has completed
+                if (!ok) break;
             }
-            umma::mma_commit(acc);  // arrives once every MMA issued above has completed
         }
     } else {
-        const bool ok = umma::mbar_wait(acc, 0u, kWaitLimit);
-        if (!ok) gemm_fail(s_fail, 1 + 2 * S);
-        umma::fence_after_sync();
-        if (ok && !*reinterpret_cast<volatile int*>(s_fail) && (nk > 0 || g.mode != kGemmAtomicF32))
-            warp_epilogue(g, reinterpret_cast<float*>(smem), tmem, (uint32_t)warp & 3u, (uint32_t)lane, m0, n0, n_tile,
-                          nk > 0);
+        const uint32_t q = (uint32_t)warp & 3u;  // TMEM lane quarter of this warp
+        float* rows = stage_out;
+        uint32_t i = 0;
+        for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x, i++) {
+            const TileCoord c = tile_coord(g, t, tiles_m, tiles_n, BN);
+            const uint32_t buf = i & 1u, u = i >> 1;
+            if (!umma::mbar_wait(&acc_full[buf], u & 1u, kWaitLimit)) {
+                gemm_fail(s_fail, 3 + 2 * S + (int)buf);
+                break;
+            }
+            umma::fence_after_sync();
+            if (gemm_failed(s_fail)) break;
+            const uint32_t n_rem = g.N - c.n0;
+            const uint32_t n_tile = ((n_rem < (uint32_t)BN ? n_rem : (uint32_t)BN) + 15u) & ~15u;
+            if (c.nk > 0 || g.mode != kGemmAtomicF32)
+                warp_epilogue(g, rows, tmem + buf * kCols, q, (uint32_t)lane, c.m0, c.n0, n_tile, c.nk > 0);
+            umma::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) umma::mbar_arrive(&acc_empty[buf]);
+        }
     }
     umma::fence_before_sync();
     __syncthreads();
-    if (warp == 1) umma::tmem_free(tmem, kCols);
+    if (warp == 1) umma::tmem_free(tmem, 2 * kCols);
 }
 
 // cuTensorMapEncodeTiled from the driver (no link-time dependency on libcuda); null when absent
@@ -423,8 +482,24 @@ bool launch_tma_bn(const GemmArgs& g, uint32_t splits, cudaStream_t st, cudaErro
     const size_t smem = tma_smem<BN>();
     *err = cudaFuncSetAttribute(umma_gemm_tma_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (*err != cudaSuccess) return true;
-    const dim3 grid((g.N + BN - 1) / BN, (g.M + kBM - 1) / kBM, splits);
-    umma_gemm_tma_kernel<BN><<<grid, kTmaThreads, smem, st>>>(ta, tb, g);
+    // persistent: as many CTAs as fit at once, each walking tiles t = blockIdx.x + i * gridDim.x
+    // (resident CTAs per SM depend on the kernel alone: asked once)
+    static const int per_sm = [smem] {
+        int n = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, umma_gemm_tma_kernel<BN>, kTmaThreads, smem) ==
+                       cudaSuccess
+                   ? n
+                   : 1;
+    }();
+    int dev = 0, sms = 0;
+    if ((*err = cudaGetDevice(&dev)) != cudaSuccess) return true;
+    if ((*err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return true;
+    // fewer than two rounds of tiles: one CTA per tile, so a second-round tile goes to whichever SM
+    // frees first rather than to a fixed CTA
+    const uint64_t tiles = (uint64_t)((g.M + kBM - 1) / kBM) * ((g.N + BN - 1) / BN) * splits;
+    const uint64_t resident = (uint64_t)std::max(1, sms * std::max(1, per_sm));
+    const uint32_t grid = (uint32_t)(tiles < 2 * resident ? tiles : resident);
+    umma_gemm_tma_kernel<BN><<<grid, kTmaThreads, smem, st>>>(ta, tb, g, splits);
     *err = cudaGetLastError();
     return true;
 }
