@@ -167,11 +167,11 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _profile_figure(workload, key):
+def _profile_figure(workload, key, summary="chaos_kernel_%s.md"):
     """A figure ("<key>: <number>") from the committed ncu summary of this workload (or None)."""
     import re
     try:
-        with open(os.path.join(ROOT, "profiles", "chaos_kernel_%s.md" % workload)) as f:
+        with open(os.path.join(ROOT, "profiles", summary % workload)) as f:
             m = re.search(r"^%s: ([0-9.]+)" % re.escape(key), f.read(), re.M)
         return float(m.group(1)) if m else None
     except OSError:
@@ -578,7 +578,8 @@ def run_gemm(args):
         "vs_baseline": None, "dtype": "bf16", "data": "random normal operands",
         "config": {"workload": CONFIG_NAME}, "shapes": res,
         "roofline": {"bound": "tensor", "achieved": v, "peak": peak, "unit": "TFLOP/s", "frac": v / peak,
-                     "traffic": None, "peak_source": src},
+                     "traffic": _profile_figure("tcgen05", "dram bytes per launch", "gemm_%s.md"), "peak_source": src,
+                     "kernel": "umma_gemm_tma_kernel<256>", "shape": "8192^3"},
         "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
     return 0
 
