@@ -144,3 +144,36 @@ def test_conv3x3_bad_arguments_rejected(rk):
         rk.conv3x3_bf16(xa, wt, torch.zeros(64, 8, device="cuda"))  # output rows narrower than N
     with pytest.raises(ValueError):
         rk.conv3x3_bf16(xa, wt[:, :96], c)  # weights narrower than 9 (ca + cb)
+
+
+# ---- the persistent TMA pipeline: shapes with more than two rounds of tiles (152 SMs, one CTA
+# each), so every CTA walks several tiles and both tensor-memory accumulators alternate
+
+@pytest.mark.parametrize("M,N,K", [(16384, 768, 192), (65536, 48, 72), (40000, 100, 136)])
+def test_persistent_many_tiles(rk, M, N, K):
+    a, b = _ops(M, N, K, M + N + K)
+    c = torch.full((M, N), float("nan"), device="cuda")
+    rk.gemm_bf16(a, b, c)
+    ref = _ref(a, b)
+    tol = 1e-5 * (a.float().abs() @ b.float().abs().t()) + 1e-6
+    assert torch.all((c - ref).abs() <= tol), float((c - ref).abs().max())
+
+
+def test_persistent_split_k_many_tiles(rk):
+    M, N, K, splits = 96, 2048, 65536, 64  # 8 column tiles x 64 splits = 512 tiles
+    a, b = _ops(M, N, K, 9)
+    c = torch.ones(M, N, device="cuda")
+    rk.gemm_bf16(a, b, c, mode=rk.GEMM_ATOMIC_F32, splits=splits)
+    ref = 1.0 + _ref(a, b)
+    tol = 1e-5 * (a.float().abs() @ b.float().abs().t()) + 1e-4
+    assert torch.all((c - ref).abs() <= tol), float((c - ref).abs().max())
+
+
+def test_persistent_bias_relu_bf16(rk):
+    M, N, K = 50000, 96, 200
+    a, b = _ops(M, N, K, 13)
+    bias = torch.randn(N, device="cuda")
+    c = torch.zeros(M, N, device="cuda", dtype=torch.bfloat16)
+    rk.gemm_bf16(a, b, c, mode=rk.GEMM_STORE_BF16, bias=bias, relu=True)
+    ref = (_ref(a, b) + bias).clamp_min(0)
+    assert torch.allclose(c.float(), ref, rtol=2 ** -8, atol=1e-3)
