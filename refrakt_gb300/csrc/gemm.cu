@@ -3,13 +3,20 @@
 //
 //   C[M x N] (+)= A[M x K] * B[N x K]^T      A, B bf16, K contiguous (K-major), K % 8 == 0
 //
-// One CTA of 128 threads computes a 128 x BN tile over a range of K (split-K along grid.z).
-// Operand tiles of 64 K-elements are staged in shared memory by cp.async in the K-major
-// no-swizzle core-matrix layout (umma.cuh) through a 3-stage ring; thread 0 issues four
-// M128 x N x K16 MMAs per stage and commits them to the stage's mbarrier, which releases the
-// stage for refilling.  The epilogue reads the accumulator with tcgen05.ld (warp w owns rows
-// 32w..32w+31), stages 32 columns at a time in shared memory and writes whole row segments with
-// one of: FP32 store, bias + ReLU + BF16 store, FP32 atomic add.
+// Two pipelines share the MMA issue and the epilogue:
+//  * plain matrices (launch_gemm): the persistent, warp-specialised TMA kernel
+//    (umma_gemm_tma_kernel, "TMA pipeline" below) — 128-byte swizzled boxes, an mbarrier ring,
+//    two tensor-memory accumulators; the cp.async kernel below only stands in when the driver
+//    offers no tensor-map encoder;
+//  * implicit 3x3 convolution (launch_gemm_conv): the cp.async kernel in conv mode, whose 128
+//    threads gather each 128 x 64 block of im2col rows from the NHWC inputs.
+// The cp.async kernel: one CTA of 128 threads computes a 128 x BN tile over a range of K
+// (split-K along grid.z); operand tiles of 64 K-elements are staged in the K-major no-swizzle
+// core-matrix layout (umma.cuh) through a 3-stage ring; thread 0 issues four M128 x N x K16 MMAs
+// per stage and commits them to the stage's mbarrier, which releases the stage for refilling.
+// Epilogue (both): each warp reads its 32 accumulator rows with tcgen05.ld, stages 32 columns at a
+// time in shared memory and writes whole row segments with one of: FP32 store, bias + ReLU + BF16
+// store, FP32 atomic add.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
