@@ -93,6 +93,7 @@ struct rf_batch {
     unsigned long long* counters = nullptr;
     uint32_t max_prog_words = 0;
     double* stats = nullptr;  // per item 3 doubles
+    unsigned char* pool = nullptr;  // every item's buffers (rf_batch_create)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -107,11 +108,7 @@ void destroy_batch(rf_batch* b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
-    for (auto& it : b->items) {
-        void* ptrs[] = {it.bins, it.hits, it.de, it.img, it.img_f32, it.palette, it.dprog, it.rad, it.dw};
-        for (void* p : ptrs) if (p) cudaFree(p);
-    }
-    void* ptrs[] = {b->table, b->dinst, b->dunits, b->queue, b->counters, b->stats};
+    void* ptrs[] = {b->pool, b->table, b->dinst, b->dunits, b->queue, b->counters, b->stats};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
@@ -304,11 +301,26 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
     if (cudaSetDevice(b->device) != cudaSuccess) return bail(fail(RF_ERR_NO_DEVICE, "rf_batch_create: no such device"));
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(cuda_err(e, "stream"));
+    // Every item's device buffers are carved from one allocation: its small constants (palette,
+    // program, DE kernel weights) packed at the start and uploaded with one copy, then the bin
+    // planes, DE buffers and images, each 256-byte aligned.
+    struct Offsets {
+        size_t pal, prog, dw, bins, hits, de, rad, img, img_f32;
+    };
+    constexpr size_t kNone = ~(size_t)0;
+    std::vector<Offsets> off(n);
+    std::vector<uint8_t> consts;
+    const auto put = [&](const void* src, size_t bytes) {
+        const size_t o = consts.size();
+        consts.resize(o + ((bytes + 255) & ~(size_t)255), 0);
+        memcpy(consts.data() + o, src, bytes);
+        return o;
+    };
     b->items.reserve(n);
     for (uint32_t i = 0; i < n; i++) {
         const rf_flame* f = items[i].flame;
         b->items.emplace_back();
-        Item& it = b->items.back();  // owned by the batch from here on, so a failure below frees it
+        Item& it = b->items.back();
         it.desc = items[i];
         it.ss = items[i].supersample ? items[i].supersample : 1;
         it.W = items[i].width * it.ss;
@@ -316,27 +328,49 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
         if (int rc = genome_program(f->g, *f->reg, it.prog)) return bail(rc);
         it.est_radius = f->g.est_radius; it.est_min = f->g.est_min; it.est_curve = f->g.est_curve;
         it.gamma = f->g.gamma; it.brightness = f->g.brightness; it.vibrancy = f->g.vibrancy;
-        const size_t nb = (size_t)it.W * it.H;
-        e = cudaMalloc((void**)&it.bins, nb * sizeof(float4));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&it.hits, nb * sizeof(uint32_t));
-        if (e == cudaSuccess && d->density_estimation && (it.est_radius > 0 || it.est_min > 0)) {
+        off[i].pal = put(f->g.palette, 256 * sizeof(float4));
+        off[i].prog = put(it.prog.data(), it.prog.size() * 4);
+        off[i].dw = kNone;
+        if (d->density_estimation && (it.est_radius > 0 || it.est_min > 0)) {
             std::vector<float> wts;
             density_weights(std::min(100, it.est_radius), std::min(100, it.est_min), wts);
-            e = cudaMalloc((void**)&it.de, nb * sizeof(float4));
-            if (e == cudaSuccess) e = cudaMalloc((void**)&it.rad, nb);
-            if (e == cudaSuccess) e = cudaMalloc((void**)&it.dw, wts.size() * sizeof(float));
-            if (e == cudaSuccess) e = cudaMemcpy(it.dw, wts.data(), wts.size() * sizeof(float), cudaMemcpyHostToDevice);
+            off[i].dw = put(wts.data(), wts.size() * sizeof(float));
         }
-        if (e == cudaSuccess) e = cudaMalloc((void**)&it.img, (size_t)items[i].width * items[i].height * sizeof(uchar4));
-        if (e == cudaSuccess && d->image_f32)
-            e = cudaMalloc((void**)&it.img_f32, (size_t)items[i].width * items[i].height * sizeof(float4));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&it.palette, 256 * sizeof(float4));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&it.dprog, it.prog.size() * 4);
-        if (e == cudaSuccess) e = cudaMemcpy(it.palette, f->g.palette, 256 * sizeof(float4), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMemcpy(it.dprog, it.prog.data(), it.prog.size() * 4, cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) return bail(cuda_err(e, "rf_batch_create allocation"));
         b->max_prog_words = std::max(b->max_prog_words, (uint32_t)it.prog.size());
         b->points += items[i].points;
+    }
+    size_t pool = consts.size();
+    const auto take = [&](size_t bytes) {
+        const size_t o = pool;
+        pool += (bytes + 255) & ~(size_t)255;
+        return o;
+    };
+    for (uint32_t i = 0; i < n; i++) {
+        const Item& it = b->items[i];
+        const size_t nb = (size_t)it.W * it.H, np = (size_t)items[i].width * items[i].height;
+        off[i].bins = take(nb * sizeof(float4));
+        off[i].hits = take(nb * sizeof(uint32_t));
+        off[i].de = off[i].dw != kNone ? take(nb * sizeof(float4)) : kNone;
+        off[i].rad = off[i].dw != kNone ? take(nb) : kNone;
+        off[i].img = take(np * sizeof(uchar4));
+        off[i].img_f32 = d->image_f32 ? take(np * sizeof(float4)) : kNone;
+    }
+    e = cudaMalloc((void**)&b->pool, pool);
+    if (e == cudaSuccess) e = cudaMemcpy(b->pool, consts.data(), consts.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return bail(cuda_err(e, "rf_batch_create allocation"));
+    for (uint32_t i = 0; i < n; i++) {
+        Item& it = b->items[i];
+        unsigned char* base = b->pool;
+        const auto at = [&](size_t o) -> void* { return o == kNone ? nullptr : base + o; };
+        it.palette = static_cast<float4*>(at(off[i].pal));
+        it.dprog = static_cast<uint32_t*>(at(off[i].prog));
+        it.dw = static_cast<float*>(at(off[i].dw));
+        it.bins = static_cast<float4*>(at(off[i].bins));
+        it.hits = static_cast<uint32_t*>(at(off[i].hits));
+        it.de = static_cast<float4*>(at(off[i].de));
+        it.rad = static_cast<uint8_t*>(at(off[i].rad));
+        it.img = static_cast<uchar4*>(at(off[i].img));
+        it.img_f32 = static_cast<float4*>(at(off[i].img_f32));
     }
     e = cudaMalloc((void**)&b->queue, ((size_t)n + 1) * sizeof(unsigned int));  // a counter per group (<= items)
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->counters, 3 * sizeof(unsigned long long));
