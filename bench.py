@@ -186,7 +186,8 @@ def _traffic(workload):
 
 def cpu_baseline(genome_xml, seconds=12.0, threads=None):
     """The oracle's FP32 transcription of flame.glsl's draw pass on the host cores, on a bounded
-    sample of this workload (same genome, same bin grid): returns (Gpoints/s, threads, sample)."""
+    sample of this workload (same genome, same bin grid): returns (Gpoints/s, threads, sample
+    description, seconds timed)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
