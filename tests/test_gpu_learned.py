@@ -40,11 +40,3 @@ def test_fallback_policy(rk, compiler, bound, expect_fallback):
     out, est, fb = LD.LearnedRenderer(net, spp=16, bound=bound).render(f, S, S, seed=9)
     assert fb == expect_fallback
     assert est >= 0.0 and out.shape == (S, S, 3) and torch.isfinite(out).all()
-
-
-def test_plain_equivalent_spp():
-    from refrakt_gb300 import learned as LD
-    spps = [16, 64, 256, 1024]
-    errs = [0.16, 0.08, 0.04, 0.02]  # error halves per 4x samples
-    assert abs(LD.plain_equivalent_spp(spps, errs, 0.04) - 256) < 1e-6
-    assert abs(LD.plain_equivalent_spp(spps, errs, 0.0565685) - 128) < 0.1
