@@ -44,6 +44,13 @@ using namespace rfk;
 
 namespace {
 
+// rf_sim's splat setting as ChaosArgs.splat's code: 0 global, 1 warp-aggregated, 2 adaptive
+int splat_code(int splat) { return splat == RF_SPLAT_WARP ? 1 : (splat == RF_SPLAT_GLOBAL ? 0 : 2); }
+
+}  // namespace
+
+namespace {
+
 constexpr size_t kInterleaveMinBytes = 256ull << 20;  // bins + counts above ~2x L2: interleave
 
 int set_device(const rf_sim* s) {
@@ -83,7 +90,7 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.seed = s->d.seed;
         a.first_run = (first_run && done == 0) ? 1 : 0;
         a.draw = draw ? 1 : 0;
-        a.splat = s->splat == RF_SPLAT_WARP ? 1 : (s->splat == RF_SPLAT_GLOBAL ? 0 : 2);
+        a.splat = splat_code(s->splat);
         a.rgba_shift = s->rgba_shift;
         a.count_shift = s->count_shift;
         if (ss) memcpy(a.ss, ss, sizeof(a.ss));
@@ -97,6 +104,14 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.trace_passes = s->trace_passes;
         a.n_groups = (uint32_t)(s->N / kGroup);
         const uint32_t grid = (uint32_t)(s->N / s->slots);
+        if (s->spec && s->spec_splat != a.splat) {  // the strategy changed since warmup: its own kernel
+            const void* k = nullptr;
+            if (int rc = spec_kernel(s->spec_prog, (int)s->threads, (int)s->slots, s->device, &k, SpecKind::Chaos,
+                                     a.splat))
+                return rc;
+            s->spec = k;
+            s->spec_splat = a.splat;
+        }
         cudaError_t e = s->spec ? launch_spec(s->spec, (int)s->threads, (int)s->slots, a, grid,
                                               chaos_smem(s->slots, a.prog_words, a.steps), s->stream)
                                 : launch_chaos((int)s->threads, (int)s->slots, a, grid, s->stream);
@@ -508,9 +523,15 @@ int rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_width) {
     s->spec = nullptr;
     if (s->d.specialize >= 0) {
         const void* k = nullptr;
-        const int rc = spec_kernel(prog, (int)s->threads, (int)s->slots, s->device, &k);
-        if (rc == RF_OK) s->spec = k;
-        else if (s->d.specialize > 0) return rc;  // required
+        const int rc = spec_kernel(prog, (int)s->threads, (int)s->slots, s->device, &k, SpecKind::Chaos,
+                                   splat_code(s->splat));
+        if (rc == RF_OK) {
+            s->spec = k;
+            s->spec_splat = splat_code(s->splat);
+            s->spec_prog = prog;
+        } else if (s->d.specialize > 0) {
+            return rc;  // required
+        }
     }
     RF_CUDA(cudaMemcpyAsync(s->base_prog, prog.data(), prog.size() * 4, cudaMemcpyHostToDevice, s->stream));
     RF_CUDA(launch_animate(s->base_prog, s->prog_words, s->T, tss_width, s->progs, s->prog_stride, s->stream));

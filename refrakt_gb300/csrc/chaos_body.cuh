@@ -66,7 +66,9 @@ __host__ __device__ inline size_t chaos_smem_bytes(int slots, uint32_t prog_word
 // each thread serves SPT slots per pass (phase_slot(k, tid), in SPT different 256-slot groups, so
 // a warp's work per pass averages over SPT xforms).  64 registers per thread:
 // 1024 threads x 1, 512 x 2 or 256 x 4 CTAs per SM.
-template <int THREADS, int SPT, class Eval>
+// SPLAT >= 0 fixes the splat strategy at compile time (0 global, 1 warp-aggregated, 2 adaptive),
+// so the hot loop carries only that one; -1 dispatches on A.splat.
+template <int THREADS, int SPT, class Eval, int SPLAT = -1>
 __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
     constexpr uint32_t SLOTS = (uint32_t)THREADS * SPT;
     constexpr int G = SLOTS / kGroup;
@@ -183,9 +185,17 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
                     drawn++;
                 }
                 const BinTarget t{A.bins, A.hits, A.rgba_shift, A.count_shift};
-                if (A.splat == 1) splat_warp(t, bin, val);
-                else if (A.splat == 2) splat_adaptive(t, bin, val);
-                else splat_global(t, bin, val);
+                if constexpr (SPLAT == 0) {
+                    splat_global(t, bin, val);
+                } else if constexpr (SPLAT == 1) {
+                    splat_warp(t, bin, val);
+                } else if constexpr (SPLAT == 2) {
+                    splat_adaptive(t, bin, val);
+                } else {
+                    if (A.splat == 1) splat_warp(t, bin, val);
+                    else if (A.splat == 2) splat_adaptive(t, bin, val);
+                    else splat_global(t, bin, val);
+                }
             }
         }
     }

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "internal.h"
 
 struct rf_compiler {
@@ -37,6 +39,8 @@ struct rf_sim {
     uint32_t pass = 0;
     int splat = RF_SPLAT_AUTO;
     const void* spec = nullptr;  // genome-specialised kernel of the warmed flame (specialize.cpp)
+    int spec_splat = -1;              // the splat strategy compiled into it (ChaosArgs.splat code)
+    std::vector<uint32_t> spec_prog;  // the warmed program, to specialise again for another strategy
     int bin_layout = RF_BINS_AUTO;
     uint32_t rgba_shift = 0, count_shift = 0;  // BinTarget addressing of the next launches
     float4* rec = nullptr;       // interleaved bin records (32 B per bin), all zero between calls
