@@ -182,48 +182,61 @@ int genome_param_buffer(const Genome& g, std::vector<float>& buf, std::string* l
     buf.clear();
     float total = 0.0f;
     for (const auto& x : g.xforms) total += x.weight;
-    std::ostringstream js;
-    auto push = [&](const Xform& x) {
-        int start = (int)buf.size();
-        std::ostringstream m;
-        m << "{\"meta\":{\"start\":" << start;
+    // one walk fills the buffer; the layout JSON (indices into it) is written only when asked for
+    const bool want = layout != nullptr;
+    const auto idx = [&]() { return std::to_string(buf.size()); };
+    const auto push = [&](const Xform& x) {
+        std::string aff, post, vars, prm;
+        const size_t start = buf.size();
         buf.push_back(x.weight / total);
-        std::ostringstream aff, post, vars, prm;
-        int weight_at = start;
-        aff << "[";
-        for (int i = 0; i < 6; i++) { aff << (i ? "," : "") << buf.size(); buf.push_back(x.affine[i]); }
-        aff << "]";
-        if (x.has_post) {
-            post << "[";
-            for (int i = 0; i < 6; i++) { post << (i ? "," : "") << buf.size(); buf.push_back(x.post[i]); }
-            post << "]";
+        for (int i = 0; i < 6; i++) {
+            if (want) aff += (i ? "," : "") + idx();
+            buf.push_back(x.affine[i]);
         }
-        vars << "{";
+        if (x.has_post)
+            for (int i = 0; i < 6; i++) {
+                if (want) post += (i ? "," : "") + idx();
+                buf.push_back(x.post[i]);
+            }
         bool first = true;
-        for (const auto& [n, v] : x.vars) { vars << (first ? "" : ",") << "\"" << n << "\":" << buf.size(); buf.push_back(v); first = false; }
-        vars << "}";
-        prm << "{";
+        for (const auto& [n, v] : x.vars) {
+            if (want) vars += (first ? "\"" : ",\"") + n + "\":" + idx();
+            buf.push_back(v);
+            first = false;
+        }
         first = true;
-        for (const auto& [n, v] : x.params) { prm << (first ? "" : ",") << "\"" << n << "\":" << buf.size(); buf.push_back(v); first = false; }
-        prm << "}";
-        int color = (int)buf.size(); buf.push_back(x.color);
-        int cs = (int)buf.size(); buf.push_back(x.color_speed);
-        int op = (int)buf.size(); buf.push_back(x.opacity);
-        int rf = (int)buf.size(); buf.push_back(x.rotation_frequency);
-        int end = (int)buf.size() - 1;
-        m << ",\"end\":" << end << ",\"size\":" << (end - start + 1) << "},\"weight\":" << weight_at
-          << ",\"affine\":" << aff.str();
-        if (x.has_post) m << ",\"post\":" << post.str();
-        m << ",\"variations\":" << vars.str() << ",\"param\":" << prm.str() << ",\"color\":" << color
-          << ",\"color_speed\":" << cs << ",\"opacity\":" << op << ",\"rotation_frequency\":" << rf << "}";
-        return m.str();
+        for (const auto& [n, v] : x.params) {
+            if (want) prm += (first ? "\"" : ",\"") + n + "\":" + idx();
+            buf.push_back(v);
+            first = false;
+        }
+        const size_t color = buf.size();
+        buf.push_back(x.color);
+        buf.push_back(x.color_speed);
+        buf.push_back(x.opacity);
+        buf.push_back(x.rotation_frequency);
+        if (!want) return std::string();
+        const size_t end = buf.size() - 1;
+        std::string m = "{\"meta\":{\"start\":" + std::to_string(start) + ",\"end\":" + std::to_string(end) +
+                        ",\"size\":" + std::to_string(end - start + 1) + "},\"weight\":" + std::to_string(start) +
+                        ",\"affine\":[" + aff + "]";
+        if (x.has_post) m += ",\"post\":[" + post + "]";
+        m += ",\"variations\":{" + vars + "},\"param\":{" + prm + "},\"color\":" + std::to_string(color) +
+             ",\"color_speed\":" + std::to_string(color + 1) + ",\"opacity\":" + std::to_string(color + 2) +
+             ",\"rotation_frequency\":" + std::to_string(color + 3) + "}";
+        return m;
     };
-    js << "{\"xforms\":[";
-    for (size_t i = 0; i < g.xforms.size(); i++) js << (i ? "," : "") << push(g.xforms[i]);
-    js << "]";
-    if (g.has_final) js << ",\"final_xform\":" << push(g.final_xf);
-    js << ",\"size\":" << buf.size() << "}";
-    if (layout) *layout = js.str();
+    std::string js = "{\"xforms\":[";
+    for (size_t i = 0; i < g.xforms.size(); i++) {
+        const std::string m = push(g.xforms[i]);
+        if (want) js += (i ? "," : "") + m;
+    }
+    js += "]";
+    if (g.has_final) {
+        const std::string m = push(g.final_xf);
+        if (want) js += ",\"final_xform\":" + m;
+    }
+    if (want) *layout = js + ",\"size\":" + std::to_string(buf.size()) + "}";
     if ((int)buf.size() > kMaxParams)
         return fail(RF_ERR_CAPACITY, "parameter buffer of " + std::to_string(buf.size()) + " floats exceeds 1024");
     return 0;
