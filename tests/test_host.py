@@ -114,9 +114,11 @@ def test_flame_matches_oracle_layout(rk, orc, compiler):
     assert lay["size"] == info["total_params"]
     for w, h in [(640, 480), (1920, 1080), (17, 3)]:
         assert np.array_equal(np.array(f.screen_affine(w, h), np.float32), o.screen_affine(w, h))
-    # palette: integer part of each component / 256 (flame.cpp:217)
-    for k, want in [(0, [10, 20, 30]), (255, [255, 128, 1])]:
-        pass
+    # palette: the integer part of each component / 256 (flame.cpp:217), as the XML writer
+    # shows it (component x 256)
+    xml = f.to_xml()
+    for k, want in [(0, "10 20 30"), (255, "255 128 1")]:
+        assert '<color index="%d" rgb="%s"' % (k, want) in xml
     assert f.xform_draws(0) == 1 + 5 and f.xform_draws(1) == 0 and f.xform_draws(-1) == 4
     assert [o.xform_draws(i) for i in (0, 1, -1)] == [6, 0, 4]
 
@@ -329,3 +331,38 @@ def test_genome_from_struct_equals_xml(rk, compiler):
     with pytest.raises(rk.RefraktError):
         rk.Flame.from_struct(compiler, {"size": (8, 8), "scale": 1, "palette": pal,
                                         "xforms": [{"weight": 1, "coefs": (1, 0, 0, 1, 0, 0), "vars": {"nope": 1}}]})
+
+
+def test_gemm_and_conv_validate_arguments_before_device_work(rk):
+    # placeholder addresses (16-byte aligned, never dereferenced): every call below must be
+    # refused by the argument checks, so no device is needed
+    L = rk.library()
+    P, Q = 1 << 20, 1 << 21
+    INVALID = 1  # RF_ERR_INVALID_ARG
+    f32, bf16, atomic = rk.GEMM_STORE_F32, rk.GEMM_STORE_BF16, rk.GEMM_ATOMIC_F32
+
+    def gemm(A=P, B=Q, C=P, M=128, N=64, K=64, lda=64, ldb=64, ldc=64, mode=f32, splits=1):
+        return L.rf_gemm_bf16(A, B, C, M, N, K, lda, ldb, ldc, mode, None, 0, splits, None)
+
+    assert gemm(A=None) == INVALID
+    assert gemm(M=0) == INVALID
+    assert gemm(K=60, lda=64, ldb=64) == INVALID       # K not a multiple of 8
+    assert gemm(lda=32) == INVALID                      # stride below K
+    assert gemm(ldc=32) == INVALID                      # output rows narrower than N
+    assert gemm(A=P + 8) == INVALID                     # operand not 16-byte aligned
+    assert gemm(mode=7) == INVALID
+    assert gemm(splits=4, mode=f32) == INVALID          # split K without atomic accumulation
+
+    def conv(xa=P, ca=32, up=0, xb=None, cb=0, n=1, h=16, w=16, B=Q, N=32, ldb=288, C=P, ldc=32, mode=bf16):
+        return L.rf_conv3x3_bf16(xa, ca, up, xb, cb, n, h, w, B, N, ldb, C, ldc, mode, None, 0, None)
+
+    assert conv(xa=None) == INVALID
+    assert conv(ca=12, ldb=108) == INVALID              # channels not a multiple of 8
+    assert conv(cb=16) == INVALID                       # skip channels without a skip tensor
+    assert conv(ldb=280) == INVALID                     # weights narrower than 9 (ca + cb)
+    assert conv(ldc=16) == INVALID                      # output rows narrower than N
+    assert conv(up=1, h=15) == INVALID                  # an upsampled input needs even h, w
+    assert conv(h=70000) == INVALID                     # beyond the 16-bit row / column range
+    assert conv(B=Q + 4) == INVALID                     # weights not 16-byte aligned
+    assert conv(mode=9) == INVALID
+    assert b"rf_conv3x3_bf16" in L.rf_last_error()
