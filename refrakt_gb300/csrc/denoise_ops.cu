@@ -17,8 +17,6 @@ namespace rfk {
 
 namespace {
 
-__device__ __forceinline__ uint4 zero16() { return make_uint4(0, 0, 0, 0); }
-
 // transposed im2col for the weight gradient: colT[k][p], k = tap * C + c (C = ca + cb); with
 // taps = 1 only the centre tap (a plain transpose, for a 1x1 convolution)
 __global__ void im2col_t_kernel(const __nv_bfloat16* __restrict__ xa, uint32_t ca, int up,

@@ -354,7 +354,7 @@ static void de_tables(int R, int min_r, float curve, DeTables& T, std::vector<fl
     const int rmax = R > min_r ? R : min_r;
     for (int r = 0; r <= rmax && r <= 100; r++) {
         T.wbase[r] = (int)wts.size();
-        const double nf = 0.63661977236 / (double)(r * r ? r * r : 1);
+        const double nf = 0.63661977236 / (double)(r > 0 ? r * r : 1);
         const double den = (r + 0.5) * (r + 0.5);
         for (int ay = 0; ay <= r; ay++)
             for (int ax = 0; ax <= r; ax++) {
