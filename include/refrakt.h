@@ -311,17 +311,23 @@ typedef struct {
 } rf_batch_item;
 typedef struct {
     uint32_t fuse_passes;       /* discarded passes at the start of every unit; 0 = 20 */
-    uint32_t cta_slots;         /* walkers per unit (1024, 2048, 4096); 0 = autotune */
-    uint32_t unit_passes;       /* drawing passes per unit; 0 = autotune */
+    uint32_t cta_slots;         /* walkers per unit (1024, 2048, 4096); 0 = autotune: timed on a
+                                   probe batch, then kept for the process per device and set of
+                                   genome structures (the one cache shared between batches, behind
+                                   a lock).  Give it explicitly for units that do not depend on
+                                   timing or on earlier batches. */
+    uint32_t unit_passes;       /* drawing passes per unit; 0 = the length whose units finish
+                                   first on the device's SMs (deterministic for given items) */
     int32_t  density_estimation;/* 1: adaptive DE with each genome's estimator fields */
     float    k2;                /* tonemap k2 (<= 0: automatic per genome) */
     int32_t  use_graph;         /* 1: capture the whole batch in a CUDA graph */
     int32_t  device;
     int32_t  splat;             /* rf_splat; AUTO chooses per genome from its probe histogram */
     int32_t  image_f32;         /* 1: keep each tonemapped image in FP32 too (rf_batch_image_f32) */
-    int32_t  specialize;        /* genome structures with >= 2 units per SM get their own launch
-                                   of a specialised kernel compiled at run time: 0 = when the
-                                   run-time compiler loads, 1 = required, -1 = never */
+    int32_t  specialize;        /* genome structures with >= 2 units per SM (or the only
+                                   structure of the batch) get their own launch of a specialised
+                                   kernel compiled at run time: 0 = when the run-time compiler
+                                   loads, 1 = required, -1 = never */
 } rf_batch_desc;
 RF_API int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc* d, rf_batch** out);
 /* Enqueues one whole batch (clear, draw, DE, tonemap) on the batch's own stream. */
