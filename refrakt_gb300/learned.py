@@ -1,5 +1,6 @@
 """Learned density estimation: data generation, training and evaluation around the C-ABI
-denoiser (rf_denoiser_*), with the plain adaptive-DE path as fallback and judge.
+denoiser (rf_denoiser_*), with the plain adaptive-DE path as its fallback and as the standard
+its error is measured against.
 
 The renderer generates its own training pairs: for each random genome, the features of a
 short-run render (16 samples per pixel: the histogram's log density and colour, and the plain
