@@ -207,7 +207,9 @@ RF_API int  rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_wid
 
 /* Splat strategy for rf_draw_to_bins: one L2 reduction per point (GLOBAL), warp-aggregated
    reductions of the points that share a bin (WARP), or per warp and pass the aggregated form
-   when a cheap test finds two lanes sharing a bin (AUTO, the default). */
+   when a cheap test finds two lanes sharing a bin (AUTO, the default).  The genome-specialised
+   kernel is compiled with the strategy set at rf_warmup; setting another one later makes the
+   next draw call fetch (or, the first time, compile) the kernel for it. */
 enum rf_splat { RF_SPLAT_AUTO = 0, RF_SPLAT_GLOBAL = 1, RF_SPLAT_WARP = 2 };
 /* flame::draw_to_bins(bins, bins_width, num_iter) (flame.cpp:283-330): num_iter passes over
    every walker, drawing into caller-owned device bins.  bins_hits may be NULL.  When `drawn`
