@@ -108,3 +108,28 @@ def test_temporal_samples_with_rotation(rk, orc, compiler, specialize):
     r2 = orc.Genome(LINEAR).chaos(N, 256, 256, fuse=F, draw=D, seed=6, temporal_samples=T, fp64=False, shuffle_mode=1,
                                   cta_slots=4096, steps_per_launch=32, table_size=1024, tss_width=tss, want_rgba=False)
     assert np.array_equal(hits2.cpu().numpy().astype(np.uint64), r2["hits"])
+
+
+def test_splat_strategies_after_warmup(rk, compiler):
+    """The specialised kernel is compiled with the splat strategy set at warmup; setting another
+    one afterwards switches to the kernel for it.  On an affine genome every strategy gives the
+    same counts (the same trajectories) and colour sums equal up to FP32 summation order."""
+    W = H = 128
+    f = rk.Flame.from_xml(LINEAR, compiler)
+    out = {}
+    for mode in (rk.SPLAT_AUTO, rk.SPLAT_GLOBAL, rk.SPLAT_WARP):
+        sim = rk.Sim(8192, seed=6)
+        sim.set_splat(rk.SPLAT_AUTO)
+        sim.warmup(f, 19)
+        assert sim.specialized()
+        sim.set_splat(mode)  # after warmup: the next draw fetches (or compiles) this strategy's kernel
+        bins, hits = _bins(W, H)
+        sim.draw_to_bins(f, bins, hits, W, H, 24)
+        sim.draw_to_bins(f, bins, hits, W, H, 8)
+        out[mode] = (bins.cpu().numpy(), hits.cpu().numpy())
+        sim.close()
+    b0, h0 = out[rk.SPLAT_AUTO]
+    assert int(h0.sum()) > 0
+    for mode, (b, h) in out.items():
+        assert np.array_equal(h, h0), mode
+        assert np.allclose(b, b0, rtol=1e-4, atol=1e-3), mode
