@@ -15,18 +15,25 @@ namespace rfk {
 
 namespace {
 
-// util.hpp:13-26 parse_strings: whitespace-separated tokens, missing ones stay 0
+// util.hpp:13-26 parse_strings: whitespace-separated tokens, missing ones stay 0.  Each token is
+// converted where it lies: the conversions (strtod, strtol) stop at the whitespace that ends it.
 template <class Conv>
 void parse_list(const std::string& in, float* out, int n, Conv cv) {
-    size_t i = 0;
+    const char* p = in.c_str();
+    const char* end = p + in.size();
     int k = 0;
     while (k < n) {
-        while (i < in.size() && isspace((unsigned char)in[i])) i++;
-        if (i >= in.size()) break;
-        size_t b = i;
-        while (i < in.size() && !isspace((unsigned char)in[i])) i++;
-        out[k++] = cv(in.substr(b, i - b));
+        while (p < end && isspace((unsigned char)*p)) p++;
+        if (p >= end) break;
+        out[k++] = cv(p);
+        while (p < end && !isspace((unsigned char)*p)) p++;
     }
+}
+// a token as a float, 0 when it does not start with a number (pugixml as_float)
+float token_float(const char* v) {
+    char* e = nullptr;
+    const double d = strtod(v, &e);
+    return e != v ? (float)d : 0.0f;
 }
 bool num(const std::string& s, double& v) {
     const char* p = s.c_str();
@@ -51,11 +58,11 @@ int apply_xform_attr(Xform& x, const std::string& name, const std::string& val, 
     else if (name == "opacity") x.opacity = as_float(val);
     else if (reg.param_owner.count(name)) x.params[name] = as_float(val);
     else if (reg.vars.count(name)) x.vars[name] = as_float(val);
-    else if (name == "coefs") parse_list(val, x.affine, 6, [](const std::string& v) { double d; return num(v, d) ? (float)d : 0.0f; });
+    else if (name == "coefs") parse_list(val, x.affine, 6, token_float);
     else if (name == "post") {
         x.has_post = true;
         for (int i = 0; i < 6; i++) x.post[i] = 0;
-        parse_list(val, x.post, 6, [](const std::string& v) { double d; return num(v, d) ? (float)d : 0.0f; });
+        parse_list(val, x.post, 6, token_float);
     }
     // flam3 files older than color_speed carry `symmetry`; flam3 maps it to (1 - symmetry) / 2
     else if (name == "symmetry") x.color_speed = (1.0f - as_float(val)) * 0.5f;
@@ -88,7 +95,7 @@ int genome_from_xml(const std::string& xml, const Registry& reg, Genome& g) {
     if (!fl) return fail(RF_ERR_PARSE, "flam3: no <flame> element");
     g = Genome();
     auto A = [&](const char* k) -> std::string { const std::string* v = fl->attr(k); return v ? *v : std::string(); };
-    parse_list(A("center"), g.center, 2, [](const std::string& v) { return as_float(v); });
+    parse_list(A("center"), g.center, 2, token_float);
     g.scale = as_float(A("scale"));
     g.rotate = as_float(A("rotate"));
     g.est_curve = as_float(A("estimator_curve"));
@@ -100,7 +107,7 @@ int genome_from_xml(const std::string& xml, const Registry& reg, Genome& g) {
     g.vibrancy = as_float(A("vibrancy"));
     {
         float sz[2] = {0, 0};
-        parse_list(A("size"), sz, 2, [](const std::string& v) { return (float)strtol(v.c_str(), nullptr, 10); });
+        parse_list(A("size"), sz, 2, [](const char* v) { return (float)strtol(v, nullptr, 10); });
         g.size[0] = (unsigned)std::max(0.0f, sz[0]);
         g.size[1] = (unsigned)std::max(0.0f, sz[1]);
     }
@@ -124,7 +131,7 @@ int genome_from_xml(const std::string& xml, const Registry& reg, Genome& g) {
             if (i < 0 || i > 255) return fail(RF_ERR_PARSE, "flam3: palette index out of range");
             // flame.cpp:217: std::stoi(v) / 256.0f — the integer part of each component
             float c[3] = {0, 0, 0};
-            parse_list(*rgb, c, 3, [](const std::string& v) { return (float)strtol(v.c_str(), nullptr, 10) / 256.0f; });
+            parse_list(*rgb, c, 3, [](const char* v) { return (float)strtol(v, nullptr, 10) / 256.0f; });
             for (int q = 0; q < 3; q++) g.palette[i][q] = c[q];
             g.palette[i][3] = 1.0f;
         } else if (k.name == "palette") {

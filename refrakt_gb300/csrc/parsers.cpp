@@ -135,7 +135,8 @@ struct YReader {
     }
 };
 
-std::string xml_unescape(const std::string& s) {
+std::string xml_unescape(std::string s) {
+    if (s.find('&') == std::string::npos) return s;  // nothing escaped: the text itself
     std::string o;
     for (size_t i = 0; i < s.size(); i++) {
         if (s[i] == '&') {
@@ -159,19 +160,23 @@ std::string xml_unescape(const std::string& s) {
     return o;
 }
 
+// XML whitespace (the S production: space, tab, CR, LF)
+inline bool xml_space(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r'; }
+
 struct XReader {
     const std::string& s;
     size_t i = 0;
     std::string err;
     explicit XReader(const std::string& t) : s(t) {}
 
-    void ws() { while (i < s.size() && isspace((unsigned char)s[i])) i++; }
+    void ws() { while (i < s.size() && xml_space(s[i])) i++; }
     // skips comments, declarations, processing instructions; stops at '<' of an element or end tag
     bool misc(std::string* text) {
         for (;;) {
             size_t b = i;
-            while (i < s.size() && s[i] != '<') i++;
-            if (text) *text += s.substr(b, i - b);
+            const void* lt = i < s.size() ? memchr(s.data() + i, '<', s.size() - i) : nullptr;
+            i = lt ? (size_t)(static_cast<const char*>(lt) - s.data()) : s.size();
+            if (text) text->append(s, b, i - b);
             if (i >= s.size()) return false;
             if (s.compare(i, 4, "<!--") == 0) {
                 size_t e = s.find("-->", i + 4);
@@ -201,8 +206,8 @@ struct XReader {
         if (depth > 64) { err = "nesting too deep"; return false; }
         i++;  // '<'
         size_t b = i;
-        while (i < s.size() && !isspace((unsigned char)s[i]) && s[i] != '>' && s[i] != '/') i++;
-        out.name = s.substr(b, i - b);
+        while (i < s.size() && !xml_space(s[i]) && s[i] != '>' && s[i] != '/') i++;
+        out.name.assign(s, b, i - b);
         if (out.name.empty()) { err = "empty element name"; return false; }
         for (;;) {
             ws();
@@ -213,7 +218,7 @@ struct XReader {
             }
             if (s[i] == '>') { i++; break; }
             size_t ab = i;
-            while (i < s.size() && s[i] != '=' && !isspace((unsigned char)s[i]) && s[i] != '>') i++;
+            while (i < s.size() && s[i] != '=' && !xml_space(s[i]) && s[i] != '>') i++;
             std::string an = s.substr(ab, i - ab);
             ws();
             if (i >= s.size() || s[i] != '=') { err = "attribute `" + an + "` without a value"; return false; }
@@ -222,7 +227,8 @@ struct XReader {
             if (i >= s.size() || (s[i] != '"' && s[i] != '\'')) { err = "unquoted attribute `" + an + "`"; return false; }
             char q = s[i++];
             size_t vb = i;
-            while (i < s.size() && s[i] != q) i++;
+            const void* qe = i < s.size() ? memchr(s.data() + i, q, s.size() - i) : nullptr;
+            i = qe ? (size_t)(static_cast<const char*>(qe) - s.data()) : s.size();
             if (i >= s.size()) { err = "unterminated attribute `" + an + "`"; return false; }
             out.attrs.emplace_back(an, xml_unescape(s.substr(vb, i - vb)));
             i++;
@@ -235,7 +241,7 @@ struct XReader {
                 std::string nm = trim(s.substr(i + 2, e - i - 2));
                 if (nm != out.name) { err = "mismatched </" + nm + "> for <" + out.name + ">"; return false; }
                 i = e + 1;
-                out.text = xml_unescape(out.text);
+                out.text = xml_unescape(std::move(out.text));
                 return true;
             }
             XNode k;
