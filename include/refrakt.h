@@ -224,6 +224,13 @@ RF_API int  rf_set_bin_layout(rf_sim* s, int layout);
 RF_API int  rf_draw_to_bins(rf_sim* s, rf_flame* f, float* bins_rgba, uint32_t* bins_hits,
                      uint32_t width, uint32_t height, uint32_t num_iter, uint64_t* drawn);
 RF_API int  rf_set_splat(rf_sim* s, int splat);
+/* The walker reset that shaders/flame.glsl:68 keeps commented out: after an xform, a walker whose
+   x or y is NaN or beyond +-1e10 (math.glsl:22 `badval`) restarts at (2u1 - 1, 2u2 - 1) from two
+   randf() draws of its slot, with opacity 0 (that step is not drawn).  0 (default) = the
+   reference's behaviour: such a walker stays lost and is never drawn again, so over thousands of
+   passes a genome with singular variations (spherical, julian ...) binns fewer and fewer points.
+   Takes effect from the next rf_warmup / rf_draw_to_bins launch. */
+RF_API int  rf_set_bad_value_reset(rf_sim* s, int on);
 /* [0] points binned and [1] points emitted (opacity > 0) by the last rf_draw_to_bins call,
    [2] walker-steps since rf_warmup. */
 RF_API int  rf_sim_counters(rf_sim* s, uint64_t out[3]);
@@ -282,6 +289,11 @@ typedef struct {
     float    tss_width;
     float    k2;                /* tonemap k2 (<= 0: automatic) */
     int32_t  density_estimation;/* 1: run the adaptive DE with the genome's estimator fields */
+    int32_t  stop_on_binned;    /* 0: `points` walker-steps are computed; 1: passes are drawn until
+                                   `points` points are binned — the reference's quality stop
+                                   (main.cpp:411-412, accumulated < quality * W * H) — reading
+                                   the binned count back between rounds of passes, at most 16x the
+                                   passes of one step per point */
 } rf_render_desc;
 /* Renders `f` into out_rgba8 (host memory, width*height*4 bytes).  stats (may be NULL):
    [0] points computed, [1] points binned, [2] milliseconds on the device. */
@@ -330,6 +342,7 @@ typedef struct {
                                    structure of the batch) get their own launch of a specialised
                                    kernel compiled at run time: 0 = when the run-time compiler
                                    loads, 1 = required, -1 = never */
+    int32_t  bad_value_reset;   /* 1: walkers that leave the plane restart, as rf_set_bad_value_reset */
 } rf_batch_desc;
 RF_API int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc* d, rf_batch** out);
 /* Enqueues one whole batch (clear, draw, DE, tonemap) on the batch's own stream. */

@@ -689,6 +689,21 @@ int xform_draws(const Xform& xf, bool first_run) {
 
 // xform_select.tpl.glsl: sequential FP32 sum of normalised weights, first i with sum >= r,
 // the last xform unconditional.
+// math.glsl:22 badval, and the walker reset flame.glsl:68 keeps commented out: result.xyw =
+// vec3(vec2(randf(), randf()) * 2.0 - 1.0, 0.0) when x or y is NaN or beyond +-1e10.  The FP32
+// walker is tested in FP32, the FP64 oracle's in double.
+template <class T>
+bool reset_bad(T& x, T& y, T& w, Jsf& s) {
+    auto bad = [](T v) { return !(std::fabs(v) <= (T)1e10f); };
+    if (!(bad(x) || bad(y))) return false;
+    float u1 = randf(s);
+    float u2 = randf(s);
+    x = (T)(u1 * 2.0f - 1.0f);
+    y = (T)(u2 * 2.0f - 1.0f);
+    w = 0;
+    return true;
+}
+
 int select_xform(const orc_genome* g, float r) {
     const int n = (int)g->xf.size();
     float sum = 0.0f;
@@ -904,6 +919,7 @@ int chaos(const orc_genome* g, const orc_chaos_cfg* cfg, double* rgba, uint64_t*
                 }
                 T w;
                 dispatch<T>(xf[t][xid[grp]], x, y, c, w, first, s);
+                if (cfg->badval_reset) reset_bad<T>(x, y, w, s);
                 nx[dstidx[slot]] = x; ny[dstidx[slot]] = y; nc[dstidx[slot]] = c;
                 if (draw) {
                     T dx = x, dy = y, dc = c, dw = w;
@@ -1012,6 +1028,50 @@ int orc_genome_param_buffer(const orc_genome* g, float* out, int cap) {
     if (out) for (int i = 0; i < (int)buf.size() && i < cap; i++) out[i] = buf[i];
     return (int)buf.size();
 }
+// flame.cpp:33-71 make_shader_buffer_map: the offsets of the buffer above, as JSON
+int orc_genome_layout_json(const orc_genome* g, char* out, int cap) {
+    std::string js = "{\"xforms\": [";
+    int off = 0;
+    auto block = [&](const Xform& x) {
+        std::string b = "{\"weight\": " + std::to_string(off++) + ", \"affine\": [";
+        for (int i = 0; i < 6; i++) b += (i ? ", " : "") + std::to_string(off++);
+        b += "]";
+        if (x.has_post) {
+            b += ", \"post\": [";
+            for (int i = 0; i < 6; i++) b += (i ? ", " : "") + std::to_string(off++);
+            b += "]";
+        }
+        b += ", \"variations\": {";
+        bool first = true;
+        for (auto& kv : x.vars) { b += (first ? "\"" : ", \"") + kv.first + "\": " + std::to_string(off++); first = false; }
+        b += "}, \"param\": {";
+        first = true;
+        for (auto& kv : x.params) { b += (first ? "\"" : ", \"") + kv.first + "\": " + std::to_string(off++); first = false; }
+        b += "}, \"color\": " + std::to_string(off++);
+        b += ", \"color_speed\": " + std::to_string(off++);
+        b += ", \"opacity\": " + std::to_string(off++);
+        b += ", \"rotation_frequency\": " + std::to_string(off++) + "}";
+        return b;
+    };
+    for (size_t i = 0; i < g->xf.size(); i++) js += (i ? ", " : "") + block(g->xf[i]);
+    js += "]";
+    if (g->has_final) js += ", \"final_xform\": " + block(g->fin);
+    js += ", \"size\": " + std::to_string(off) + "}";
+    if (out && cap > 0) snprintf(out, (size_t)cap, "%s", js.c_str());
+    return (int)js.size();
+}
+
+int orc_animate_params(const orc_genome* g, uint32_t T, float tss_width, uint32_t t, float* out, int cap) {
+    if (T == 0 || t >= T) return -1;
+    std::vector<std::vector<Xform>> xf;
+    std::vector<Xform> fin;
+    animate(g, T, tss_width, xf, fin);
+    orc_genome tmp = *g;
+    tmp.xf = xf[t];
+    tmp.fin = fin[t];
+    return orc_genome_param_buffer(&tmp, out, cap);
+}
+
 void orc_genome_info(const orc_genome* g, double* o) {
     o[0] = g->size[0]; o[1] = g->size[1]; o[2] = g->center[0]; o[3] = g->center[1];
     o[4] = g->scale; o[5] = g->rotate; o[6] = g->est_radius; o[7] = g->est_min; o[8] = g->est_curve;
@@ -1078,7 +1138,8 @@ int orc_xid_sequence(const orc_genome* g, uint64_t N, uint32_t TS, uint64_t seed
 }
 
 uint64_t orc_cpu_baseline(const orc_genome* g, uint64_t N, uint32_t passes, uint32_t W, uint32_t H,
-                          int threads, uint64_t seed, float* rgba_out, uint32_t* hits_out) {
+                          int threads, uint64_t seed, int badval_reset, float* rgba_out, uint32_t* hits_out,
+                          uint64_t* binned_out) {
     // FP32 transcription of flame.glsl's draw pass over walker slices (one temporal sample per
     // slice, shuffled within the slice), private histograms merged at the end.
     threads = std::max(1, threads);
@@ -1088,7 +1149,7 @@ uint64_t orc_cpu_baseline(const orc_genome* g, uint64_t N, uint32_t passes, uint
     screen_affine(g, W, H, ss);
     std::vector<std::vector<float>> prgba(threads);
     std::vector<std::vector<uint32_t>> phits(threads);
-    std::vector<uint64_t> done(threads, 0);
+    std::vector<uint64_t> done(threads, 0), binned(threads, 0);
     auto work = [&](int ti) {
         uint64_t g0 = groups * ti / threads, g1 = groups * (ti + 1) / threads;
         uint64_t n = (g1 - g0) * 256, base = g0 * 256;
@@ -1103,7 +1164,7 @@ uint64_t orc_cpu_baseline(const orc_genome* g, uint64_t N, uint32_t passes, uint
         std::vector<uint32_t> perm(n);
         for (uint64_t i = 0; i < n; i++) { float a, b; sample_point((uint32_t)i, (uint32_t)n, a, b); px[i] = a; py[i] = b; pc[i] = 0.5f; perm[i] = (uint32_t)i; }
         std::mt19937_64 pr(seed * 7919 + ti);
-        uint64_t cnt = 0;
+        uint64_t cnt = 0, nb = 0;
         for (uint32_t p = 0; p < passes; p++) {
             std::shuffle(perm.begin(), perm.end(), pr);
             int xid = 0;
@@ -1112,6 +1173,7 @@ uint64_t orc_cpu_baseline(const orc_genome* g, uint64_t N, uint32_t passes, uint
                 if (i % 256 == 0) xid = select_xform(g, randf(s));
                 float x = px[perm[i]], y = py[perm[i]], c = pc[perm[i]], w;
                 dispatch<float>(g->xf[xid], x, y, c, w, false, s);
+                if (badval_reset) reset_bad<float>(x, y, w, s);
                 nx[i] = x; ny[i] = y; nc[i] = c;
                 if (g->has_final) { float fw; dispatch<float>(g->fin, x, y, c, fw, false, s); w *= fw; }
                 float sx_ = std::fma(ss[0], x, std::fma(ss[2], y, ss[4]));
@@ -1123,23 +1185,27 @@ uint64_t orc_cpu_baseline(const orc_genome* g, uint64_t N, uint32_t passes, uint
                     hr[idx * 4] += g->palette[ci][0]; hr[idx * 4 + 1] += g->palette[ci][1];
                     hr[idx * 4 + 2] += g->palette[ci][2]; hr[idx * 4 + 3] += w;
                     hh[idx] += 1;
+                    nb++;
                 }
                 cnt++;
             }
             std::swap(px, nx); std::swap(py, ny); std::swap(pc, nc);
         }
         done[ti] = cnt;
+        binned[ti] = nb;
     };
     std::vector<std::thread> th;
     for (int t = 0; t < threads; t++) th.emplace_back(work, t);
     for (auto& t : th) t.join();
-    uint64_t total = 0;
+    uint64_t total = 0, total_binned = 0;
     for (int t = 0; t < threads; t++) {
         total += done[t];
+        total_binned += binned[t];
         if (prgba[t].empty()) continue;
         if (rgba_out) for (size_t i = 0; i < prgba[t].size(); i++) rgba_out[i] += prgba[t][i];
         if (hits_out) for (size_t i = 0; i < phits[t].size(); i++) hits_out[i] += phits[t][i];
     }
+    if (binned_out) *binned_out = total_binned;
     return total;
 }
 
@@ -1161,6 +1227,15 @@ int de_radius(double a, int R, double curve) {
 }  // namespace
 
 extern "C" {
+
+int orc_de_radius(double a, int R, int minr, double curve) { return std::max(minr, de_radius(a, R, curve)); }
+
+double orc_de_weight(int dx, int dy, int r) {
+    if (r == 0) return (dx == 0 && dy == 0) ? 1.0 : -1.0;
+    const int d2 = dx * dx + dy * dy;
+    if (4 * d2 > (2 * r + 1) * (2 * r + 1)) return -1.0;
+    return (1.0 - (double)d2 / ((r + 0.5) * (r + 0.5))) * (0.63661977236 / (double)(r * r));
+}
 
 // density_vert.glsl:26-63, density_frag.glsl:9-18, restated symmetrically: every bin with a > 0
 // spreads over the pixels (dx, dy) with 4*(dx^2+dy^2) <= (2r+1)^2, weight

@@ -42,6 +42,13 @@ int  orc_genome_num_xforms(const orc_genome* g);
 int  orc_genome_has_final(const orc_genome* g);
 /* flat parameter buffer (src/flame.cpp:33-103); returns total_params or -1 */
 int  orc_genome_param_buffer(const orc_genome* g, float* out, int cap);
+/* its layout as the reference's buffer_map_ JSON (flame.cpp:33-71: per xform weight, affine[6],
+   post[6], variations, param, color, color_speed, opacity, rotation_frequency; final_xform;
+   size) — what the reference renders its shader templates with.  Returns the length (the
+   text is truncated to cap - 1 bytes and NUL-terminated). */
+int  orc_genome_layout_json(const orc_genome* g, char* out, int cap);
+/* the flat parameter buffer of temporal sample t of T after animate.tpl.glsl's rotation */
+int  orc_animate_params(const orc_genome* g, uint32_t T, float tss_width, uint32_t t, float* out, int cap);
 /* camera + tonemap fields: size[2], center[2], scale, rotate, est_radius, est_min, est_curve,
    gamma, vibrancy, brightness  -> 12 doubles */
 void orc_genome_info(const orc_genome* g, double* out12);
@@ -76,6 +83,7 @@ typedef struct {
     int      threads;          /* worker threads (>=1) */
     int      table_seed_set;   /* shuffle_mode 1: 1 = the local table is keyed by table_seed, */
     uint64_t table_seed;       /*   0 = by seed (the batched launch shares one table) */
+    int      badval_reset;     /* 1: the walker reset flame.glsl:68 keeps commented out */
 } orc_chaos_cfg;
 
 /* rgba: W*H*4 doubles (may be NULL), hits: W*H u64 (may be NULL),
@@ -84,15 +92,23 @@ typedef struct {
 int orc_chaos(const orc_genome* g, const orc_chaos_cfg* cfg, double* rgba, uint64_t* hits,
               uint8_t* xid_trace, uint64_t* counters);
 
-/* The xid sequence alone, predicted from RNG draw counts (no walker arithmetic). */
+/* The xid sequence alone, predicted from RNG draw counts (no walker arithmetic; without the
+   walker reset, whose draws depend on the walker). */
 int orc_xid_sequence(const orc_genome* g, uint64_t walkers, uint32_t temporal_samples,
                      uint64_t seed, uint32_t fuse_passes, uint32_t draw_passes, uint8_t* out);
 
 /* Multi-threaded FP32 transcription used as the timed CPU baseline: walker slices
-   with private float histograms merged at the end.  Returns points computed. */
+   with private float histograms merged at the end, optionally with the walker reset of
+   flame.glsl:68.  Returns points computed; *binned_out (may be NULL) the points binned. */
 uint64_t orc_cpu_baseline(const orc_genome* g, uint64_t walkers, uint32_t passes,
-                          uint32_t width, uint32_t height, int threads, uint64_t seed,
-                          float* rgba_out, uint32_t* hits_out);
+                          uint32_t width, uint32_t height, int threads, uint64_t seed, int badval_reset,
+                          float* rgba_out, uint32_t* hits_out, uint64_t* binned_out);
+
+/* The density estimator's radius of a bin with density a (density_vert.glsl:35-44) and the
+   kernel weight at offset (dx, dy) of a disc of radius r (density_frag.glsl:9-18, symmetric
+   restatement); the weight is -1 outside the disc. */
+int    orc_de_radius(double a, int radius, int min_radius, double curve);
+double orc_de_weight(int dx, int dy, int r);
 
 /* Adaptive density estimation (shaders/density_vert.glsl:26-63, density_frag.glsl:9-18),
    symmetric restatement: d = |delta|^2/(r+0.5)^2. in/out W*H*4 doubles. */

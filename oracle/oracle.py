@@ -44,7 +44,8 @@ class ChaosCfg(ctypes.Structure):
                 ("height", ctypes.c_uint32), ("fp64", ctypes.c_int), ("shuffle_mode", ctypes.c_int),
                 ("cta_slots", ctypes.c_uint32), ("steps_per_launch", ctypes.c_uint32),
                 ("table_size", ctypes.c_uint32), ("tss_width", ctypes.c_float),
-                ("threads", ctypes.c_int), ("table_seed_set", ctypes.c_int), ("table_seed", ctypes.c_uint64)]
+                ("threads", ctypes.c_int), ("table_seed_set", ctypes.c_int), ("table_seed", ctypes.c_uint64),
+                ("badval_reset", ctypes.c_int)]
 
 
 def lib():
@@ -70,6 +71,12 @@ def lib():
         L.orc_genome_has_final.argtypes = [ctypes.c_void_p]
         L.orc_genome_param_buffer.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         L.orc_genome_info.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_genome_layout_json.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]
+        L.orc_animate_params.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_float, ctypes.c_uint32,
+                                         ctypes.c_void_p, ctypes.c_int]
+        L.orc_de_radius.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        L.orc_de_weight.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.orc_de_weight.restype = ctypes.c_double
         L.orc_screen_affine.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p]
         L.orc_xform_draws.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.orc_select_xform.argtypes = [ctypes.c_void_p, ctypes.c_float]
@@ -80,8 +87,8 @@ def lib():
         L.orc_xid_sequence.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64,
                                        ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p]
         L.orc_cpu_baseline.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
-                                       ctypes.c_uint32, ctypes.c_int, ctypes.c_uint64, ctypes.c_void_p,
-                                       ctypes.c_void_p]
+                                       ctypes.c_uint32, ctypes.c_int, ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p]
         L.orc_cpu_baseline.restype = ctypes.c_uint64
         L.orc_density_estimate.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
@@ -176,6 +183,22 @@ class Genome:
         lib().orc_genome_param_buffer(self.h, _ptr(out), n)
         return out
 
+    def layout(self):
+        """The parameter buffer's layout as the reference's buffer_map_ (flame.cpp:33-71)."""
+        import json
+        n = lib().orc_genome_layout_json(self.h, None, 0)
+        buf = ctypes.create_string_buffer(n + 1)
+        lib().orc_genome_layout_json(self.h, buf, n + 1)
+        return json.loads(buf.value.decode())
+
+    def animate_params(self, T, tss_width, t):
+        """The flat parameter buffer of temporal sample t of T (animate.tpl.glsl)."""
+        n = lib().orc_genome_param_buffer(self.h, None, 0)
+        out = np.zeros(n, np.float32)
+        if lib().orc_animate_params(self.h, T, tss_width, t, _ptr(out), n) != n:
+            raise ValueError("animate_params failed")
+        return out
+
     def info(self):
         o = np.zeros(12, np.float64)
         lib().orc_genome_info(self.h, _ptr(o))
@@ -206,10 +229,10 @@ class Genome:
 
     def chaos(self, walkers, width, height, fuse=20, draw=16, seed=0, temporal_samples=1, fp64=True,
               shuffle_mode=0, cta_slots=1024, steps_per_launch=32, table_size=1024, tss_width=0.02,
-              trace=False, want_rgba=True, table_seed=None):
+              trace=False, want_rgba=True, table_seed=None, badval_reset=False, threads=1):
         cfg = ChaosCfg(walkers, temporal_samples, seed, fuse, draw, width, height, int(fp64), shuffle_mode,
-                       cta_slots, steps_per_launch, table_size, tss_width, 1, int(table_seed is not None),
-                       table_seed or 0)
+                       cta_slots, steps_per_launch, table_size, tss_width, threads, int(table_seed is not None),
+                       table_seed or 0, int(bool(badval_reset)))
         rgba = np.zeros((height, width, 4), np.float64) if want_rgba else None
         hits = np.zeros((height, width), np.uint64)
         tr = np.zeros((fuse + draw, walkers // 256), np.uint8) if trace else None
@@ -227,12 +250,25 @@ class Genome:
             raise ValueError("xid_sequence failed")
         return out
 
-    def cpu_baseline(self, walkers, passes, width, height, threads, seed=0, want=False):
+    def cpu_baseline(self, walkers, passes, width, height, threads, seed=0, want=False, badval_reset=False,
+                     binned=False):
         rgba = np.zeros((height, width, 4), np.float32) if want else None
         hits = np.zeros((height, width), np.uint32) if want else None
-        n = lib().orc_cpu_baseline(self.h, walkers, passes, width, height, threads, seed,
-                                   _ptr(rgba) if want else None, _ptr(hits) if want else None)
+        nb = ctypes.c_uint64(0)
+        n = lib().orc_cpu_baseline(self.h, walkers, passes, width, height, threads, seed, int(bool(badval_reset)),
+                                   _ptr(rgba) if want else None, _ptr(hits) if want else None, ctypes.byref(nb))
+        if binned:
+            return n, rgba, hits, nb.value
         return n, rgba, hits
+
+
+def de_radius(a, radius, min_radius, curve):
+    return lib().orc_de_radius(a, radius, min_radius, curve)
+
+
+def de_weight(dx, dy, r):
+    """Kernel weight at offset (dx, dy) of a disc of radius r, or -1 outside it."""
+    return lib().orc_de_weight(dx, dy, r)
 
 
 def density_estimate(rgba, radius, min_radius, curve):

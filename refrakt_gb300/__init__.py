@@ -79,7 +79,7 @@ class SimDesc(ctypes.Structure):
 class RenderDesc(ctypes.Structure):
     _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("supersample", ctypes.c_uint32),
                 ("fuse_passes", ctypes.c_uint32), ("points", ctypes.c_uint64), ("tss_width", ctypes.c_float),
-                ("k2", ctypes.c_float), ("density_estimation", ctypes.c_int32)]
+                ("k2", ctypes.c_float), ("density_estimation", ctypes.c_int32), ("stop_on_binned", ctypes.c_int32)]
 
 
 class BatchItem(ctypes.Structure):
@@ -91,7 +91,7 @@ class BatchDesc(ctypes.Structure):
     _fields_ = [("fuse_passes", ctypes.c_uint32), ("cta_slots", ctypes.c_uint32), ("unit_passes", ctypes.c_uint32),
                 ("density_estimation", ctypes.c_int32), ("k2", ctypes.c_float), ("use_graph", ctypes.c_int32),
                 ("device", ctypes.c_int32), ("splat", ctypes.c_int32), ("image_f32", ctypes.c_int32),
-                ("specialize", ctypes.c_int32)]
+                ("specialize", ctypes.c_int32), ("bad_value_reset", ctypes.c_int32)]
 
 
 class DenoiserDesc(ctypes.Structure):
@@ -146,6 +146,7 @@ _SIGS = {
     "rf_draw_to_bins": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                          ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "rf_set_splat": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rf_set_bad_value_reset": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rf_set_bin_layout": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rf_sim_counters": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "rf_density_estimate": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
@@ -485,6 +486,11 @@ class Sim:
     def set_splat(self, splat):
         _check(library().rf_set_splat(self._h, splat))
 
+    def set_bad_value_reset(self, on):
+        """Restart walkers that leave the plane (rf_set_bad_value_reset; the reference keeps this
+        step commented out at shaders/flame.glsl:68, so the default is off)."""
+        _check(library().rf_set_bad_value_reset(self._h, int(bool(on))))
+
     def set_bin_layout(self, layout):
         """BINS_AUTO, BINS_DIRECT or BINS_INTERLEAVED (rf_set_bin_layout)."""
         _check(library().rf_set_bin_layout(self._h, layout))
@@ -501,11 +507,14 @@ class Sim:
         return {"drawn": out[0], "emitted": out[1], "steps": out[2]}
 
     def render(self, flame, width, height, points, supersample=1, fuse_passes=20, tss_width=0.0, k2=0.0,
-               density_estimation=True, out=None):
-        """One frame from genome to host RGBA8 (rf_render).  Returns (image, stats)."""
+               density_estimation=True, out=None, stop_on_binned=False):
+        """One frame from genome to host RGBA8 (rf_render).  Returns (image, stats).  With
+        stop_on_binned, `points` counts binned points (the reference's quality stop) instead of
+        walker-steps."""
         import numpy as np
         img = out if out is not None else np.zeros((height, width, 4), np.uint8)
-        d = RenderDesc(width, height, supersample, fuse_passes, points, tss_width, k2, int(density_estimation))
+        d = RenderDesc(width, height, supersample, fuse_passes, points, tss_width, k2, int(density_estimation),
+                       int(stop_on_binned))
         st = (ctypes.c_double * 3)()
         _check(library().rf_render(self._h, flame._h, ctypes.byref(d), img.ctypes.data_as(ctypes.c_void_p), st))
         return img, {"points": st[0], "binned": st[1], "ms": st[2]}
@@ -517,7 +526,7 @@ class Batch:
     (flame, width, height, points, seed, supersample) tuples."""
 
     def __init__(self, items, fuse_passes=20, cta_slots=0, unit_passes=0, density_estimation=True, k2=0.0,
-                 use_graph=True, device=0, splat=0, image_f32=False, specialize=0):
+                 use_graph=True, device=0, splat=0, image_f32=False, specialize=0, bad_value_reset=False):
         arr = (BatchItem * len(items))()
         self.sizes = []
         self._flames = [it[0] for it in items]  # keep the genomes alive as long as the batch
@@ -527,7 +536,7 @@ class Batch:
             arr[i] = BatchItem(flame._h, w, h, ss, points, seed)
             self.sizes.append((w, h, ss))
         d = BatchDesc(fuse_passes, cta_slots, unit_passes, int(density_estimation), k2, int(use_graph), device, splat,
-                      int(image_f32), specialize)
+                      int(image_f32), specialize, int(bool(bad_value_reset)))
         h = ctypes.c_void_p()
         _check(library().rf_batch_create(arr, len(items), ctypes.byref(d), ctypes.byref(h)))
         self._h = h

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -91,6 +92,7 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.first_run = (first_run && done == 0) ? 1 : 0;
         a.draw = draw ? 1 : 0;
         a.splat = splat_code(s->splat);
+        a.reset = s->reset;
         a.rgba_shift = s->rgba_shift;
         a.count_shift = s->count_shift;
         if (ss) memcpy(a.ss, ss, sizeof(a.ss));
@@ -104,13 +106,15 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.trace_passes = s->trace_passes;
         a.n_groups = (uint32_t)(s->N / kGroup);
         const uint32_t grid = (uint32_t)(s->N / s->slots);
-        if (s->spec && s->spec_splat != a.splat) {  // the strategy changed since warmup: its own kernel
+        if (s->spec && (s->spec_splat != a.splat || s->spec_reset != a.reset)) {
+            // the splat strategy or the reset changed since warmup: the kernel compiled for them
             const void* k = nullptr;
             if (int rc = spec_kernel(s->spec_prog, (int)s->threads, (int)s->slots, s->device, &k, SpecKind::Chaos,
-                                     a.splat))
+                                     a.splat, a.reset))
                 return rc;
             s->spec = k;
             s->spec_splat = a.splat;
+            s->spec_reset = a.reset;
         }
         cudaError_t e = s->spec ? launch_spec(s->spec, (int)s->threads, (int)s->slots, a, grid,
                                               chaos_smem(s->slots, a.prog_words, a.steps), s->stream)
@@ -524,10 +528,11 @@ int rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_width) {
     if (s->d.specialize >= 0) {
         const void* k = nullptr;
         const int rc = spec_kernel(prog, (int)s->threads, (int)s->slots, s->device, &k, SpecKind::Chaos,
-                                   splat_code(s->splat));
+                                   splat_code(s->splat), s->reset);
         if (rc == RF_OK) {
             s->spec = k;
             s->spec_splat = splat_code(s->splat);
+            s->spec_reset = s->reset;
             s->spec_prog = prog;
         } else if (s->d.specialize > 0) {
             return rc;  // required
@@ -584,6 +589,12 @@ int rf_set_bin_layout(rf_sim* s, int layout) {
 int rf_set_splat(rf_sim* s, int splat) {
     if (!s) return fail(RF_ERR_INVALID_ARG, "rf_set_splat: null sim");
     s->splat = splat;
+    return RF_OK;
+}
+
+int rf_set_bad_value_reset(rf_sim* s, int on) {
+    if (!s || (on != 0 && on != 1)) return fail(RF_ERR_INVALID_ARG, "rf_set_bad_value_reset: null sim or flag not 0/1");
+    s->reset = on;
     return RF_OK;
 }
 
@@ -730,13 +741,31 @@ int rf_render(rf_sim* s, rf_flame* f, const rf_render_desc* d, uint8_t* out, dou
     if (cudaEventRecord(e0, s->stream) != cudaSuccess) return done(fail(RF_ERR_CUDA, "event record"));
     // fuse_passes counts every discarded pass, the first-run pass included
     if (int rc = rf_warmup(s, f, d->fuse_passes ? d->fuse_passes - 1 : 0, d->tss_width)) return done(rc);
-    const uint64_t passes = (d->points + s->N - 1) / s->N;
-    if (passes > 0xffffffffull) return done(fail(RF_ERR_CAPACITY, "rf_render: too many passes"));
+    const uint64_t passes1 = (d->points + s->N - 1) / s->N;  // passes of one walker-step per point
+    if (passes1 > 0xffffffffull / 16) return done(fail(RF_ERR_CAPACITY, "rf_render: too many passes"));
     cudaError_t e = cudaMemsetAsync(s->r_bins, 0, nb * sizeof(float4), s->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s->r_hits, 0, nb * sizeof(uint32_t), s->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s->counters, 0, 2 * sizeof(unsigned long long), s->stream);
     if (e != cudaSuccess) return done(cuda_fail(e, "rf_render clear"));
-    if (int rc = draw_passes(s, (uint32_t)passes, s->r_bins, s->r_hits, W, H, ssa)) return done(rc);
+    uint64_t passes = passes1;
+    if (int rc = draw_passes(s, (uint32_t)passes1, s->r_bins, s->r_hits, W, H, ssa)) return done(rc);
+    if (d->stop_on_binned) {
+        // main.cpp:411-412: keep drawing while the binned count is below the target.  Each round
+        // reads the count back and draws the passes the measured binned-per-pass rate predicts
+        // for the rest (at least one), up to 16x the first round.
+        for (;;) {
+            unsigned long long got = 0;
+            e = cudaMemcpyAsync(&got, s->counters, sizeof got, cudaMemcpyDeviceToHost, s->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+            if (e != cudaSuccess) return done(cuda_fail(e, "rf_render binned count"));
+            if (got >= d->points || passes >= 16 * passes1) break;
+            const double rate = (double)got / (double)passes;  // points binned per pass
+            uint64_t more = rate > 0.0 ? (uint64_t)std::ceil((double)(d->points - got) / rate) : passes1;
+            more = std::max<uint64_t>(1, std::min<uint64_t>(more, 16 * passes1 - passes));
+            if (int rc = draw_passes(s, (uint32_t)more, s->r_bins, s->r_hits, W, H, ssa)) return done(rc);
+            passes += more;
+        }
+    }
     const float4* src = s->r_bins;
     if (d->density_estimation && (f->g.est_radius > 0 || f->g.est_min > 0)) {
         const int R = std::min(100, f->g.est_radius), mn = std::min(100, f->g.est_min);

@@ -161,6 +161,7 @@ int build_tables(rf_batch* b, uint32_t slots, uint32_t unit_passes, uint32_t pro
         I.W = it.W;
         I.H = it.H;
         I.splat = it.splat;
+        I.reset = b->d.bad_value_reset ? 1u : 0u;
         genome_screen_affine(b->items[i].desc.flame->g, it.W, it.H, I.ss);
         inst.push_back(I);
         if (probe_passes) {

@@ -16,6 +16,7 @@ struct BatchInstance {
     uint32_t* hits;         // counts, may be null
     uint32_t W, H;
     uint32_t splat;         // 0: a reduction per point; 1: warp-aggregated (splat.cuh)
+    uint32_t reset;         // 1: walkers that leave the plane restart (reset_bad_walker, device.cuh)
     float ss[6];            // screen affine
 };
 

@@ -119,8 +119,12 @@ __device__ __forceinline__ void batch_body(const BatchArgs& A) {
                 for (int it = 0;; it++) {
                     float o;
                     Eval::apply(s_prog, it == 0 ? xi : -1, foff, ex, ey, ec, o, fr, rng);
-                    if (it == 0) { x = ex; y = ey; c = ec; op = o; }
-                    else op = o * op;
+                    if (it == 0) {
+                        if (I.reset) reset_bad_walker(ex, ey, o, rng);  // flame.glsl:68
+                        x = ex; y = ey; c = ec; op = o;
+                    } else {
+                        op = o * op;
+                    }
                     if (it == 1 || !with_final) break;
                     fr = false;
                 }

@@ -23,6 +23,7 @@ struct ChaosArgs {
     int first_run;           // pass 0 reads the start points, jitters, draws colours
     int draw;
     int splat;               // 0: a reduction per point; 1: warp-aggregated; 2: adaptive (splat.cuh)
+    int reset;               // 1: walkers that leave the plane restart (reset_bad_walker, device.cuh)
     uint32_t rgba_shift;     // bin addressing (splat.cuh BinTarget): 0 and 0 for the caller's
     uint32_t count_shift;    //   planes, 1 and 3 for interleaved 32-byte records
     float ss[6];             // screen affine

@@ -67,8 +67,9 @@ __host__ __device__ inline size_t chaos_smem_bytes(int slots, uint32_t prog_word
 // a warp's work per pass averages over SPT xforms).  64 registers per thread:
 // 1024 threads x 1, 512 x 2 or 256 x 4 CTAs per SM.
 // SPLAT >= 0 fixes the splat strategy at compile time (0 global, 1 warp-aggregated, 2 adaptive),
-// so the hot loop carries only that one; -1 dispatches on A.splat.
-template <int THREADS, int SPT, class Eval, int SPLAT = -1>
+// so the hot loop carries only that one; -1 dispatches on A.splat.  RESET >= 0 likewise fixes
+// the walker reset of flame.glsl:68 (reset_bad_walker); -1 reads A.reset.
+template <int THREADS, int SPT, class Eval, int SPLAT = -1, int RESET = -1>
 __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
     constexpr uint32_t SLOTS = (uint32_t)THREADS * SPT;
     constexpr int G = SLOTS / kGroup;
@@ -116,6 +117,7 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
     const bool has_final = A.draw && foff != 0;
     const int dphase = draw_phase<THREADS, SPT>(tid);
     const float W = (float)A.W, H = (float)A.H;
+    const bool reset = RESET >= 0 ? RESET != 0 : A.reset != 0;
     uint32_t drawn = 0, emitted = 0;
 
     for (uint32_t s = 0; s < A.steps; s++) {
@@ -164,8 +166,12 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
             for (int it = 0;; it++) {
                 float o;
                 Eval::apply(s_prog, it == 0 ? xi : -1, foff, ex, ey, ec, o, fr, rng);
-                if (it == 0) { x = ex; y = ey; c = ec; op = o; }
-                else op = o * op;
+                if (it == 0) {
+                    if (reset) reset_bad_walker(ex, ey, o, rng);  // flame.glsl:68, before pos_out
+                    x = ex; y = ey; c = ec; op = o;
+                } else {
+                    op = o * op;
+                }
                 if (it == 1 || !has_final) break;
                 fr = false;
             }

@@ -130,6 +130,24 @@ __device__ __forceinline__ int select_xform(const uint32_t* prog, float r) {
     return (int)n - 1;
 }
 
+// math.glsl:22 `badval`: NaN, or beyond +-1e10.
+__device__ __forceinline__ bool bad_value(float v) { return !(fabsf(v) <= 1e10f); }
+
+// The walker reset the reference keeps commented out after dispatch (flame.glsl:68):
+// `if (badval(result.x) || badval(result.y)) result.xyw = vec3(vec2(randf(), randf()) * 2.0 - 1.0, 0.0)`.
+// A walker that left the plane (NaN, infinity, |v| > 1e10) restarts at a uniform point of
+// [-1, 1]^2 with opacity 0, so the restart itself is not drawn.  u * 2 is exact, so the FP32 fma
+// rounds 2u - 1 once, as the shader's mul-then-sub does.  Returns true when it reset.
+__device__ __forceinline__ bool reset_bad_walker(float& x, float& y, float& op, Jsf& rng) {
+    if (!(bad_value(x) || bad_value(y))) return false;
+    const float u1 = randf(rng);
+    const float u2 = randf(rng);
+    x = fmaf(u1, 2.0f, -1.0f);
+    y = fmaf(u2, 2.0f, -1.0f);
+    op = 0.0f;
+    return true;
+}
+
 // flame.glsl:84: min(255, uint(ceil(c * 255.0))); negative or NaN colours index 0.
 __device__ __forceinline__ uint32_t palette_index(float c) {
     const float v = ceilf(__fmul_rn(c, 255.0f));

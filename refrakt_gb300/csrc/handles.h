@@ -40,6 +40,8 @@ struct rf_sim {
     int splat = RF_SPLAT_AUTO;
     const void* spec = nullptr;  // genome-specialised kernel of the warmed flame (specialize.cpp)
     int spec_splat = -1;              // the splat strategy compiled into it (ChaosArgs.splat code)
+    int reset = 0;                    // walker reset of flame.glsl:68 (rf_set_bad_value_reset)
+    int spec_reset = -1;              // the reset setting compiled into the specialised kernel
     std::vector<uint32_t> spec_prog;  // the warmed program, to specialise again for another strategy
     int bin_layout = RF_BINS_AUTO;
     uint32_t rgba_shift = 0, count_shift = 0;  // BinTarget addressing of the next launches
