@@ -7,7 +7,8 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
-REFERENCE = os.environ.get("REFRAKT_REFERENCE", "/root/reference")
+# the reference checkout: $REFRAKT_REFERENCE, else <repo>/../reference (oracle/ref_build.py)
+REFERENCE = os.path.normpath(os.environ.get("REFRAKT_REFERENCE") or os.path.join(ROOT, os.pardir, "reference"))
 
 
 def pytest_configure(config):
