@@ -73,6 +73,42 @@ struct vin {
     vec2 xy() const { return vec2(x, y); }
 };
 
+// ---- what the whole shaders (tonemap.glsl, density_{vert,frag}.glsl, the templates) need
+inline real dot(vec2 a, vec2 b) { return a.x * b.x + a.y * b.y; }
+struct vec3 {
+    real x, y, z;
+    vec3() : x(0), y(0), z(0) {}
+    vec3(real a, real b, real c) : x(a), y(b), z(c) {}
+    explicit vec3(real a) : x(a), y(a), z(a) {}
+};
+inline vec3 operator*(real s, vec3 v) { return vec3(s * v.x, s * v.y, s * v.z); }
+inline vec3 operator*(vec3 v, real s) { return vec3(s * v.x, s * v.y, s * v.z); }
+inline vec3 pow(vec3 a, vec3 b) { return vec3(std::pow(a.x, b.x), std::pow(a.y, b.y), std::pow(a.z, b.z)); }
+inline vec3 mix(vec3 x, vec3 y, real a) { return vec3(mix(x.x, y.x, a), mix(x.y, y.y, a), mix(x.z, y.z, a)); }
+inline vec3 clamp(vec3 v, real lo, real hi) { return vec3(clamp(v.x, lo, hi), clamp(v.y, lo, hi), clamp(v.z, lo, hi)); }
+// vec4 as the shaders use it: .r .g .b .a, .rgb read (rgb()) and written (set_rgb, textual rewrite)
+struct vec4 {
+    real r, g, b, a;
+    vec4() : r(0), g(0), b(0), a(0) {}
+    vec4(real x, real y, real z, real w) : r(x), g(y), b(z), a(w) {}
+    vec4(vec2 v, real z, real w) : r(v.x), g(v.y), b(z), a(w) {}
+    vec3 rgb() const { return vec3(r, g, b); }
+    void set_rgb(vec3 v) { r = v.x; g = v.y; b = v.z; }
+    vec4& operator*=(real s) { r *= s; g *= s; b *= s; a *= s; return *this; }
+};
+inline vec4 operator*(vec4 v, real s) { return vec4(v.r * s, v.g * s, v.b * s, v.a * s); }
+struct uvec2 { uint x, y; };
+struct uvec3 { uint x, y, z; uvec2 xy; };
+struct ivec2 {
+    int x, y;
+    ivec2() : x(0), y(0) {}
+    ivec2(int a, int b) : x(a), y(b) {}
+    explicit ivec2(uvec2 u) : x((int)u.x), y((int)u.y) {}
+};
+// the vertex shader's projection: identity (its output position is not part of the pins)
+struct mat4 {};
+inline vec4 operator*(mat4, vec4 v) { return v; }
+
 }  // namespace glsl
 
 #endif

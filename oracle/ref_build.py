@@ -9,6 +9,15 @@ Compiles, from the sources where they lie in the reference checkout, into oracle
     own macro rules (src/util.cpp:6-9 replace_macro, src/variation_table.cpp:174-180 and
     :107-161): $x -> v.x, $y -> v.y, $v -> v.xy, $weight, parameters, precalcs.
 
+A second library, oracle/_ref/libref_shaders.so (build_shader_pins), compiles the reference's
+whole image shaders and its shader templates the same way:
+  * shaders/tonemap.glsl (the compute shader's main, image load/store stubbed);
+  * shaders/density_vert.glsl and shaders/density_frag.glsl (the point-sprite radius, offset,
+    normalisation and per-fragment kernel weight; projection and rasteriser stubbed);
+  * shaders/templates/xform_select.tpl.glsl and animate.tpl.glsl rendered for given parameter
+    layouts (oracle/inja_lite.py, the inja subset they use), as src/variation_table.cpp:260 and
+    src/flame.cpp:334 render them.
+
 Nothing generated here is committed (oracle/_ref is git-ignored).  Usage:
     python oracle/ref_build.py [reference_dir]
 Exits 0 without building when the reference checkout is absent.
@@ -20,6 +29,13 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
+# The reference checkout: $REFRAKT_REFERENCE, else a directory named `reference` beside this
+# repository's root (<repo>/../reference).
+DEFAULT_REFERENCE = os.path.join(os.path.dirname(HERE), os.pardir, "reference")
+
+
+def reference_dir():
+    return os.path.normpath(os.environ.get("REFRAKT_REFERENCE") or DEFAULT_REFERENCE)
 sys.path.insert(0, HERE)
 import yaml_lite  # noqa: E402
 
@@ -234,8 +250,130 @@ float ref_glsl_randf(uint32_t* st) {
     return "\n".join(out) + "\n", broken
 
 
+# ---------------------------------------------------------------------------------------------
+# whole shaders and shader templates
+# ---------------------------------------------------------------------------------------------
+def shader_to_cpp(src, name, keep_float=False):
+    """A GLSL shader (or rendered template) as C++ over glsl_shim.h: the version line, layout
+    qualifiers, storage-buffer blocks, image and interface declarations removed (the harness
+    declares those globals), `uniform` declarations turned into globals, `discard` into a flag
+    and a return, `.rgb` into the shim's accessors, main() renamed."""
+    s = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    s = re.sub(r"//[^\n]*", "", s)
+    s = re.sub(r"^\s*#version[^\n]*", "", s, flags=re.M)
+    s = re.sub(r"layout\s*\([^)]*\)\s*buffer\s+\w+\s*\{[^}]*\}\s*;", "", s)
+    s = re.sub(r"layout\s*\([^)]*\)\s*in\s*;", "", s)
+    s = re.sub(r"layout\s*\([^)]*\)\s*uniform\s+image2D\s+\w+\s*;", "", s)
+    s = re.sub(r"^\s*(flat\s+)?(in|out)\s+\w+\s+\w+\s*;", "", s, flags=re.M)
+    s = re.sub(r"\buniform\s+", "", s)
+    s = re.sub(r"\bdiscard\s*;", "{ g_discard = true; return; }", s)
+    s = re.sub(r"(\w+)\.rgb\s*=\s*([^;]+);", r"\1.set_rgb(\2);", s)
+    s = re.sub(r"(\w+)\.rgb\b", r"\1.rgb()", s)
+    s = re.sub(r"\bvoid\s+main\s*\(\s*\)", "void %s_main()" % name, s)
+    return glsl_to_cpp(s, keep_float=keep_float)
+
+
+def shader_pins_source(ref, selects, animates):
+    """C++ of the shader pins; `selects` and `animates` are parameter layouts (the reference's
+    buffer_map_ JSON) to render xform_select.tpl.glsl and animate.tpl.glsl with."""
+    import inja_lite
+    rd = lambda p: open(os.path.join(ref, p)).read()
+    out = ["// GENERATED by oracle/ref_build.py from the reference checkout. Do not commit.",
+           '#include "glsl_shim.h"', "#include <cstring>"]
+    # tonemap.glsl
+    out += ["namespace glsl { namespace sh_tonemap {",
+            "static uvec3 gl_GlobalInvocationID{0, 0, 0, {0, 0}};",
+            "static int image_in = 0, image_out = 1; static vec4 g_in, g_out;",
+            "static vec4 imageLoad(int, ivec2) { return g_in; }",
+            "static void imageStore(int, ivec2, vec4 c) { g_out = c; }",
+            shader_to_cpp(rd("shaders/tonemap.glsl"), "tonemap"), "}}"]
+    # density_vert.glsl + density_frag.glsl: the vertex stage's flat outputs are the fragment
+    # stage's inputs (radius, color, offset, norm_factor)
+    out += ["namespace glsl { namespace sh_density {",
+            "static int radius; static vec4 color; static vec2 offset; static real norm_factor;",
+            "static vec4 outColor; static bool g_discard; static vec4 gl_Position; static real gl_PointSize;",
+            "static vec2 gl_PointCoord; static int gl_VertexID = 0; static vec4 bins[1];",
+            shader_to_cpp(rd("shaders/density_vert.glsl"), "vert"),
+            shader_to_cpp(rd("shaders/density_frag.glsl"), "frag"), "}}"]
+    sel_t = rd("shaders/templates/xform_select.tpl.glsl")
+    for k, lay in enumerate(selects):
+        out += ["namespace glsl { namespace sh_select%d { static float fp[4096];" % k,
+                shader_to_cpp(inja_lite.render(sel_t, lay), "select", keep_float=True), "}}"]
+    ani_t = rd("shaders/templates/animate.tpl.glsl")
+    for k, lay in enumerate(animates):
+        out += ["namespace glsl { namespace sh_animate%d {" % k,
+                "static real fp[4096]; static real fp_inflated[1 << 17];",
+                "static uvec3 gl_GlobalInvocationID, gl_NumWorkGroups, gl_WorkGroupSize;",
+                shader_to_cpp(inja_lite.render(ani_t, lay), "animate"), "}}"]
+    out.append('extern "C" {')
+    out.append("""// tonemap.glsl on one pixel (k2 is the shader's scale_constant)
+int ref_tonemap_pixel(const double* in, double gamma, double brightness, double vibrancy, double k2, double* o) {
+    using namespace glsl::sh_tonemap;
+    glsl::sh_tonemap::gamma = gamma; glsl::sh_tonemap::brightness = brightness;
+    glsl::sh_tonemap::vibrancy = vibrancy;
+    scale_constant = k2;
+    g_in = glsl::vec4(in[0], in[1], in[2], in[3]);
+    tonemap_main();
+    o[0] = g_out.r; o[1] = g_out.g; o[2] = g_out.b; o[3] = g_out.a;
+    return 0;
+}
+// density_vert.glsl for one bin of density a: returns 0 when the bin is culled (a == 0)
+int ref_de_vertex(double a, int R, int minr, double curve, int* radius_out, double* norm_out, double* off_out) {
+    using namespace glsl::sh_density;
+    estimator_radius = R; estimator_min = minr; estimator_curve = curve; row_width = 1; height = 1;
+    bins[0] = glsl::vec4(1.0, 1.0, 1.0, a);
+    radius = -1;
+    vert_main();
+    if (radius < 0) return 0;
+    *radius_out = radius; *norm_out = norm_factor; off_out[0] = offset.x; off_out[1] = offset.y;
+    return 1;
+}
+// density_frag.glsl for a sprite of `radius` (bin colour 1, 1, 1, 1) at gl_PointCoord (pcx, pcy)
+// with the vertex stage's offset; returns 0 when the fragment is discarded
+int ref_de_fragment(int r, double nf, double offx, double offy, double pcx, double pcy, double* w) {
+    using namespace glsl::sh_density;
+    radius = r; norm_factor = nf; offset = glsl::vec2(offx, offy); color = glsl::vec4(1.0, 1.0, 1.0, 1.0);
+    gl_PointCoord = glsl::vec2(pcx, pcy); g_discard = false;
+    frag_main();
+    if (g_discard) return 0;
+    *w = outColor.a;
+    return 1;
+}""")
+    for k in range(len(selects)):
+        out.append("""int ref_select_%d(const float* fp, int n, float r) {
+    std::memcpy(glsl::sh_select%d::fp, fp, sizeof(float) * n);
+    return glsl::sh_select%d::get_xform_id(r);
+}""" % (k, k, k))
+    for k in range(len(animates)):
+        out.append("""int ref_animate_%d(const float* fp, int n, int T, int t, float tss_width, float* o) {
+    using namespace glsl::sh_animate%d;
+    for (int i = 0; i < n; i++) glsl::sh_animate%d::fp[i] = fp[i];
+    temporal_sample_width = tss_width;
+    gl_NumWorkGroups = glsl::uvec3{(glsl::uint)(T / 32), 1, 1, {0, 0}};
+    gl_WorkGroupSize = glsl::uvec3{32, 1, 1, {0, 0}};
+    gl_GlobalInvocationID = glsl::uvec3{(glsl::uint)t, 0, 0, {(glsl::uint)t, 0}};
+    animate_main();
+    for (int i = 0; i < n; i++) o[i] = (float)fp_inflated[t * n + i];
+    return 0;
+}""" % (k, k, k))
+    out.append("}")
+    return "\n".join(out) + "\n"
+
+
+def build_shader_pins(ref, selects, animates):
+    """Compiles oracle/_ref/libref_shaders.so for these layouts; returns its path."""
+    os.makedirs(OUT, exist_ok=True)
+    gen = os.path.join(OUT, "ref_shaders.cpp")
+    with open(gen, "w") as f:
+        f.write(shader_pins_source(ref, selects, animates))
+    lib = os.path.join(OUT, "libref_shaders.so")
+    subprocess.run(["g++", "-std=c++20", "-O1", "-fPIC", "-shared", "-w", "-ffp-contract=off", "-I", HERE, gen,
+                    "-o", lib], check=True)
+    return lib
+
+
 def build(ref=None, quiet=False):
-    ref = ref or os.environ.get("REFRAKT_REFERENCE", "/root/reference")
+    ref = ref or reference_dir()
     if not os.path.isfile(os.path.join(ref, "variations.yaml")):
         if not quiet:
             print("ref_build: reference checkout not found at %s; skipping oracle/_ref" % ref)
