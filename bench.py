@@ -3,9 +3,16 @@
 with 8 xforms plus a final xform; adaptive DE radius 9, min 0, curve 0.4; log-density tonemap).
 
 A step is one frame: warmup (20 discarded passes), the chaos game over all walkers until the
-frame's points are drawn, density estimation, tonemap.  `value` is points per second with the
-genome and all buffers resident in HBM; `e2e` is the same frame through the C ABI's rf_render
-from a host genome to a pinned host RGBA8 image (upload and read-back inside the timed region).
+frame's points are drawn, density estimation, tonemap.  A point is one post-fuse walker-step;
+`binned_gpoints_s` counts the points that land in the frame.  Walkers that leave the plane
+(NaN / beyond 1e10) restart, as the reference's commented-out reset at flame.glsl:68 would do
+(--no-badval-reset keeps the reference's default, where they stay lost and over the frame's
+3,331 passes most of them stop drawing).  `value` is points per second with the genome and all
+buffers resident in HBM; `e2e` is the same frame through the C ABI's rf_render from a host
+genome to a pinned host RGBA8 image (upload and read-back inside the timed region).
+
+Genomes come from tests/golden/genomes/ (written once by tests/golden/make_genomes.py from the
+library's seeded synthesiser), so the reference arm reads the same genome without the library.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
 
@@ -32,21 +39,26 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     "frame1080": dict(name="plain 1080p frame, supersample 2 (3840x2160 bins), 1000 points/bin, DE r9 c0.4",
                       genome=dict(kind=1, seed=1, n_xforms=8, final_xform=True, force_parametric=True),
+                      genome_file="frame1080.flam3",
                       out=(1920, 1080), ss=2, points=1000 * 3840 * 2160, de=(9, 0, 0.4), image=True),
     "small": dict(name="small genome (seed 0, 3 xforms), 512x512 bins, 65,536 walkers x 256 passes",
                   genome=dict(kind=0, seed=0, n_xforms=0, final_xform=False, force_parametric=False),
+                  genome_file="small.flam3",
                   out=(512, 512), ss=1, points=65536 * 256, de=None, image=True, walkers=65536,
                   cta_slots=2048),  # 65,536 walkers fill only 16 CTAs of 4096 slots
     "contract": dict(name="contracting genome (seed 4, 6 xforms), 1920x1080 bins, 2^34 points",
                      genome=dict(kind=2, seed=4, n_xforms=0, final_xform=False, force_parametric=False),
+                     genome_file="contract.flam3",
                      out=(1920, 1080), ss=1, points=2 ** 34, de=None, image=False),
     "spacefill": dict(name="space-filling genome (seed 5, 16 xforms), 8192x8192 bins, 2^34 points",
                       genome=dict(kind=3, seed=5, n_xforms=0, final_xform=False, force_parametric=False),
+                      genome_file="spacefill.flam3",
                       out=(4096, 4096), ss=2, points=2 ** 34, de=None, image=False),
     "batch": dict(name="batched animation: 120 frames interpolated seed 2 (4 xforms) -> seed 3 (10 xforms) at "
                        "1024x768 + 64 random genomes (2-16 xforms) at 512x512 / 1024x768 / 1920x1080, 200 spp, "
                        "one persistent graph-captured launch",
-                  genome=None, out=(1024, 768), ss=1, points=None, de=(9, 0, 0.4), image=True),
+                  genome=None, genome_file="batch_frame0.flam3",
+                  out=(1024, 768), ss=1, points=None, de=(9, 0, 0.4), image=True),
     "gemm": dict(name="tcgen05 BF16 GEMM of the learned density estimator: 8192^3 (FP32 accumulation) and the "
                       "U-Net's largest convolution (1,048,576 x 32 x 720) as a GEMM and as an implicit GEMM",
                  genome=None, out=(512, 512), ss=1, points=None, de=None, image=False),
@@ -56,6 +68,9 @@ WORKLOADS = {
                     genome=None, out=(1920, 1080), ss=1, points=None, de=(9, 0, 0.4), image=True),
 }
 FUSE = 20
+GENOME_DIR = os.path.join(ROOT, "tests", "golden", "genomes")
+BATCH_SIZES = [(512, 512), (1024, 768), (1920, 1080)]
+BATCH_POINTS = 120 * 200 * 1024 * 768 + sum(200 * BATCH_SIZES[k % 3][0] * BATCH_SIZES[k % 3][1] for k in range(64))
 WL = WORKLOADS["frame1080"]
 W_OUT, H_OUT = WL["out"]
 SS = WL["ss"]
@@ -76,6 +91,29 @@ def select_workload(key):
     DE = WL["de"]
     GENOME = WL["genome"]
     CONFIG_NAME = WL["name"]
+
+
+def genome_xml():
+    """The workload's genome (flam3 XML) as committed under tests/golden/genomes/."""
+    with open(os.path.join(GENOME_DIR, WL["genome_file"])) as f:
+        return f.read()
+
+
+def workload_config(reset):
+    """The workload's definition — identical in the native and the reference arm's line (what
+    each run chose at run time goes to the line's `launch`)."""
+    if WL["genome"] is None:  # the batched animation
+        return {"workload": CONFIG_NAME, "images": 184, "requested_points": BATCH_POINTS,
+                "genome_file": WL["genome_file"], "density_estimation": list(DE), "fuse_passes": FUSE,
+                "bad_value_reset": bool(reset),
+                "l2": "%.1f GB of bins per batch (L2 129 MB)" %
+                      ((120 * 1024 * 768 + sum(BATCH_SIZES[k % 3][0] * BATCH_SIZES[k % 3][1] for k in range(64)))
+                       * 20 / 1e9)}
+    return {"workload": CONFIG_NAME, "genome": GENOME, "genome_file": WL["genome_file"], "points_per_frame": POINTS,
+            "bins": [W, H], "output": [W_OUT, H_OUT], "fuse_passes": FUSE,
+            "density_estimation": list(DE) if DE else None, "bad_value_reset": bool(reset),
+            "l2": "bins %dx%d x 20 B = %.0f MB (L2 129 MB)%s" % (
+                W, H, W * H * 20 / 1e6, "; exceed L2" if W * H * 20 > 129e6 else "; an L2 flush separates frames")}
 
 
 def _dist():
@@ -178,16 +216,90 @@ def _profile_figure(workload, key, summary="chaos_kernel_%s.md"):
         return None
 
 
+def kernel_build_id(flame):
+    """Identifies the chaos kernel a run launches: a hash of the genome-specialised kernel's
+    generated source and the device headers it is compiled from.  The committed ncu summary
+    records the id of the build it captured; bench.py uses its figures only when they match."""
+    import hashlib
+    sys.path.insert(0, os.path.join(ROOT, "refrakt_gb300"))
+    from nvbuild import RTC_HEADERS
+    h = hashlib.sha256(flame.kernel_source().encode())
+    for name in RTC_HEADERS + ["chaos_body.cuh"]:
+        with open(os.path.join(ROOT, "refrakt_gb300", "csrc", name), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def _profile_build(workload):
+    """The kernel build id recorded in the committed ncu summary of this workload (or None)."""
+    import re
+    try:
+        with open(os.path.join(ROOT, "profiles", "chaos_kernel_%s.md" % workload)) as f:
+            m = re.search(r"^kernel build: ([0-9a-f]+)", f.read(), re.M)
+        return m.group(1) if m else None
+    except OSError:
+        return None
+
+
+# FP32 operation counts of one evaluation of each variation, from its formula in variations.yaml
+# (tests/golden/reference_vectors.json: `libm_calls` = sin, cos, pow, exp, log, atan, sqrt ...
+# calls incl. the precalcs it uses; `arith_ops` = +, -, *, / and fused forms in its text).
+def _variation_costs():
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "reference_vectors.json")) as f:
+            g = json.load(f)
+        return g.get("libm_calls", {}), g.get("arith_ops", {})
+    except OSError:
+        return {}, {}
+
+
+def algorithmic_ops_per_point(xml):
+    """Expected FP32 arithmetic operations and library (transcendental) calls per point of a
+    genome: each xform's affine (4 FMA), its variations' formulas (weighted by the xform's
+    selection probability), colour blend (3), the final xform when present, and the screen
+    affine (4 FMA).  Counted from the formulas, not from any implementation."""
+    import xml.etree.ElementTree as ET
+    libm, arith = _variation_costs()
+    root = ET.fromstring(xml)
+    if root.tag != "flame":
+        root = root.find("flame")
+    xfs = root.findall("xform")
+    fin = root.find("finalxform")
+    tw = sum(float(x.get("weight", "0")) for x in xfs) or 1.0
+
+    def cost(x):
+        ops, calls = 4.0 + 3.0, 0.0
+        for name, val in x.attrib.items():
+            if name in libm and float(val) != 0.0:
+                calls += libm[name]
+                ops += arith.get(name, 0) + 2  # weight multiply and accumulate
+        if x.get("post"):
+            ops += 4
+        return ops, calls
+
+    ops = calls = 0.0
+    for x in xfs:
+        o, c = cost(x)
+        p = float(x.get("weight", "0")) / tw
+        ops += p * o
+        calls += p * c
+    if fin is not None:
+        o, c = cost(fin)
+        ops += o
+        calls += c
+    return ops + 4.0, calls
+
+
 def _traffic(workload):
     """DRAM bytes per chaos launch from the committed ncu summary of this workload (or None)."""
     v = _profile_figure(workload, "dram bytes per launch")
     return int(v) if v is not None else None
 
 
-def cpu_baseline(genome_xml, seconds=12.0, threads=None):
+def cpu_baseline(genome_xml, seconds=12.0, threads=None, reset=True):
     """The oracle's FP32 transcription of flame.glsl's draw pass on the host cores, on a bounded
-    sample of this workload (same genome, same bin grid): returns (Gpoints/s, threads, sample
-    description, seconds timed)."""
+    sample of this workload (same genome, same bin grid, same walker reset): returns (Gpoints/s,
+    threads, sample description, seconds timed, binned Gpoints/s)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
@@ -195,43 +307,46 @@ def cpu_baseline(genome_xml, seconds=12.0, threads=None):
     threads = threads or os.cpu_count() or 1
     walkers = 256 * 64 * threads
     t0 = time.perf_counter()
-    n, _, _ = g.cpu_baseline(walkers, 2, W, H, threads)
+    n, _, _ = g.cpu_baseline(walkers, 2, W, H, threads, badval_reset=reset)
     rate = n / max(time.perf_counter() - t0, 1e-6)
     passes = max(2, int(seconds * rate / walkers))
     t0 = time.perf_counter()
-    n, _, _ = g.cpu_baseline(walkers, passes, W, H, threads)
+    n, _, _, nb = g.cpu_baseline(walkers, passes, W, H, threads, badval_reset=reset, binned=True)
     dt = time.perf_counter() - t0
-    sample = "%d walkers x %d passes = %.3g points of the frame's %.3g, %dx%d bins" % (walkers, passes, n, POINTS, W, H)
-    return n / dt / 1e9, threads, sample, dt
+    points = POINTS or BATCH_POINTS
+    sample = "%d walkers x %d passes = %.3g points of the workload's %.3g, %dx%d bins" % (
+        walkers, passes, n, points, W, H)
+    return n / dt / 1e9, threads, sample, dt, nb / dt / 1e9
 
 
 def run_reference(args):
+    """The reference's path on the host cores (the oracle's FP32 port of flame.glsl's iteration;
+    the reference has no CPU path of its own), on the same genome file and bin grid as the native
+    arm.  Each step times one bounded sample of the workload; ms_per_step is that sample's time."""
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
-    import refrakt_gb300 as R
-    R.build()
-    comp = R.FlameCompiler()
-    if GENOME is None:  # batched workload: the first animation frame stands for the batch
-        xml = batch_items(R, comp)[0][0].to_xml()
-    else:
-        xml = R.Flame.synthesize(comp, GENOME["kind"], GENOME["seed"], W, H, n_xforms=GENOME["n_xforms"],
-                                 final_xform=GENOME["final_xform"],
-                                 force_parametric=GENOME["force_parametric"]).to_xml()
-    points = POINTS or 200 * 1024 * 768
-    vals = []
+    xml = genome_xml()
+    reset = not args.no_badval_reset
+    vals, binned, dts = [], [], []
     last = None
     for i in range(args.warmup + args.steps):
-        v, thr, sample, dt = cpu_baseline(xml, seconds=max(3.0, 30.0 / (args.warmup + args.steps)))
+        v, thr, sample, dt, vb = cpu_baseline(xml, seconds=max(3.0, 30.0 / (args.warmup + args.steps)), reset=reset)
         if i >= args.warmup:
             vals.append(v)
+            binned.append(vb)
+            dts.append(dt)
         last = (thr, sample)
     v = statistics.median(vals)
+    points = POINTS or BATCH_POINTS
     line = {"metric": "Gpoints/s histogrammed", "value": v, "unit": "Gpoints/s", "impl": "reference",
-            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": points / (v * 1e9) * 1e3,
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(dts) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic genome (seed %d); no dataset" % (GENOME["seed"] if GENOME else 2),
-            "config": {"workload": CONFIG_NAME, "points_per_frame": points, "bins": [W, H], "genome": GENOME},
+            "data": "synthetic genome (%s); no dataset" % WL["genome_file"],
+            "config": workload_config(reset),
+            "binned_gpoints_s": statistics.median(binned),
+            "step": "one bounded sample of the workload per step (%s); the whole workload would take %.1f s "
+                    "at this rate" % (last[1], points / (v * 1e9)),
             "cpu_baseline": {"value": v, "unit": "Gpoints/s", "cores": last[0], "kind": "port", "sample": last[1]},
             "e2e": {"value": v, "unit": "Gpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -250,10 +365,10 @@ def run_native(args):
     torch.cuda.set_device(local)
     R.build()
     comp = R.FlameCompiler()
-    flame = R.Flame.synthesize(comp, GENOME["kind"], GENOME["seed"], W, H, n_xforms=GENOME["n_xforms"],
-                               final_xform=GENOME["final_xform"], force_parametric=GENOME["force_parametric"])
-    xml = flame.to_xml()
+    xml = genome_xml()
+    flame = R.Flame.from_xml(xml, comp)
     info = flame.info()
+    reset = not args.no_badval_reset
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     cta = args.cta_slots or WL.get("cta_slots", 4096)
     walkers = WL.get("walkers") or sms * args.ctas_per_sm * cta
@@ -268,6 +383,7 @@ def run_native(args):
     stream = torch.cuda.current_stream()
     sim.set_stream(stream)
     sim.set_splat({"auto": R.SPLAT_AUTO, "global": R.SPLAT_GLOBAL, "warp": R.SPLAT_WARP}[args.splat])
+    sim.set_bad_value_reset(reset)
 
     # bins smaller than the 129 MB L2: write a 256 MB buffer before every frame
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda") if W * H * 20 <= 129e6 else None
@@ -326,10 +442,9 @@ def run_native(args):
         de_ms = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps
         tm_ms = sum(e[2].elapsed_time(e[3]) for e in evs) / args.steps
         nb = W * H
-        # algorithmic bytes: DE radius pass 16 B read + 1 B write, gather/scatter pass 16 B read +
-        # 1 B radius read + 16 B write per bin; stats 16 B read per bin (FP64 reduction) + tonemap
-        # 16 B read per bin + 4 B write per output pixel
-        de_bytes = nb * (16 + 1 + 16 + 1 + 16) if DE else 0
+        # algorithmic bytes: DE 16 B read + 16 B write per bin (radii are intermediate); the
+        # FP64 statistics and the tonemap read 16 B per bin each and write 4 B per output pixel
+        de_bytes = nb * 32 if DE else 0
         tm_bytes = nb * 16 + nb * 16 + W_OUT * H_OUT * 4
         peak_, _ = _peaks()
         image_passes = {"de_ms": de_ms if DE else 0.0, "de_bytes": de_bytes,
@@ -359,52 +474,66 @@ def run_native(args):
     h2d = prog_bytes + 256 * 16
     d2h = W_OUT * H_OUT * 4
 
+    # roofline of the chaos kernel (per launch of steps_per_launch passes)
     peak, peak_kind = _peaks()
+    clk_sum = clk.summary()
+    clk_mhz = clk_sum.get("sm_mhz") or 2070.0
     per_launch_ms = draw_ms / launches
-    bytes_per_point = 20  # payload of the histogram reductions: float4 RGBA + uint32 count
     pts_per_launch = walkers * args.steps_per_launch
-    achieved = bytes_per_point * pts_per_launch / (per_launch_ms * 1e-3) / 1e9
+    pts_s = pts_per_launch / (per_launch_ms * 1e-3)
     prof_key = {"frame1080": "1080p"}.get(args.workload, args.workload)
-    traffic = _traffic(prof_key) if sim.specialized() else None
-    inst = _profile_figure(prof_key, "warp instructions per point") if sim.specialized() else None
-    sms_ = torch.cuda.get_device_properties(local).multi_processor_count
-    issue = None
-    if inst:
-        clk_mhz = (clk.summary() or {}).get("sm_mhz") or 2070.0
-        bound = sms_ * 4 * clk_mhz * 1e6 / inst / 1e9  # Gpoints/s at one warp instruction per scheduler-cycle
-        issue = {"warp_inst_per_point": inst, "bound_gpoints_s": bound,
-                 "frac": (pts_per_launch / (per_launch_ms * 1e-3) / 1e9) / bound}
+    build = kernel_build_id(flame) if sim.specialized() else None
+    same_build = build is not None and build == _profile_build(prof_key)
+    inst = _profile_figure(prof_key, "warp instructions per point") if same_build else None
+    traffic = _traffic(prof_key) if same_build else None
+    issue_bound = sms * 4 * clk_mhz * 1e6 / inst if inst else None  # points/s at one warp-inst per SMSP-cycle
+    payload = 20.0 * binned_fraction  # float4 RGBA + u32 count reduced per binned point
+    ops, calls = algorithmic_ops_per_point(xml)
+    fp32_rate = sms * 128 * clk_mhz * 1e6  # FP32 lane operations per second (FMA = one)
+    xu_rate = sms * 16 * clk_mhz * 1e6     # transcendental (XU) operations per second
+    alg_bound = min(fp32_rate / ops, xu_rate / calls if calls else float("inf"))
+    roofline = {
+        "bound": "issue", "kernel": "rfk_chaos_spec" if sim.specialized() else "chaos_kernel",
+        "achieved": pts_s / 1e9, "peak": issue_bound / 1e9 if issue_bound else None, "unit": "Gpoints/s",
+        "frac": pts_s / issue_bound if issue_bound else None, "traffic": traffic,
+        "peak_source": "152 SMs x 4 schedulers x %.0f MHz / %s warp instructions per point (ncu, same kernel "
+                       "build %s)" % (clk_mhz, inst, build) if inst else
+                       "no ncu summary of this kernel build (%s)" % build,
+        "points_per_launch": pts_per_launch, "launch_ms": per_launch_ms,
+        "l2_reduction": {"bytes_per_point": payload, "gbs": payload * pts_s / 1e9,
+                         "note": "20 B (float4 RGBA + u32 count) per binned point"},
+        "hbm": {"achieved": (traffic / (per_launch_ms * 1e-3) / 1e9) if traffic else None, "peak": peak,
+                "unit": "GB/s", "peak_source": peak_kind},
+        "algorithmic": {"fp32_ops_per_point": ops, "library_calls_per_point": calls,
+                        "bound_gpoints_s": alg_bound / 1e9, "frac": pts_s / alg_bound,
+                        "note": "operations of the genome's formulas (variations.yaml) against %d FP32 lanes and "
+                                "16 XU lanes per SM; a library call counted as one XU operation" % 128},
+    }
     line = {
         "metric": "Gpoints/s histogrammed", "value": value, "unit": "Gpoints/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic genome (seed %d); no dataset" % GENOME["seed"],
-        "config": {"workload": CONFIG_NAME, "points_per_frame": POINTS, "bins": [W, H], "output": [W_OUT, H_OUT],
-                   "genome": GENOME, "walkers": walkers, "cta_slots": cta, "steps_per_launch": args.steps_per_launch,
-                   "passes_per_frame": passes, "fuse_passes": FUSE, "splat": args.splat,
-                   "specialized_kernel": sim.specialized(),
-                   "first_warmup_s": first_warmup_s, "density_estimation": list(DE) if DE else None,
-                   "l2": "bins %dx%d x 20 B = %.0f MB (L2 129 MB)%s" % (W, H, W * H * 20 / 1e6,
-                         "; exceed L2" if W * H * 20 > 129e6 else "; an L2 flush separates frames"),
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic genome (%s); no dataset" % WL["genome_file"],
+        "config": workload_config(reset),
+        "launch": {"walkers": walkers, "cta_slots": cta, "steps_per_launch": args.steps_per_launch,
+                   "passes_per_frame": passes, "splat": args.splat, "specialized_kernel": sim.specialized(),
+                   "kernel_build": build, "first_warmup_s": first_warmup_s,
                    "parallelism": "replicas" if ws > 1 else "single"},
         "s_per_frame": ms_step / 1e3,
         "draw_ms_per_frame": draw_ms,
         "binned_fraction": binned_fraction,
+        "binned_gpoints_s": value * binned_fraction,
         "image_passes": image_passes,
         "gpu_launches": (launches + (FUSE + args.steps_per_launch - 1) // args.steps_per_launch + 4) * args.steps,
         "e2e": {"value": e2e_value, "unit": "Gpoints/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "s_per_frame": e2e_step / 1e3},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "rfk_chaos_spec" if sim.specialized() else "chaos_kernel", "peak_source": peak_kind,
-                     "algorithmic_bytes_per_point": bytes_per_point, "points_per_launch": pts_per_launch,
-                     "launch_ms": per_launch_ms, "issue": issue,
-                     "note": "atomic-reduction payload per point; the chaos game is bound by SM issue and L2 "
-                             "reduction throughput, not DRAM"},
-        "clocks": clk.summary(),
+                "s_per_frame": e2e_step / 1e3, "binned_gpoints_s": st["binned"] / (statistics.median(e2e_ms) * 1e-3) / 1e9},
+        "roofline": roofline,
+        "clocks": clk_sum,
     }
     if rank == 0:
         if ws == 1 and not args.no_cpu_baseline and args.workload == "frame1080":
-            v, thr, sample, _ = cpu_baseline(xml)
-            line["cpu_baseline"] = {"value": v, "unit": "Gpoints/s", "cores": thr, "kind": "port", "sample": sample}
+            v, thr, sample, _, vb = cpu_baseline(xml, reset=reset)
+            line["cpu_baseline"] = {"value": v, "unit": "Gpoints/s", "cores": thr, "kind": "port", "sample": sample,
+                                    "binned_gpoints_s": vb}
         print(json.dumps(line))
     sim.close()
     if ws > 1:
@@ -444,7 +573,8 @@ def run_batch(args):
         f.set_estimator(*DE)
     points = sum(it[3] for it in items)
     n_img = len(items)
-    b = R.Batch(items, fuse_passes=FUSE, density_estimation=True, device=local)
+    reset = not args.no_badval_reset
+    b = R.Batch(items, fuse_passes=FUSE, density_estimation=True, device=local, bad_value_reset=reset)
     info = b.info()
     spec_groups = len({items[i][0].kernel_source() for i, sp in enumerate(info["specialized"]) if sp})
 
@@ -480,7 +610,7 @@ def run_batch(args):
         barrier()
         t_a = time.perf_counter()
         fl = [(R.Flame.from_xml(x, comp), w, h, p, s) for x, w, h, p, s in xmls]
-        bb = R.Batch(fl, fuse_passes=FUSE, density_estimation=True, device=local)
+        bb = R.Batch(fl, fuse_passes=FUSE, density_estimation=True, device=local, bad_value_reset=reset)
         bb.run()
         for k in range(n_img):
             bb.image(k, outs[k])
@@ -495,13 +625,12 @@ def run_batch(args):
         "metric": "Gpoints/s histogrammed", "value": value, "unit": "Gpoints/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic genomes (seeds 2, 3, 100-163); no dataset",
-        "config": {"workload": CONFIG_NAME, "images": n_img, "points_per_batch": st["points"],
-                   "requested_points": points, "density_estimation": list(DE), "fuse_passes": FUSE,
-                   "autotuned": info, "l2": "%.1f GB of bins per batch (L2 129 MB)" %
-                   (sum(w * h * 20 for _, w, h, *_ in items) / 1e9),
-                   "parallelism": "replicas" if ws > 1 else "single"},
+        "config": workload_config(reset),
+        "launch": {"images": n_img, "points_per_batch": st["points"], "requested_points": points,
+                   "autotuned": info, "parallelism": "replicas" if ws > 1 else "single"},
         "frames_per_s": n_img / (ms_step * 1e-3),
         "binned_fraction": st["binned"] / st["points"],
+        "binned_gpoints_s": value * st["binned"] / st["points"],
         "wall_ms_per_step": wall / args.steps,
         # per batch: the persistent chaos launches (one per specialised structure group + the
         # interpreted one) and per image DE radius + DE gather + FP64 stats + tonemap
@@ -753,6 +882,8 @@ def main():
     ap.add_argument("--ctas-per-sm", type=int, default=4)
     ap.add_argument("--steps-per-launch", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-badval-reset", action="store_true",
+                    help="keep walkers that leave the plane lost (the reference's default, flame.glsl:68)")
     ap.add_argument("--splat", default="auto", choices=["auto", "global", "warp"])
     ap.add_argument("--specialize", default="auto", choices=["auto", "on", "off"],
                     help="genome-specialised chaos kernel compiled at run time")

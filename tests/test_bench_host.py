@@ -2,6 +2,9 @@
 the clock-sample summary, workload selection, the oracle CPU baseline on a bounded sample, and the
 reference arm's JSON line (every key of the line contract)."""
 import json
+import os
+import subprocess
+import sys
 import types
 
 import pytest
@@ -45,16 +48,16 @@ def test_select_workload_sets_the_config():
     assert (bench.W, bench.H) == (3840, 2160) and bench.POINTS == 1000 * 3840 * 2160
 
 
-def test_cpu_baseline_bounded_sample(rk, compiler, small_workload):
-    xml = rk.Flame.synthesize(compiler, 0, 0, bench.W, bench.H).to_xml()
-    v, threads, sample, dt = bench.cpu_baseline(xml, seconds=0.2, threads=2)
-    assert v > 0 and threads == 2 and "walkers" in sample and 0 < dt < 30
+def test_cpu_baseline_bounded_sample(small_workload):
+    v, threads, sample, dt, vb = bench.cpu_baseline(bench.genome_xml(), seconds=0.2, threads=2)
+    assert v > 0 and threads == 2 and "walkers" in sample and 0 < dt < 30 and 0 < vb <= v
 
 
-def test_reference_arm_line(rk, monkeypatch, capsys, small_workload):
+def test_reference_arm_line(monkeypatch, capsys, small_workload):
     # the timed oracle sample is stubbed: this checks the line, not the oracle's speed
-    monkeypatch.setattr(bench, "cpu_baseline", lambda xml, seconds=0, threads=None: (0.05, 4, "stub sample", 1.0))
-    assert bench.run_reference(types.SimpleNamespace(steps=2, warmup=1)) == 0
+    monkeypatch.setattr(bench, "cpu_baseline",
+                        lambda xml, seconds=0, threads=None, reset=True: (0.05, 4, "stub sample", 1.5, 0.04))
+    assert bench.run_reference(types.SimpleNamespace(steps=2, warmup=1, no_badval_reset=False)) == 0
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
               "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
@@ -63,5 +66,38 @@ def test_reference_arm_line(rk, monkeypatch, capsys, small_workload):
     assert line["cpu_baseline"] == {"value": 0.05, "unit": "Gpoints/s", "cores": 4, "kind": "port",
                                     "sample": "stub sample"}
     assert line["e2e"] == {"value": 0.05, "unit": "Gpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
-    assert line["config"]["workload"] == bench.WORKLOADS["small"]["name"] and "seed 0" in line["data"]
-    assert line["ms_per_step"] == pytest.approx(65536 * 256 / 0.05e9 * 1e3)
+    # the same workload definition as the native arm's line, read from the same genome file
+    assert line["config"] == bench.workload_config(True)
+    assert line["config"]["workload"] == bench.WORKLOADS["small"]["name"] and "small.flam3" in line["data"]
+    assert line["ms_per_step"] == pytest.approx(1500.0) and line["binned_gpoints_s"] == 0.04
+
+
+def test_reference_arm_does_not_load_the_library(tmp_path):
+    """The reference arm runs the oracle only: it never imports the product package."""
+    code = ("import sys, types, bench\n"
+            "bench.select_workload('small')\n"
+            "bench.cpu_baseline = lambda xml, seconds=0, threads=None, reset=True: (0.05, 1, 's', 1.0, 0.04)\n"
+            "bench.run_reference(types.SimpleNamespace(steps=1, warmup=0, no_badval_reset=False))\n"
+            "assert 'refrakt_gb300' not in sys.modules, 'product package imported'\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=bench.ROOT, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+
+
+def test_genome_fixtures_match_the_synthesiser(rk, compiler):
+    """tests/golden/genomes/ holds what the library's seeded synthesiser writes (make_genomes.py)."""
+    sys.path.insert(0, os.path.join(bench.ROOT, "tests", "golden"))
+    import make_genomes
+    for name, xml in make_genomes.synthesize_all(rk, compiler).items():
+        with open(os.path.join(bench.GENOME_DIR, name + ".flam3")) as f:
+            assert f.read() == xml, name
+
+
+def test_algorithmic_operation_count():
+    bench.select_workload("frame1080")
+    ops, calls = bench.algorithmic_ops_per_point(bench.genome_xml())
+    # affine, colour and screen affine alone are 11 operations; julian / ngon / pdj call pow,
+    # atan2, sin, cos
+    assert 20 < ops < 200 and 1 < calls < 30
+    small_ops, small_calls = bench.algorithmic_ops_per_point(
+        '<flame size="8 8" scale="1"><xform weight="1" color="0" coefs="1 0 0 1 0 0" linear="1"/></flame>')
+    assert small_calls == 0 and small_ops == 4 + 3 + 2 + 4
