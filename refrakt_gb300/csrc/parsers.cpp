@@ -253,6 +253,24 @@ struct XReader {
 
 }  // namespace
 
+// FNV-1a over a variation's src and result text with whitespace left out (so re-indented or
+// re-wrapped YAML hashes alike), the two parts separated by 0x1f.
+uint64_t snippet_hash(const std::string& src, const std::string& result) {
+    uint64_t h = 1469598103934665603ull;
+    auto feed = [&](const std::string& s) {
+        for (unsigned char ch : s) {
+            if (std::isspace(ch)) continue;
+            h ^= ch;
+            h *= 1099511628211ull;
+        }
+    };
+    feed(src);
+    h ^= 0x1f;
+    h *= 1099511628211ull;
+    feed(result);
+    return h;
+}
+
 bool parse_yaml(const std::string& text, YNode& out, std::string& err) {
     YReader r;
     size_t p = 0;

@@ -150,18 +150,7 @@ std::shared_ptr<const Registry> builtin_registry() {
 }
 
 // FNV-1a over the snippet texts (src, a 0x1f separator, result) as a YAML reader returns them.
-uint64_t snippet_hash(const std::string& src, const std::string& result) {
-    uint64_t h = 1469598103934665603ull;
-    auto feed = [&](const std::string& s) {
-        for (unsigned char ch : s) { h ^= ch; h *= 1099511628211ull; }
-    };
-    feed(src);
-    h ^= 0x1f; h *= 1099511628211ull;
-    feed(result);
-    return h;
-}
-
-// Hashes of the reference's snippets, filled in by snippet_hashes.cpp.
+// Hashes of the reference's snippets (snippet_hashes.cpp, generated by gen_snippet_hashes.py).
 const std::map<std::string, uint64_t>& builtin_snippet_hashes();
 
 int load_registry_yaml(const std::string& path, std::shared_ptr<const Registry>& out) {
@@ -203,7 +192,7 @@ int load_registry_yaml(const std::string& path, std::shared_ptr<const Registry>&
             uint64_t h = snippet_hash(src, res);
             if (d.params != it->second->params || d.flags != it->second->flags) {
                 d.note = "parameters or flags of `" + name + "` differ from the device implementation";
-            } else if (hv != hashes.end() && hv->second != h) {
+            } else if (hv == hashes.end() || hv->second != h) {
                 d.note = "snippet of `" + name + "` differs from the one the device code implements";
             } else {
                 d.kernel_id = it->second->kernel_id;

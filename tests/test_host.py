@@ -4,6 +4,7 @@ parameter buffer and layout, the screen affine, synthetic genomes, PNG output.""
 import os
 import re
 import struct
+import sys
 import zlib
 
 import numpy as np
@@ -73,6 +74,50 @@ def test_yaml_reconciliation(rk, tmp_path):
     with pytest.raises(rk.RefraktError) as e:
         rk.Flame.from_xml(xml, c)
     assert e.value.status == 4  # UNSUPPORTED
+
+
+def test_yaml_snippet_text_must_be_the_reference_formula(rk, tmp_path):
+    """The kernels implement the reference's formulas, so a caller's entry is evaluated only when
+    its snippet is the reference's text (whitespace aside); an edited body is unsupported
+    (flame_compiler generates code from whatever the file says, variation_table.cpp:182-215)."""
+    y = tmp_path / "v.yaml"
+    y.write_text("variations:\n"
+                 "  linear:\n    result: |-\n      (  $v\n      )\n"            # re-wrapped: the same formula
+                 "  spherical:\n    result: $v * ($rsq + EPS)\n")                # edited
+    c = rk.FlameCompiler(str(y))
+    assert c.is_supported("linear")
+    assert c.is_variation("spherical") and not c.is_supported("spherical")
+    xml = '<flame size="8 8" scale="1"><xform weight="1" color="0" color_speed="0" opacity="1" coefs="1 0 0 1 0 0" spherical="1"/></flame>'
+    with pytest.raises(rk.RefraktError) as e:
+        rk.Flame.from_xml(xml, c)
+    assert e.value.status == 4  # UNSUPPORTED
+
+
+@pytest.mark.skipif(reference_file("variations.yaml") is None, reason="reference checkout absent")
+def test_edited_reference_yaml_disables_only_the_edited_variation(rk, tmp_path):
+    text = open(os.path.join(REFERENCE, "variations.yaml")).read()
+    edited = text.replace("    result: $v / ($rsq + EPS)\n", "    result: $v / ($rsq + 2.0 * EPS)\n", 1)
+    assert edited != text
+    y = tmp_path / "variations.yaml"
+    y.write_text(edited)
+    c = rk.FlameCompiler(str(y))
+    assert not c.is_supported("spherical")
+    assert sum(c.is_supported(v) for v in c.variations()) == 67
+
+
+@pytest.mark.skipif(reference_file("variations.yaml") is None, reason="reference checkout absent")
+def test_snippet_hash_table_is_current():
+    """refrakt_gb300/csrc/snippet_hashes.cpp holds the hashes gen_snippet_hashes.py computes from
+    the reference's variations.yaml."""
+    import re
+    sys.path.insert(0, os.path.join(ROOT, "refrakt_gb300"))
+    import gen_snippet_hashes
+    h = gen_snippet_hashes.hashes(os.path.join(REFERENCE, "variations.yaml"))
+    with open(os.path.join(ROOT, "refrakt_gb300", "csrc", "snippet_hashes.cpp")) as f:
+        table = dict(re.findall(r'\{"(\w+)", 0x([0-9a-f]+)ull\}', f.read()))
+    assert len(table) == 68
+    for name, v in table.items():
+        assert h[name] == v, name
 
 
 def test_yaml_errors(rk, tmp_path):
@@ -227,9 +272,9 @@ def test_png_writer(rk, tmp_path):
     assert np.array_equal(np.frombuffer(b"".join(rows), np.uint8).reshape(5, 7, 4), img)
 
 
-@pytest.mark.skipif(reference_file("flames", "electricsheep.247.11256.flam3") is None, reason="reference checkout absent")
 def test_reference_fixture_genome(rk, orc, compiler):
-    path = reference_file("flames", "electricsheep.247.11256.flam3")
+    # the reference's flames/electricsheep.247.11256.flam3, copied by tests/golden/make_genomes.py
+    path = os.path.join(ROOT, "tests", "golden", "genomes", "electricsheep.247.11256.flam3")
     f = rk.Flame.load_flame(path, compiler)
     with open(path) as fh:
         o = orc.Genome(fh.read())
