@@ -378,7 +378,6 @@ def run_native(args):
     launches = (passes + args.steps_per_launch - 1) // args.steps_per_launch
     bins = torch.zeros(H, W, 4, device="cuda")
     hits = torch.zeros(H, W, dtype=torch.int32, device="cuda")
-    de = torch.zeros_like(bins) if DE else None
     img = torch.zeros(H_OUT, W_OUT, 4, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
     sim.set_stream(stream)
@@ -401,15 +400,14 @@ def run_native(args):
             ev[1].record(stream)
         if not WL["image"]:
             return
-        src = bins
-        if DE:
-            R.density_estimate(bins, W, H, DE[0], DE[1], DE[2], de, stream=stream)
-            src = de
+        if DE:  # main.cpp:490-535 in one call: the estimator's tiles are tonemapped on chip
+            R.density_tonemap(bins, W, H, DE[0], DE[1], DE[2], SS, info["gamma"], info["brightness"],
+                              info["vibrancy"], 0.0, None, img, stream=stream)
+        else:
+            R.tonemap(bins, W, H, SS, info["gamma"], info["brightness"], info["vibrancy"], 0.0, None, img,
+                      stream=stream)
         if ev:
             ev[2].record(stream)
-        R.tonemap(src, W, H, SS, info["gamma"], info["brightness"], info["vibrancy"], 0.0, None, img, stream=stream)
-        if ev:
-            ev[3].record(stream)
 
     def barrier():
         if ws > 1:
@@ -423,7 +421,7 @@ def run_native(args):
     for _ in range(args.warmup):
         frame()
     barrier()
-    evs = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(4)) for _ in range(args.steps)]
+    evs = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(3)) for _ in range(args.steps)]
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
@@ -439,19 +437,16 @@ def run_native(args):
     draw_ms = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
     image_passes = None
     if WL["image"]:
-        de_ms = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps
-        tm_ms = sum(e[2].elapsed_time(e[3]) for e in evs) / args.steps
-        nb = W * H
-        # algorithmic bytes: DE 16 B read + 16 B write per bin (radii are intermediate); the
-        # FP64 statistics and the tonemap read 16 B per bin each and write 4 B per output pixel
-        de_bytes = nb * 32 if DE else 0
-        tm_bytes = nb * 16 + nb * 16 + W_OUT * H_OUT * 4
+        tail_ms = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps
+        # algorithmic bytes of the image tail: the bins read once (16 B per bin) and the RGBA8
+        # image written (4 B per output pixel); with DE the passes read the bins twice (the radius
+        # pass, then the tiles) plus a radius byte per bin, and never write the estimator's output
+        tail_bytes = W * H * 16 + W_OUT * H_OUT * 4
         peak_, _ = _peaks()
-        image_passes = {"de_ms": de_ms if DE else 0.0, "de_bytes": de_bytes,
-                        "de_gbs": de_bytes / (de_ms * 1e-3) / 1e9 if DE and de_ms > 0 else None,
-                        "stats_tonemap_ms": tm_ms, "stats_tonemap_bytes": tm_bytes,
-                        "stats_tonemap_gbs": tm_bytes / (tm_ms * 1e-3) / 1e9 if tm_ms > 0 else None,
-                        "peak_gbs": peak_}
+        image_passes = {"kernels": "de_radius_sum_kernel + de_tile_kernel<9, tonemap>" if DE else
+                                   "stats_kernel + tonemap_kernel",
+                        "ms": tail_ms, "algorithmic_bytes": tail_bytes,
+                        "gbs": tail_bytes / (tail_ms * 1e-3) / 1e9 if tail_ms > 0 else None, "peak_gbs": peak_}
     ms_step = slowest_rank_ms(ms / args.steps)
     value = replica_throughput(POINTS, ms / args.steps)
 
@@ -523,7 +518,9 @@ def run_native(args):
         "binned_fraction": binned_fraction,
         "binned_gpoints_s": value * binned_fraction,
         "image_passes": image_passes,
-        "gpu_launches": (launches + (FUSE + args.steps_per_launch - 1) // args.steps_per_launch + 4) * args.steps,
+        # per frame: the drawing launches, the warmup launch, animate_kernel, and the image tail
+        # (radius/sum + tile-tonemap with DE, statistics + tonemap without)
+        "gpu_launches": (launches + (FUSE + args.steps_per_launch - 1) // args.steps_per_launch + 3) * args.steps,
         "e2e": {"value": e2e_value, "unit": "Gpoints/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "s_per_frame": e2e_step / 1e3, "binned_gpoints_s": st["binned"] / (statistics.median(e2e_ms) * 1e-3) / 1e9},
         "roofline": roofline,
@@ -633,8 +630,8 @@ def run_batch(args):
         "binned_gpoints_s": value * st["binned"] / st["points"],
         "wall_ms_per_step": wall / args.steps,
         # per batch: the persistent chaos launches (one per specialised structure group + the
-        # interpreted one) and per image DE radius + DE gather + FP64 stats + tonemap
-        "gpu_launches": (spec_groups + (1 if 0 in info["specialized"] else 0) + 4 * n_img) * args.steps,
+        # interpreted one) and per image the DE radius/sum pass + the tile-tonemap pass
+        "gpu_launches": (spec_groups + (1 if 0 in info["specialized"] else 0) + 2 * n_img) * args.steps,
         "e2e": {"value": replica_throughput(st["points"], statistics.median(e2e_ms)), "unit": "Gpoints/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "frames_per_s": n_img / (e2e_step * 1e-3),
                 "includes": "genome parse + compile + upload + autotune + graph capture + run + image readback"},

@@ -153,6 +153,8 @@ typedef struct {
     uint32_t num_xforms;
     int32_t  has_final;
     uint32_t total_params;      /* flat parameter buffer size (flame.cpp:68) */
+    float    filter;            /* flam3 spatial filter radius in output pixels (0: the ss x ss box) */
+    int32_t  filter_shape;      /* rf_filter_shape of flam3's filter_shape attribute */
 } rf_flame_info;
 RF_API int  rf_flame_get_info(const rf_flame* f, rf_flame_info* out);
 /* The mutable view fields the reference UI edits in place (main.cpp:324-381). */
@@ -250,11 +252,33 @@ RF_API int rf_density_estimate(const float* bins_rgba, uint32_t width, uint32_t 
    For callers that cannot call cudaMalloc — e.g. a plug-in inside a host application that owns
    the device memory pool, or a frame loop with a fixed memory budget that must not enter the
    allocator.  Its scratch (bin radii, kernel weights) lives in static device arrays of the
-   library: at most 8,388,608 bins (one 3840x2160 grid); larger grids return RF_ERR_CAPACITY.
-   The first call on a device looks the arrays up (make it before any stream capture); calls
-   share the scratch, so calls that overlap on the GPU race and must be serialised. */
+   library: at most 8,388,608 bins (one 3840x2160 grid) and 65,535 rows; larger grids return
+   RF_ERR_CAPACITY.  The first call on a device looks the arrays up and fills the kernel-weight
+   table with one synchronous copy (make it before any stream capture); later calls copy nothing
+   from the host.  Calls share the radius scratch, so calls that overlap on the GPU race and must
+   be serialised. */
 RF_API int rf_density_estimate_static(const float* bins_rgba, uint32_t width, uint32_t height, int radius,
                                       int min_radius, float curve, float* out_rgba, void* stream);
+/* The tonemap with flam3's spatial filter in place of the ss x ss box — the flam3 `filter` (radius
+   in output pixels) and `filter_shape` attributes the reference ignores (flame.cpp:166-176).  The
+   separable window is fwidth = int(2 * support * ss * radius) + 1 bins wide, made the parity of
+   ss, sampled at cell centres and normalised; each output pixel weighs the log-scaled bins of its
+   window (bins beyond the grid count as empty), then gamma / vibrancy / clamp as rf_tonemap.
+   radius <= 0 is rf_tonemap's box; 2 * support * ss * radius must stay below 63. */
+enum rf_filter_shape { RF_FILTER_GAUSSIAN = 0, RF_FILTER_BOX = 1, RF_FILTER_TRIANGLE = 2, RF_FILTER_HERMITE = 3 };
+RF_API int rf_tonemap_filter(const float* rgba, uint32_t width, uint32_t height, uint32_t ss, float filter_radius,
+                             int filter_shape, float gamma, float brightness, float vibrancy, float k2, float* out_f32,
+                             uint8_t* out_rgba8, void* stream);
+/* The reference's image tail (main.cpp:490-535: the density-estimation raster pass, then the
+   tonemap pass) in one call: rf_density_estimate followed by rf_tonemap of its output, the same
+   arithmetic, with k2 <= 0 taking bins / sum(a) of the estimator's output (FP64).  For radii up
+   to 12 and ss dividing 8 the estimator's output stays in on-chip memory (each 32 x 8 tile is
+   tonemapped where it is estimated) and the density sum comes from the radius pass, so the FP32
+   output plane is never written; otherwise the passes run one after another.  Scratch comes from
+   cudaMallocAsync on `stream`. */
+RF_API int rf_density_tonemap(const float* bins_rgba, uint32_t width, uint32_t height, int radius, int min_radius,
+                              float curve, uint32_t ss, float gamma, float brightness, float vibrancy, float k2,
+                              float* out_f32, uint8_t* out_rgba8, void* stream);
 /* FP64 statistics of the density channel: out[0] = sum of a, out[1] = max a, out[2] = bins with a > 0. */
 RF_API int rf_hist_stats(const float* rgba, uint32_t width, uint32_t height, double* out3, void* stream);
 /* Log-density tonemap (tonemap.glsl:18-38) with a box supersample filter of ss x ss bins:

@@ -1300,6 +1300,83 @@ int orc_tonemap(const double* in, uint32_t w, uint32_t h, uint32_t ss, double ga
     return 0;
 }
 
+// flam3's spatial filter functions and their supports (the published definitions: Gaussian
+// exp(-2x^2) sqrt(2/pi) on [-1.5, 1.5], box on [-0.5, 0.5], triangle 1 - |x| on [-1, 1], the cubic
+// Hermite 2|x|^3 - 3x^2 + 1 on [-1, 1])
+static double filter_support(int shape) { return shape == 1 ? 0.5 : (shape == 0 ? 1.5 : 1.0); }
+static double filter_value(int shape, double x) {
+    const double t = std::fabs(x);
+    switch (shape) {
+        case 0: return std::exp(-2.0 * x * x) * std::sqrt(2.0 / 3.14159265358979323846);
+        case 1: return t <= 0.5 ? 1.0 : 0.0;
+        case 2: return t < 1.0 ? 1.0 - t : 0.0;
+        case 3: return t < 1.0 ? (2.0 * t - 3.0) * t * t + 1.0 : 0.0;
+        default: return 0.0;
+    }
+}
+
+// Taps of the separable filter over the supersampled bins: the window spans
+// fw = 2 * support * ss * radius bins, rounded up to an integer width of the same parity as ss
+// (so the window centres on the output pixel's ss x ss block), sampled at the centre of each
+// cell with the coordinate stretched so the window covers exactly the support; normalised.
+int orc_filter_kernel(uint32_t ss, double radius, int shape, double* taps, int cap) {
+    if (ss == 0 || !(radius > 0.0) || shape < 0 || shape > 3) return -1;
+    const double support = filter_support(shape);
+    const double fw = 2.0 * support * (double)ss * radius;
+    int fwidth = (int)fw + 1;
+    if ((fwidth ^ (int)ss) & 1) fwidth++;
+    if (fwidth > cap) return -1;
+    const double adjust = fw > 0.0 ? support * (double)fwidth / fw : 1.0;
+    double sum = 0.0;
+    for (int i = 0; i < fwidth; i++) {
+        taps[i] = filter_value(shape, ((2.0 * i + 1.0) / (double)fwidth - 1.0) * adjust);
+        sum += taps[i];
+    }
+    for (int i = 0; i < fwidth; i++) taps[i] /= sum;
+    return fwidth;
+}
+
+int orc_tonemap_filter(const double* in, uint32_t w, uint32_t h, uint32_t ss, double radius, int shape,
+                       double gamma, double brightness, double vibrancy, double k2, double* out) {
+    if (ss == 0 || w % ss || h % ss) return -1;
+    double taps[256];
+    const int fwidth = orc_filter_kernel(ss, radius, shape, taps, 256);
+    if (fwidth < 0) return -1;
+    const int pad = (fwidth - (int)ss) / 2;
+    // per-bin log-density scaling (tonemap.glsl:26), zero where there is no density
+    std::vector<double> L((size_t)w * h * 4, 0.0);
+    for (size_t i = 0; i < (size_t)w * h; i++) {
+        const double a = in[i * 4 + 3];
+        if (!(a > 0.0)) continue;
+        const double ls = 0.5 * brightness * std::log(1.0 + a * k2) * 0.434294481903251827651128918916 / a;
+        for (int k = 0; k < 4; k++) L[i * 4 + k] = in[i * 4 + k] * ls;
+    }
+    const uint32_t ow = w / ss, oh = h / ss;
+    for (uint32_t oy = 0; oy < oh; oy++)
+        for (uint32_t ox = 0; ox < ow; ox++) {
+            double acc[4] = {0, 0, 0, 0};
+            for (int j = 0; j < fwidth; j++) {
+                const int y = (int)(oy * ss) - pad + j;
+                if (y < 0 || y >= (int)h) continue;
+                for (int i = 0; i < fwidth; i++) {
+                    const int x = (int)(ox * ss) - pad + i;
+                    if (x < 0 || x >= (int)w) continue;
+                    const double wt = taps[i] * taps[j];
+                    for (int k = 0; k < 4; k++) acc[k] += wt * L[((size_t)y * w + x) * 4 + k];
+                }
+            }
+            double* o = out + ((size_t)oy * ow + ox) * 4;
+            if (!(acc[3] > 0.0)) { o[0] = o[1] = o[2] = 0.0; o[3] = 1.0; continue; }
+            const double ig = 1.0 / gamma, gf = std::pow(acc[3], ig) / acc[3];
+            for (int k = 0; k < 3; k++) {
+                const double t = std::pow(acc[k], ig) * (1.0 - vibrancy) + gf * acc[k] * vibrancy;
+                o[k] = std::min(std::max(t, 0.0), 1.0);
+            }
+            o[3] = 1.0;
+        }
+    return 0;
+}
+
 int orc_downsample(const double* in, uint32_t w, uint32_t h, uint32_t ss, double* out) {
     if (ss == 0 || w % ss || h % ss) return -1;
     uint32_t ow = w / ss, oh = h / ss;

@@ -118,6 +118,15 @@ int orc_density_estimate(const double* in, uint32_t w, uint32_t h, int radius, i
    per-bin log scaling.  out (W/ss)*(H/ss)*4 doubles. */
 int orc_tonemap(const double* in, uint32_t w, uint32_t h, uint32_t ss, double gamma, double brightness,
                 double vibrancy, double k2, double* out);
+/* The flam3 spatial filter in place of the box (no counterpart in the reference, which ignores
+   flam3's filter / filter_shape, flame.cpp:166-176): shape 0 gaussian, 1 box, 2 triangle,
+   3 hermite; a separable kernel of fwidth taps (orc_filter_kernel), each output pixel the
+   weighted sum of the log-scaled bins of its fwidth x fwidth window, then gamma / vibrancy /
+   clamp as tonemap.glsl.  orc_filter_kernel writes the normalised 1-D taps (cap >= 64) and
+   returns fwidth, or -1. */
+int orc_filter_kernel(uint32_t ss, double radius, int shape, double* taps, int cap);
+int orc_tonemap_filter(const double* in, uint32_t w, uint32_t h, uint32_t ss, double radius, int shape,
+                       double gamma, double brightness, double vibrancy, double k2, double* out);
 /* Box supersample filter: out[(W/ss)*(H/ss)*4] = mean of ss*ss blocks. */
 int orc_downsample(const double* in, uint32_t w, uint32_t h, uint32_t ss, double* out);
 

@@ -95,6 +95,10 @@ def lib():
         L.orc_tonemap.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                   ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_void_p]
+        L.orc_filter_kernel.argtypes = [ctypes.c_uint32, ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+        L.orc_tonemap_filter.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                         ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
         L.orc_downsample.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                      ctypes.c_void_p]
         _lib = L
@@ -286,6 +290,24 @@ def tonemap(rgba, gamma, brightness, vibrancy, k2, ss=1):
     out = np.zeros((h // ss, w // ss, 4), np.float64)
     if lib().orc_tonemap(_ptr(rgba), w, h, ss, gamma, brightness, vibrancy, k2, _ptr(out)) != 0:
         raise ValueError("tonemap failed")
+    return out
+
+
+def filter_kernel(ss, radius, shape):
+    taps = np.zeros(256, np.float64)
+    n = lib().orc_filter_kernel(ss, radius, shape, _ptr(taps), 256)
+    if n < 0:
+        raise ValueError("bad filter")
+    return taps[:n]
+
+
+def tonemap_filter(rgba, ss, radius, shape, gamma, brightness, vibrancy, k2):
+    """The tonemap with flam3's spatial filter in place of the ss x ss box."""
+    rgba = np.ascontiguousarray(rgba, np.float64)
+    h, w = rgba.shape[:2]
+    out = np.zeros((h // ss, w // ss, 4), np.float64)
+    if lib().orc_tonemap_filter(_ptr(rgba), w, h, ss, radius, shape, gamma, brightness, vibrancy, k2, _ptr(out)) != 0:
+        raise ValueError("tonemap_filter failed")
     return out
 
 

@@ -25,6 +25,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "librefrakt_gb300.so")
 SYNTH_SMALL, SYNTH_RANDOM, SYNTH_CONTRACT, SYNTH_SPACEFILL = 0, 1, 2, 3
 SPLAT_AUTO, SPLAT_GLOBAL, SPLAT_WARP = 0, 1, 2
 BINS_AUTO, BINS_DIRECT, BINS_INTERLEAVED = 0, 1, 2
+FILTER_GAUSSIAN, FILTER_BOX, FILTER_TRIANGLE, FILTER_HERMITE = 0, 1, 2, 3
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "PARSE", 3: "UNKNOWN_NAME", 4: "UNSUPPORTED", 5: "CAPACITY",
           6: "CUDA", 7: "NEEDS_WARMUP", 8: "IO", 9: "NO_DEVICE"}
@@ -49,7 +50,7 @@ class FlameInfo(ctypes.Structure):
                 ("estimator_min", ctypes.c_int32), ("estimator_curve", ctypes.c_float),
                 ("gamma", ctypes.c_float), ("vibrancy", ctypes.c_float), ("brightness", ctypes.c_float),
                 ("num_xforms", ctypes.c_uint32), ("has_final", ctypes.c_int32),
-                ("total_params", ctypes.c_uint32)]
+                ("total_params", ctypes.c_uint32), ("filter", ctypes.c_float), ("filter_shape", ctypes.c_int32)]
 
 
 class XformDesc(ctypes.Structure):
@@ -151,6 +152,12 @@ _SIGS = {
     "rf_sim_counters": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "rf_density_estimate": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
                              ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rf_tonemap_filter": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
+                           ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rf_density_tonemap": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
+                            ctypes.c_float, ctypes.c_uint32, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                            ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rf_hist_stats": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p], ctypes.c_int),
     "rf_tonemap": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
                     ctypes.c_float, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
@@ -389,7 +396,7 @@ class Flame:
                 "estimator_radius": i.estimator_radius, "estimator_min": i.estimator_min,
                 "estimator_curve": i.estimator_curve, "gamma": i.gamma, "vibrancy": i.vibrancy,
                 "brightness": i.brightness, "num_xforms": i.num_xforms, "has_final": bool(i.has_final),
-                "total_params": i.total_params}
+                "total_params": i.total_params, "filter": i.filter, "filter_shape": i.filter_shape}
 
     def set_view(self, center, scale, rotate):
         c = (ctypes.c_float * 2)(*center)
@@ -597,6 +604,20 @@ def render(sim, flame, *a, **k):
 def density_estimate(bins_rgba, width, height, radius, min_radius, curve, out, stream=None):
     _check(library().rf_density_estimate(_ptr(bins_rgba), width, height, radius, min_radius, curve, _ptr(out),
                                          _stream(stream)))
+
+
+def tonemap_filter(rgba, width, height, ss, radius, shape, gamma, brightness, vibrancy, k2, out_f32=None,
+                   out_rgba8=None, stream=None):
+    """The tonemap with flam3's spatial filter (FILTER_GAUSSIAN ...) in place of the box (rf_tonemap_filter)."""
+    _check(library().rf_tonemap_filter(_ptr(rgba), width, height, ss, radius, shape, gamma, brightness, vibrancy, k2,
+                                       _ptr(out_f32), _ptr(out_rgba8), _stream(stream)))
+
+
+def density_tonemap(bins_rgba, width, height, radius, min_radius, curve, ss, gamma, brightness, vibrancy, k2,
+                    out_f32=None, out_rgba8=None, stream=None):
+    """Density estimation then the tonemap in one call (rf_density_tonemap)."""
+    _check(library().rf_density_tonemap(_ptr(bins_rgba), width, height, radius, min_radius, curve, ss, gamma,
+                                        brightness, vibrancy, k2, _ptr(out_f32), _ptr(out_rgba8), _stream(stream)))
 
 
 def hist_stats(rgba, width, height, stream=None):

@@ -340,6 +340,8 @@ int rf_flame_get_info(const rf_flame* f, rf_flame_info* o) {
     o->has_final = g.has_final ? 1 : 0;
     std::vector<float> buf;
     o->total_params = (genome_param_buffer(g, buf, nullptr) == 0) ? (uint32_t)buf.size() : 0;
+    o->filter = g.filter;
+    o->filter_shape = g.filter_shape;
     return RF_OK;
 }
 
@@ -477,7 +479,7 @@ int rf_sim_destroy(rf_sim* s) {
     cudaSetDevice(s->device);
     cudaStreamSynchronize(s->stream);
     void* ptrs[] = {s->rec, s->walk[0], s->walk[1], s->rng, s->table, s->base_prog, s->progs, s->palette, s->counters,
-                    s->trace, s->r_bins, s->r_hits, s->r_de, s->r_img, s->r_stats};
+                    s->trace, s->r_bins, s->r_hits, s->r_de, s->r_img, s->r_stats, s->r_rad, s->r_dw};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -640,7 +642,62 @@ int rf_density_estimate(const float* in, uint32_t w, uint32_t h, int radius, int
     if (radius < 0 || radius > 100 || min_radius < 0 || min_radius > 100)
         return fail(RF_ERR_INVALID_ARG, "estimator radii must be within 0..100 (main.cpp:502)");
     if (in == out) return fail(RF_ERR_INVALID_ARG, "rf_density_estimate: in and out must differ");
+    if (h > 65535) return fail(RF_ERR_CAPACITY, "rf_density_estimate: more than 65535 rows");
     RF_CUDA(launch_density((const float4*)in, w, h, radius, min_radius, curve, (float4*)out, (cudaStream_t)stream));
+    return RF_OK;
+}
+
+int rf_tonemap_filter(const float* rgba, uint32_t w, uint32_t h, uint32_t ss, float radius, int shape, float gamma,
+                      float brightness, float vibrancy, float k2, float* out_f32, uint8_t* out8, void* stream) {
+    if (!(radius > 0.0f)) return rf_tonemap(rgba, w, h, ss, gamma, brightness, vibrancy, k2, out_f32, out8, stream);
+    if (!rgba || w == 0 || h == 0 || ss == 0 || w % ss || h % ss)
+        return fail(RF_ERR_INVALID_ARG, "rf_tonemap_filter: bad arguments (width and height must be multiples of ss)");
+    if (shape < RF_FILTER_GAUSSIAN || shape > RF_FILTER_HERMITE) return fail(RF_ERR_INVALID_ARG, "unknown filter shape");
+    float taps[kMaxFilterTaps];
+    if (filter_taps(ss, radius, shape, taps) < 0)
+        return fail(RF_ERR_CAPACITY, "rf_tonemap_filter: the filter window exceeds 64 bins");
+    cudaStream_t st = (cudaStream_t)stream;
+    double* stats = nullptr;
+    if (!(k2 > 0.0f)) {
+        RF_CUDA(cudaMallocAsync((void**)&stats, 3 * sizeof(double), st));
+        cudaError_t e = launch_stats((const float4*)rgba, w, h, stats, st);
+        if (e != cudaSuccess) { cudaFreeAsync(stats, st); return cuda_fail(e, "stats"); }
+    }
+    cudaError_t e = launch_tonemap_filter((const float4*)rgba, w, h, ss, radius, shape, gamma, brightness, vibrancy,
+                                          k2, stats, (float4*)out_f32, (uchar4*)out8, st);
+    if (stats) cudaFreeAsync(stats, st);
+    if (e != cudaSuccess) return cuda_fail(e, "rf_tonemap_filter");
+    return RF_OK;
+}
+
+int rf_density_tonemap(const float* in, uint32_t w, uint32_t h, int radius, int min_radius, float curve, uint32_t ss,
+                       float gamma, float brightness, float vibrancy, float k2, float* out_f32, uint8_t* out8,
+                       void* stream) {
+    if (!in || w == 0 || h == 0 || ss == 0 || w % ss || h % ss)
+        return fail(RF_ERR_INVALID_ARG, "rf_density_tonemap: bad arguments (width and height must be multiples of ss)");
+    if (radius < 0 || radius > 100 || min_radius < 0 || min_radius > 100)
+        return fail(RF_ERR_INVALID_ARG, "estimator radii must be within 0..100 (main.cpp:502)");
+    if (h > 65535 || h / ss > 65535) return fail(RF_ERR_CAPACITY, "rf_density_tonemap: more than 65535 rows");
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t n = (size_t)w * h;
+    std::vector<float> wts;
+    density_weights(radius, min_radius, wts);
+    const bool fused = density_tonemap_fused(radius, min_radius, ss);
+    uint8_t* rad = nullptr;
+    float* dw = nullptr;
+    double* stats = nullptr;
+    float4* de = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&rad, n, st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&dw, wts.size() * sizeof(float), st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&stats, 3 * sizeof(double), st);
+    if (e == cudaSuccess && !fused) e = cudaMallocAsync((void**)&de, n * sizeof(float4), st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dw, wts.data(), wts.size() * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = launch_density_tonemap((const float4*)in, w, h, radius, min_radius, curve, ss, gamma, brightness, vibrancy,
+                                   k2, (float4*)out_f32, (uchar4*)out8, rad, dw, stats, de, st);
+    for (void* p : {(void*)rad, (void*)dw, (void*)stats, (void*)de})
+        if (p) cudaFreeAsync(p, st);
+    if (e != cudaSuccess) return cuda_fail(e, "rf_density_tonemap");
     return RF_OK;
 }
 
@@ -718,8 +775,8 @@ int rf_render(rf_sim* s, rf_flame* f, const rf_render_desc* d, uint8_t* out, dou
     if (int rc = set_device(s)) return rc;
     const size_t nb = (size_t)W * H, ni = (size_t)d->width * d->height;
     if (s->r_bins_n != nb) {
-        cudaFree(s->r_bins); cudaFree(s->r_hits); cudaFree(s->r_de);
-        s->r_bins = nullptr; s->r_hits = nullptr; s->r_de = nullptr; s->r_bins_n = 0;
+        cudaFree(s->r_bins); cudaFree(s->r_hits); cudaFree(s->r_de); cudaFree(s->r_rad);
+        s->r_bins = nullptr; s->r_hits = nullptr; s->r_de = nullptr; s->r_rad = nullptr; s->r_bins_n = 0;
         RF_CUDA(cudaMalloc((void**)&s->r_bins, nb * sizeof(float4)));
         RF_CUDA(cudaMalloc((void**)&s->r_hits, nb * sizeof(uint32_t)));
         RF_CUDA(cudaMalloc((void**)&s->r_de, nb * sizeof(float4)));
@@ -766,21 +823,52 @@ int rf_render(rf_sim* s, rf_flame* f, const rf_render_desc* d, uint8_t* out, dou
             passes += more;
         }
     }
-    const float4* src = s->r_bins;
-    if (d->density_estimation && (f->g.est_radius > 0 || f->g.est_min > 0)) {
+    const bool flam3_filter = f->g.filter > 0.0f && ss > 1;
+    if (flam3_filter) {
+        // the genome's flam3 spatial filter over the supersampled (density-estimated) bins
+        float taps[kMaxFilterTaps];
+        if (filter_taps(ss, f->g.filter, f->g.filter_shape, taps) < 0)
+            return done(fail(RF_ERR_CAPACITY, "rf_render: the genome's filter window exceeds 64 bins"));
+        const float4* src = s->r_bins;
+        if (d->density_estimation && (f->g.est_radius > 0 || f->g.est_min > 0)) {
+            e = launch_density(s->r_bins, W, H, std::min(100, f->g.est_radius), std::min(100, f->g.est_min),
+                               f->g.est_curve, s->r_de, s->stream);
+            if (e != cudaSuccess) return done(cuda_fail(e, "density estimation"));
+            src = s->r_de;
+        }
+        if (!(d->k2 > 0.0f)) e = launch_stats(src, W, H, s->r_stats, s->stream);
+        if (e == cudaSuccess)
+            e = launch_tonemap_filter(src, W, H, ss, f->g.filter, f->g.filter_shape, f->g.gamma, f->g.brightness,
+                                      f->g.vibrancy, d->k2, d->k2 > 0.0f ? nullptr : s->r_stats, nullptr, s->r_img,
+                                      s->stream);
+    } else if (d->density_estimation && (f->g.est_radius > 0 || f->g.est_min > 0)) {
+        // main.cpp:490-535: density estimation and tonemap, the estimator's output kept on chip
         const int R = std::min(100, f->g.est_radius), mn = std::min(100, f->g.est_min);
-        e = launch_density(s->r_bins, W, H, R, mn, f->g.est_curve, s->r_de, s->stream);
-        if (e != cudaSuccess) return done(cuda_fail(e, "density estimation"));
-        src = s->r_de;
+        if (!s->r_rad) {
+            e = cudaMalloc((void**)&s->r_rad, nb);
+            if (e != cudaSuccess) return done(cuda_fail(e, "cudaMalloc"));
+            s->r_rad_n = nb;
+        }
+        if (!s->r_dw) {  // every radius up to 100: the table is a prefix of itself for any R
+            std::vector<float> wts;
+            density_weights(100, 0, wts);
+            e = cudaMalloc((void**)&s->r_dw, wts.size() * sizeof(float));
+            if (e == cudaSuccess) e = cudaMemcpy(s->r_dw, wts.data(), wts.size() * sizeof(float), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return done(cuda_fail(e, "density weights"));
+        }
+        e = launch_density_tonemap(s->r_bins, W, H, R, mn, f->g.est_curve, ss, f->g.gamma, f->g.brightness,
+                                   f->g.vibrancy, d->k2, nullptr, s->r_img, s->r_rad, s->r_dw, s->r_stats, s->r_de,
+                                   s->stream);
+    } else {
+        const double* st = nullptr;
+        if (!(d->k2 > 0.0f)) {
+            e = launch_stats(s->r_bins, W, H, s->r_stats, s->stream);
+            if (e != cudaSuccess) return done(cuda_fail(e, "stats"));
+            st = s->r_stats;
+        }
+        e = launch_tonemap(s->r_bins, W, H, ss, f->g.gamma, f->g.brightness, f->g.vibrancy, d->k2, st, nullptr,
+                           s->r_img, s->stream);
     }
-    const double* st = nullptr;
-    if (!(d->k2 > 0.0f)) {
-        e = launch_stats(src, W, H, s->r_stats, s->stream);
-        if (e != cudaSuccess) return done(cuda_fail(e, "stats"));
-        st = s->r_stats;
-    }
-    e = launch_tonemap(src, W, H, ss, f->g.gamma, f->g.brightness, f->g.vibrancy, d->k2, st, nullptr, s->r_img,
-                       s->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, s->r_img, ni * sizeof(uchar4), cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaEventRecord(e1, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);

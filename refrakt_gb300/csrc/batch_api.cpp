@@ -256,20 +256,21 @@ int enqueue(rf_batch* b) {
     if (e != cudaSuccess) return cuda_err(e, "batch kernel");
     for (size_t i = 0; i < b->items.size(); i++) {
         Item& it = b->items[i];
-        const float4* src = it.bins;
-        if (it.de) {
-            e = launch_density_resident(it.bins, it.W, it.H, std::min(100, it.est_radius), std::min(100, it.est_min),
-                                        it.est_curve, it.de, it.rad, it.dw, st);
-            if (e != cudaSuccess) return cuda_err(e, "batch density estimation");
-            src = it.de;
+        if (it.de) {  // density estimation and tonemap, the estimator's output kept on chip where it fits
+            e = launch_density_tonemap(it.bins, it.W, it.H, std::min(100, it.est_radius), std::min(100, it.est_min),
+                                       it.est_curve, it.ss, it.gamma, it.brightness, it.vibrancy, b->d.k2, it.img_f32,
+                                       it.img, it.rad, it.dw, b->stats + 3 * i, it.de, st);
+            if (e != cudaSuccess) return cuda_err(e, "batch density estimation and tonemap");
+            continue;
         }
         const double* stt = nullptr;
         if (!(b->d.k2 > 0.0f)) {
-            e = launch_stats(src, it.W, it.H, b->stats + 3 * i, st);
+            e = launch_stats(it.bins, it.W, it.H, b->stats + 3 * i, st);
             if (e != cudaSuccess) return cuda_err(e, "batch stats");
             stt = b->stats + 3 * i;
         }
-        e = launch_tonemap(src, it.W, it.H, it.ss, it.gamma, it.brightness, it.vibrancy, b->d.k2, stt, it.img_f32, it.img, st);
+        e = launch_tonemap(it.bins, it.W, it.H, it.ss, it.gamma, it.brightness, it.vibrancy, b->d.k2, stt, it.img_f32,
+                           it.img, st);
         if (e != cudaSuccess) return cuda_err(e, "batch tonemap");
     }
     return RF_OK;

@@ -11,14 +11,17 @@
 //
 // In host code a __device__ array's name stands for a host-side shadow, not a device address, so
 // the device address is looked up with cudaGetSymbolAddress once per device, with that device
-// current, on the first call made on it; that first call should come before any stream capture.
-// Every call on a device shares the same arrays and leaves its radii and weights in them; each
-// call rewrites all of the scratch it reads (every bin's radius, the whole weight table) before
-// reading it, so nothing has to start at zero.  Calls that overlap on the GPU (two streams at
-// once) race on the shared scratch and must be serialised by the caller.
+// current, on the first call made on it.  That first call also fills the weight table — the
+// weights of every radius up to 100, which do not depend on the call's arguments (a radius's
+// weights sit at the same offset whatever the largest radius) — with one synchronous copy; it
+// should come before any stream capture.  Later calls copy nothing from the host.  Every call on
+// a device shares the radius array and leaves its radii in it; each call rewrites every bin's
+// radius before reading it, so nothing has to start at zero.  Calls that overlap on the GPU (two
+// streams at once) race on the shared radii and must be serialised by the caller.
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <vector>
 
 #include "internal.h"
 #include "kernels.h"
@@ -58,6 +61,12 @@ int scratch_for_current_device(StaticScratch& out) {
         if (e != cudaSuccess) return fail(RF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         e = cudaGetSymbolAddress(&wts, g_de_weight_scratch);
         if (e != cudaSuccess) return fail(RF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        // the weights of every radius up to 100, once per device
+        std::vector<float> table;
+        density_weights(100, 0, table);
+        if (table.size() != kStaticDeMaxWeights) return fail(RF_ERR_CAPACITY, "static weight table size mismatch");
+        e = cudaMemcpy(wts, table.data(), table.size() * sizeof(float), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return fail(RF_ERR_CUDA, std::string("static weight table: ") + cudaGetErrorString(e));
         s.radius = static_cast<uint8_t*>(rad);
         s.weights = static_cast<float*>(wts);
     }
@@ -80,12 +89,11 @@ extern "C" int rf_density_estimate_static(const float* in, uint32_t w, uint32_t 
         return fail(RF_ERR_CAPACITY, "rf_density_estimate_static: " + std::to_string((size_t)w * h) +
                                          " bins exceed the static scratch of " + std::to_string(kStaticDeMaxBins) +
                                          " bins; use rf_density_estimate");
-    if (density_weight_count(radius, min_radius) > kStaticDeMaxWeights)
-        return fail(RF_ERR_CAPACITY, "rf_density_estimate_static: weight table exceeds the static scratch");
+    if (h > 65535) return fail(RF_ERR_CAPACITY, "rf_density_estimate_static: more than 65535 rows");
     StaticScratch s;
     if (int rc = scratch_for_current_device(s)) return rc;
-    cudaError_t e = launch_density_scratch((const float4*)in, w, h, radius, min_radius, curve, (float4*)out, s.radius,
-                                           s.weights, kStaticDeMaxWeights, (cudaStream_t)stream);
+    cudaError_t e = launch_density_resident((const float4*)in, w, h, radius, min_radius, curve, (float4*)out, s.radius,
+                                            s.weights, (cudaStream_t)stream);
     if (e != cudaSuccess) return fail(RF_ERR_CUDA, std::string("rf_density_estimate_static: ") + cudaGetErrorString(e));
     return RF_OK;
 }

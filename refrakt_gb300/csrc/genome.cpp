@@ -113,6 +113,11 @@ int genome_from_xml(const std::string& xml, const Registry& reg, Genome& g) {
     }
     if (fl->attr("supersample")) g.supersample = (unsigned)std::max(1, as_int(A("supersample")));
     g.filter = as_float(A("filter"));
+    {  // flam3 filter shapes; the ones without a kernel here are drawn with the Gaussian
+        const std::string fs = A("filter_shape");
+        g.filter_shape = fs == "box" ? RF_FILTER_BOX : fs == "triangle" ? RF_FILTER_TRIANGLE
+                       : fs == "hermite" ? RF_FILTER_HERMITE : RF_FILTER_GAUSSIAN;
+    }
     for (const auto& k : fl->kids) {
         if (k.name == "xform" || k.name == "finalxform") {
             Xform x;
@@ -360,6 +365,12 @@ std::string genome_to_xml(const Genome& g) {
     o << "\" scale=\""; fmt_float(o, g.scale);
     o << "\" rotate=\""; fmt_float(o, g.rotate);
     o << "\" supersample=\"" << g.supersample;
+    if (g.filter > 0.0f) {
+        static const char* shapes[] = {"gaussian", "box", "triangle", "hermite"};
+        o << "\" filter=\"";
+        fmt_float(o, g.filter);
+        o << "\" filter_shape=\"" << shapes[g.filter_shape & 3];
+    }
     o << "\" estimator_radius=\"" << g.est_radius << "\" estimator_min=\"" << g.est_min;
     o << "\" estimator_curve=\""; fmt_float(o, g.est_curve);
     o << "\" brightness=\""; fmt_float(o, g.brightness);

@@ -53,6 +53,8 @@ struct rf_sim {
     float4* r_de = nullptr;
     uchar4* r_img = nullptr;
     double* r_stats = nullptr;
-    size_t r_bins_n = 0, r_img_n = 0;
+    uint8_t* r_rad = nullptr;     // density estimation: a radius byte per bin
+    float* r_dw = nullptr;        // density estimation: kernel weights of every radius up to 100
+    size_t r_bins_n = 0, r_img_n = 0, r_rad_n = 0;
 };
 

@@ -27,6 +27,7 @@ struct DeTables {
     float thr[101];      // thr[k-1]: bin radius >= k  <=>  a <= thr (curve > 0) or a >= thr (curve < 0)
     int R, min_r, mode;  // mode 0: curve > 0, 1: curve < 0, 2: curve == 0 (radius R)
     int wbase[102];      // offset of radius r's (r+1)^2 weights
+    double wsum[101];    // the weights of a whole disc of radius r, summed in FP64
 };
 
 __device__ __forceinline__ int de_radius(float a, const DeTables& T) {
@@ -53,6 +54,134 @@ __global__ void de_radius_kernel(const float4* __restrict__ in, size_t n, const 
     }
 }
 
+// block-wide FP64 sum, added to *out by one thread per block (blockDim.x a multiple of 32, <= 1024)
+__device__ __forceinline__ void block_sum_to(double s, double* out) {
+    __shared__ double part[32];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) part[wid] = s;
+    __syncthreads();
+    if (wid == 0) {
+        s = lane < (int)(blockDim.x >> 5) ? part[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) atomicAdd(out, s);
+    }
+}
+
+// sum of k^2 for k = lo .. hi (lo <= hi), in closed form
+__host__ __device__ __forceinline__ double square_sum(int lo, int hi) {
+    auto F = [](int m) { return (double)m * (m + 1) * (2.0 * m + 1) / 6.0; };  // 0^2 + .. + m^2, m >= 0
+    if (lo >= 0) return F(hi) - (lo > 0 ? F(lo - 1) : 0.0);
+    if (hi <= 0) return F(-lo) - (hi < 0 ? F(-hi - 1) : 0.0);
+    return F(-lo) + F(hi);
+}
+
+// The kernel weights of a disc of radius r >= 1 centred at (x, y), summed over the cells inside
+// the w x h grid, in FP64: each row ay of the disc (4 (dx^2 + ay^2) <= (2r + 1)^2, i.e.
+// dx^2 <= r^2 + r - ay^2) clipped to the grid adds nf ((1 - ay^2/rho^2) n - sum dx^2 / rho^2),
+// rho = r + 0.5, nf = 0.63661977236 / r^2 — the density_frag.glsl kernel in closed form.
+__host__ __device__ inline double disc_weight_sum(int r, int x, int y, int w, int h) {
+    const double rho2 = (r + 0.5) * (r + 0.5), nf = 0.63661977236 / (double)(r * r);
+    const int y0 = -r > -y ? -r : -y, y1 = r < h - 1 - y ? r : h - 1 - y;
+    double s = 0.0;
+    for (int dy = y0; dy <= y1; dy++) {
+        const int lim = r * r + r - dy * dy;
+        int sx = (int)sqrt((double)lim);
+        while ((sx + 1) * (sx + 1) <= lim) sx++;
+        while (sx * sx > lim) sx--;
+        const int lo = -sx > -x ? -sx : -x, hi = sx < w - 1 - x ? sx : w - 1 - x;
+        if (lo > hi) continue;
+        s += (1.0 - (double)(dy * dy) / rho2) * (double)(hi - lo + 1) - square_sum(lo, hi) / rho2;
+    }
+    return nf * s;
+}
+
+// pass 1 of the fused image tail: the radius per bin, and the total density of the estimator's
+// output, sum_out a = sum over bins of a * (the kernel weights of its disc inside the grid), in
+// FP64 — the log-density scale's sum (k2 = W * H / sum a) without a pass over the output.
+__global__ void de_radius_sum_kernel(const float4* __restrict__ in, uint32_t w, uint32_t h, const DeTables T,
+                                     uint8_t* __restrict__ rad, double* __restrict__ sum_out) {
+    const uint32_t n = w * h;  // < 2^32 (the caller's grids hold fewer bins)
+    double s = 0.0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float a = in[i].w;
+        if (a == 0.0f || a != a) {
+            rad[i] = 255;
+            continue;
+        }
+        const int r = de_radius(a, T);
+        rad[i] = (uint8_t)r;
+        const int y = (int)(i / w), x = (int)(i - (uint32_t)y * w);
+        const bool inside = x >= r && y >= r && x + r < (int)w && y + r < (int)h;
+        const double ws = (r == 0) ? 1.0 : inside ? T.wsum[r] : disc_weight_sum(r, x, y, (int)w, (int)h);
+        s += (double)a * ws;
+    }
+    block_sum_to(s, sum_out);
+}
+
+// tonemap.glsl:26: the per-bin log-density scale 0.5*brightness*log10(1 + a*k)/a (a > 0)
+__device__ __forceinline__ float tonemap_log_scale(float a, float k, float brightness) {
+    return 0.5f * brightness * log1pf(a * k) * 0.434294481903251827651128918916f / a;
+}
+
+// tonemap.glsl:28-37 on a filtered (r, g, b, a): z = a^(1/gamma), rgb = clamp(mix(rgb^(1/gamma),
+// (z/a)*rgb, vibrancy)), alpha 1; no density is opaque black
+__device__ __forceinline__ float4 tonemap_finish(float r, float g, float b, float a, float gamma, float vibrancy) {
+    if (!(a > 0.0f)) return make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    const float ig = 1.0f / gamma;
+    const float gf = powf(a, ig) / a;
+    const float rgb[3] = {r, g, b};
+    float res[3];
+    for (int q = 0; q < 3; q++) {
+        const float v = powf(rgb[q], ig) * (1.0f - vibrancy) + gf * rgb[q] * vibrancy;
+        res[q] = fminf(fmaxf(v, 0.0f), 1.0f);
+    }
+    return make_float4(res[0], res[1], res[2], 1.0f);
+}
+
+// tonemap.glsl:18-38 for one output pixel from its ss x ss block of bins (rows `stride` apart):
+// per bin c *= 0.5*brightness*log10(1 + a*k)/a, mean over the block, then tonemap_finish.
+__device__ __forceinline__ float4 tonemap_block(const float4* src, size_t stride, uint32_t ss, float k, float gamma,
+                                                float brightness, float vibrancy) {
+    float4 acc = make_float4(0, 0, 0, 0);
+    for (uint32_t j = 0; j < ss; j++) {
+        const float4* row = src + (size_t)j * stride;
+        for (uint32_t i = 0; i < ss; i++) {
+            const float4 c = row[i];
+            if (c.w > 0.0f) {
+                const float ls = tonemap_log_scale(c.w, k, brightness);
+                acc.x = fmaf(c.x, ls, acc.x);
+                acc.y = fmaf(c.y, ls, acc.y);
+                acc.z = fmaf(c.z, ls, acc.z);
+                acc.w = fmaf(c.w, ls, acc.w);
+            }
+        }
+    }
+    const float inv = 1.0f / (float)(ss * ss);
+    return tonemap_finish(acc.x * inv, acc.y * inv, acc.z * inv, acc.w * inv, gamma, vibrancy);
+}
+
+// the log-density scale: k2 when given, else bins / sum(a) from the FP64 statistics
+__device__ __forceinline__ float tonemap_scale(float k2, const double* stats, uint32_t w, uint32_t h) {
+    if (k2 > 0.0f) return k2;
+    const double sum = stats ? stats[0] : 0.0;
+    return sum > 0.0 ? (float)((double)w * (double)h / sum) : 1.0f;
+}
+
+__device__ __forceinline__ uchar4 to_rgba8(float4 o) {
+    return make_uchar4((unsigned char)lrintf(o.x * 255.0f), (unsigned char)lrintf(o.y * 255.0f),
+                       (unsigned char)lrintf(o.z * 255.0f), 255);
+}
+
+// the tonemap a DE tile kernel applies to its own output (TM = true)
+struct TmArgs {
+    uint32_t ss;
+    float gamma, brightness, vibrancy, k2;
+    const double* stats;  // [0] = sum of the estimator's output density (k2 <= 0)
+    float4* out_f32;      // (w / ss) x (h / ss), may be null
+    uchar4* out8;         // may be null
+};
+
 // pass 2: a CTA owns a 32 x 8 output tile.  It stages the colours and radii of the tile and
 // its R halo in shared memory and forms each output bin as a gather in one of two ways, chosen
 // per tile by their work:
@@ -66,15 +195,18 @@ __global__ void de_radius_kernel(const float4* __restrict__ in, size_t n, const 
 // sparse fringes full of large discs take the box.  The sum is deterministic either way.
 constexpr int kDsX = 32, kDsY = 8, kDsThreads = 256;
 
-template <int R>
+// With TM the tile's output stays in shared memory and the CTA tonemaps its (32/ss) x (8/ss)
+// output pixels from it (ss dividing 8): the estimator's output never goes through DRAM.
+template <int R, bool TM = false>
 __host__ __device__ constexpr size_t de_tile_smem() {
-    return (size_t)(kDsX + 2 * R) * (kDsY + 2 * R) * (16 + 4 + 1) + 16 + 64 + 4 * (kDsY + 2 * R);
+    return (((size_t)(kDsX + 2 * R) * (kDsY + 2 * R) * (16 + 4 + 1) + 16 + 64 + 4 * (kDsY + 2 * R) + 15) & ~(size_t)15) +
+           (TM ? (size_t)kDsX * kDsY * 16 : 0);
 }
 
-template <int R>
+template <int R, bool TM = false>
 __global__ void __launch_bounds__(kDsThreads) de_tile_kernel(
     const float4* __restrict__ in, const uint8_t* __restrict__ rad, uint32_t w, uint32_t h,
-    const float* __restrict__ weights, const DeTables T, float4* __restrict__ out) {
+    const float* __restrict__ weights, const DeTables T, float4* __restrict__ out, const TmArgs tm) {
     constexpr int SW = kDsX + 2 * R, SH = kDsY + 2 * R, NS = SW * SH, NO = kDsX * kDsY;
     extern __shared__ __align__(16) unsigned char smem[];
     float4* s_c = reinterpret_cast<float4*>(smem);                  // NS colours
@@ -82,6 +214,7 @@ __global__ void __launch_bounds__(kDsThreads) de_tile_kernel(
     uint8_t* s_r = reinterpret_cast<uint8_t*>(s_list + NS);         // NS radii (255: empty)
     int* s_stat = reinterpret_cast<int*>(s_r + ((NS + 15) & ~15));  // [0] rmax, [1..8] per-warp counts
     int* s_rowmax = s_stat + 16;                                     // SH: largest radius per staged row
+    float4* s_out = reinterpret_cast<float4*>(smem + ((de_tile_smem<R, false>() + 15) & ~(size_t)15));  // TM: NO outputs
     const int tx0 = blockIdx.x * kDsX, ty0 = blockIdx.y * kDsY;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_stat[0] = 0;
@@ -179,13 +312,33 @@ __global__ void __launch_bounds__(kDsThreads) de_tile_kernel(
             }
         }
         const int gx = tx0 + ox, gy = ty0 + oy;
-        if (gx < (int)w && gy < (int)h) out[(size_t)gy * w + gx] = a4;
+        if (out && gx < (int)w && gy < (int)h) out[(size_t)gy * w + gx] = a4;
+        if (TM) s_out[o] = a4;
+    }
+    if (TM) {
+        __syncthreads();
+        const uint32_t ss = tm.ss, pw = kDsX / ss, ph = kDsY / ss, ow = w / ss, oh = h / ss;
+        const float k = tonemap_scale(tm.k2, tm.stats, w, h);
+        for (uint32_t p = threadIdx.x; p < pw * ph; p += kDsThreads) {
+            const uint32_t px = p % pw, py = p / pw;
+            const uint32_t gx = tx0 / ss + px, gy = ty0 / ss + py;
+            if (gx >= ow || gy >= oh) continue;
+            const float4 o = tonemap_block(s_out + (size_t)py * ss * kDsX + px * ss, kDsX, ss, k, tm.gamma,
+                                           tm.brightness, tm.vibrancy);
+            const size_t oi = (size_t)gy * ow + gx;
+            if (tm.out_f32) tm.out_f32[oi] = o;
+            if (tm.out8) tm.out8[oi] = to_rgba8(o);
+        }
     }
 }
 
 template <int R>
 static cudaError_t set_de_tile_smem() {
-    return cudaFuncSetAttribute(de_tile_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)de_tile_smem<R>());
+    cudaError_t e = cudaFuncSetAttribute(de_tile_kernel<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)de_tile_smem<R, false>());
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(de_tile_kernel<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)de_tile_smem<R, true>());
 }
 
 // the DE kernels' shared-memory limits, set once per device before any launch (also before a
@@ -206,12 +359,14 @@ cudaError_t density_prepare() {
 
 template <int R>
 static cudaError_t launch_de_tile(const float4* in, const uint8_t* rad, uint32_t w, uint32_t h, const float* dw,
-                                  const DeTables& T, float4* out, cudaStream_t st) {
-    const size_t smem = de_tile_smem<R>();
+                                  const DeTables& T, float4* out, cudaStream_t st, const TmArgs* tm = nullptr) {
     cudaError_t e = density_prepare();
     if (e != cudaSuccess) return e;
     const dim3 grid((w + kDsX - 1) / kDsX, (h + kDsY - 1) / kDsY);
-    de_tile_kernel<R><<<grid, kDsThreads, smem, st>>>(in, rad, w, h, dw, T, out);
+    if (tm)
+        de_tile_kernel<R, true><<<grid, kDsThreads, de_tile_smem<R, true>(), st>>>(in, rad, w, h, dw, T, out, *tm);
+    else
+        de_tile_kernel<R, false><<<grid, kDsThreads, de_tile_smem<R, false>(), st>>>(in, rad, w, h, dw, T, out, TmArgs{});
     return cudaGetLastError();
 }
 
@@ -289,52 +444,143 @@ __global__ void stats_kernel(const float4* __restrict__ in, size_t n, double* ou
     }
 }
 
-// tonemap.glsl:18-38 with an ss x ss box filter: per bin c *= 0.5*brightness*log10(1 + a*k2)/a,
-// mean over the block, then z = a^(1/gamma), rgb = clamp(mix(rgb^(1/gamma), (z/a)*rgb, vibrancy)).
-// A block with no density (where the shader would divide 0 by 0) is opaque black.
+// tonemap.glsl:18-38 with an ss x ss box filter (tonemap_block), one output pixel per thread
 __global__ void tonemap_kernel(const float4* __restrict__ in, uint32_t w, uint32_t h, uint32_t ss, float gamma,
                                float brightness, float vibrancy, float k2, const double* __restrict__ stats,
                                float4* __restrict__ out_f32, uchar4* __restrict__ out8) {
     const uint32_t ow = w / ss, oh = h / ss;
     const uint32_t ox = blockIdx.x * blockDim.x + threadIdx.x, oy = blockIdx.y;
     if (ox >= ow || oy >= oh) return;
-    float k = k2;
-    if (!(k > 0.0f)) {
-        const double sum = stats ? stats[0] : 0.0;
-        k = sum > 0.0 ? (float)((double)w * (double)h / sum) : 1.0f;
-    }
-    float4 acc = make_float4(0, 0, 0, 0);
-    for (uint32_t j = 0; j < ss; j++) {
-        const float4* row = in + (size_t)(oy * ss + j) * w + (size_t)ox * ss;
-        for (uint32_t i = 0; i < ss; i++) {
-            const float4 c = row[i];
-            if (c.w > 0.0f) {
-                const float ls = 0.5f * brightness * log1pf(c.w * k) * 0.434294481903251827651128918916f / c.w;
-                acc.x = fmaf(c.x, ls, acc.x);
-                acc.y = fmaf(c.y, ls, acc.y);
-                acc.z = fmaf(c.z, ls, acc.z);
-                acc.w = fmaf(c.w, ls, acc.w);
-            }
-        }
-    }
-    const float inv = 1.0f / (float)(ss * ss);
-    float4 o = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
-    const float a = acc.w * inv;
-    if (a > 0.0f) {
-        const float ig = 1.0f / gamma;
-        const float gf = powf(a, ig) / a;
-        const float rgb[3] = {acc.x * inv, acc.y * inv, acc.z * inv};
-        float res[3];
-        for (int q = 0; q < 3; q++) {
-            const float v = powf(rgb[q], ig) * (1.0f - vibrancy) + gf * rgb[q] * vibrancy;
-            res[q] = fminf(fmaxf(v, 0.0f), 1.0f);
-        }
-        o = make_float4(res[0], res[1], res[2], 1.0f);
-    }
+    const float k = tonemap_scale(k2, stats, w, h);
+    const float4 o = tonemap_block(in + (size_t)oy * ss * w + (size_t)ox * ss, w, ss, k, gamma, brightness, vibrancy);
     const size_t oi = (size_t)oy * ow + ox;
     if (out_f32) out_f32[oi] = o;
-    if (out8) out8[oi] = make_uchar4((unsigned char)lrintf(o.x * 255.0f), (unsigned char)lrintf(o.y * 255.0f),
-                                     (unsigned char)lrintf(o.z * 255.0f), 255);
+    if (out8) out8[oi] = to_rgba8(o);
+}
+
+// The tonemap with flam3's spatial filter in place of the ss x ss box (no counterpart in the
+// reference, which ignores flam3's filter and filter_shape, flame.cpp:166-176): output pixel
+// (ox, oy) is the weighted sum, by the separable taps c[i] c[j], of the log-scaled bins of the
+// fwidth x fwidth window starting at (ox ss - pad, oy ss - pad), pad = (fwidth - ss) / 2, then
+// tonemap_finish.  A CTA stages the log-scaled bins of its tile's windows once in shared memory.
+struct FilterArgs {
+    int fwidth, pad;
+    int tw, th;        // output pixels per CTA tile
+    float taps[kMaxFilterTaps];
+};
+
+__global__ void __launch_bounds__(256) tonemap_filter_kernel(const float4* __restrict__ in, uint32_t w, uint32_t h,
+                                                             uint32_t ss, float gamma, float brightness,
+                                                             float vibrancy, float k2, const double* __restrict__ stats,
+                                                             const FilterArgs F, float4* __restrict__ out_f32,
+                                                             uchar4* __restrict__ out8) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4* s_l = reinterpret_cast<float4*>(smem);
+    const int rw = F.tw * (int)ss + F.fwidth - (int)ss, rh = F.th * (int)ss + F.fwidth - (int)ss;
+    const int ox0 = blockIdx.x * F.tw, oy0 = blockIdx.y * F.th;
+    const int gx0 = ox0 * (int)ss - F.pad, gy0 = oy0 * (int)ss - F.pad;
+    const float k = tonemap_scale(k2, stats, w, h);
+    for (int i = threadIdx.x; i < rw * rh; i += blockDim.x) {
+        const int gx = gx0 + i % rw, gy = gy0 + i / rw;
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (gx >= 0 && gy >= 0 && gx < (int)w && gy < (int)h) {
+            const float4 c = in[(size_t)gy * w + gx];
+            if (c.w > 0.0f) {
+                const float ls = tonemap_log_scale(c.w, k, brightness);
+                v = make_float4(c.x * ls, c.y * ls, c.z * ls, c.w * ls);
+            }
+        }
+        s_l[i] = v;
+    }
+    __syncthreads();
+    const uint32_t ow = w / ss, oh = h / ss;
+    for (int p = threadIdx.x; p < F.tw * F.th; p += blockDim.x) {
+        const int px = p % F.tw, py = p / F.tw;
+        const uint32_t ox = ox0 + px, oy = oy0 + py;
+        if (ox >= ow || oy >= oh) continue;
+        float4 acc = make_float4(0, 0, 0, 0);
+        for (int j = 0; j < F.fwidth; j++) {
+            const float4* row = s_l + (size_t)(py * (int)ss + j) * rw + px * (int)ss;
+            float4 r = make_float4(0, 0, 0, 0);
+            for (int i = 0; i < F.fwidth; i++) {
+                const float4 v = row[i];
+                const float c = F.taps[i];
+                r.x = fmaf(v.x, c, r.x);
+                r.y = fmaf(v.y, c, r.y);
+                r.z = fmaf(v.z, c, r.z);
+                r.w = fmaf(v.w, c, r.w);
+            }
+            const float c = F.taps[j];
+            acc.x = fmaf(r.x, c, acc.x);
+            acc.y = fmaf(r.y, c, acc.y);
+            acc.z = fmaf(r.z, c, acc.z);
+            acc.w = fmaf(r.w, c, acc.w);
+        }
+        const float4 o = tonemap_finish(acc.x, acc.y, acc.z, acc.w, gamma, vibrancy);
+        const size_t oi = (size_t)oy * ow + ox;
+        if (out_f32) out_f32[oi] = o;
+        if (out8) out8[oi] = to_rgba8(o);
+    }
+}
+
+// flam3's filter functions and their supports: Gaussian exp(-2x^2) sqrt(2/pi) on [-1.5, 1.5],
+// box on [-0.5, 0.5], triangle 1 - |x| and the cubic Hermite 2|x|^3 - 3x^2 + 1 on [-1, 1]
+static double filter_support(int shape) { return shape == RF_FILTER_BOX ? 0.5 : (shape == RF_FILTER_GAUSSIAN ? 1.5 : 1.0); }
+static double filter_value(int shape, double x) {
+    const double t = std::fabs(x);
+    switch (shape) {
+        case RF_FILTER_GAUSSIAN: return std::exp(-2.0 * x * x) * std::sqrt(2.0 / 3.14159265358979323846);
+        case RF_FILTER_BOX: return t <= 0.5 ? 1.0 : 0.0;
+        case RF_FILTER_TRIANGLE: return t < 1.0 ? 1.0 - t : 0.0;
+        case RF_FILTER_HERMITE: return t < 1.0 ? (2.0 * t - 3.0) * t * t + 1.0 : 0.0;
+        default: return 0.0;
+    }
+}
+
+// The taps: the window spans fw = 2 * support * ss * radius bins, rounded up to an integer width
+// of the parity of ss (so it centres on the output pixel's ss x ss block), sampled at each
+// cell's centre with the coordinate stretched so the window covers the support, normalised in
+// FP64.  Returns fwidth, or -1 beyond kMaxFilterTaps.
+int filter_taps(uint32_t ss, float radius, int shape, float* taps) {
+    const double support = filter_support(shape);
+    const double fw = 2.0 * support * (double)ss * (double)radius;
+    int fwidth = (int)fw + 1;
+    if ((fwidth ^ (int)ss) & 1) fwidth++;
+    if (fwidth > kMaxFilterTaps) return -1;
+    const double adjust = fw > 0.0 ? support * (double)fwidth / fw : 1.0;
+    double t[kMaxFilterTaps], sum = 0.0;
+    for (int i = 0; i < fwidth; i++) {
+        t[i] = filter_value(shape, ((2.0 * i + 1.0) / (double)fwidth - 1.0) * adjust);
+        sum += t[i];
+    }
+    for (int i = 0; i < fwidth; i++) taps[i] = (float)(t[i] / sum);
+    return fwidth;
+}
+
+cudaError_t launch_tonemap_filter(const float4* in, uint32_t w, uint32_t h, uint32_t ss, float radius, int shape,
+                                  float gamma, float brightness, float vibrancy, float k2, const double* stats,
+                                  float4* out_f32, uchar4* out8, cudaStream_t st) {
+    FilterArgs F{};
+    F.fwidth = filter_taps(ss, radius, shape, F.taps);
+    if (F.fwidth < 0) return cudaErrorInvalidValue;
+    F.pad = (F.fwidth - (int)ss) / 2;
+    // the largest tile whose staged windows fit in 96 KB of shared memory
+    static const int tiles[][2] = {{32, 8}, {16, 8}, {8, 8}, {8, 4}, {4, 4}, {2, 2}, {1, 1}};
+    size_t smem = 0;
+    for (const auto& t : tiles) {
+        F.tw = t[0];
+        F.th = t[1];
+        smem = (size_t)(F.tw * ss + F.fwidth - ss) * (F.th * ss + F.fwidth - ss) * sizeof(float4);
+        if (smem <= 96 * 1024) break;
+    }
+    if (smem > 96 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(tonemap_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+    if (e != cudaSuccess) return e;
+    const uint32_t ow = w / ss, oh = h / ss;
+    const dim3 grid((ow + F.tw - 1) / F.tw, (oh + F.th - 1) / F.th);
+    tonemap_filter_kernel<<<grid, 256, smem, st>>>(in, w, h, ss, gamma, brightness, vibrancy, k2, stats, F, out_f32,
+                                                   out8);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -361,6 +607,8 @@ static void de_tables(int R, int min_r, float curve, DeTables& T, std::vector<fl
                 const int d2 = ax * ax + ay * ay;
                 wts.push_back(r == 0 ? 1.0f : (float)((1.0 - (double)d2 / den) * nf));
             }
+        // the whole disc's weights (far from the grid's edges)
+        T.wsum[r] = r == 0 ? 1.0 : disc_weight_sum(r, r, r, 2 * r + 1, 2 * r + 1);
     }
 }
 
@@ -393,30 +641,66 @@ size_t density_weight_count(int R, int min_r) {
     return n;
 }
 
+// the tile kernel for the largest radius (rmax <= kDeMaxSmemR)
+static cudaError_t launch_tile_for(int rmax, const float4* in, const uint8_t* rad, uint32_t w, uint32_t h,
+                                   const float* dw, const DeTables& T, float4* out, cudaStream_t st,
+                                   const TmArgs* tm) {
+    if (rmax <= 3) return launch_de_tile<3>(in, rad, w, h, dw, T, out, st, tm);
+    if (rmax <= 6) return launch_de_tile<6>(in, rad, w, h, dw, T, out, st, tm);
+    if (rmax <= 9) return launch_de_tile<9>(in, rad, w, h, dw, T, out, st, tm);
+    return launch_de_tile<kDeMaxSmemR>(in, rad, w, h, dw, T, out, st, tm);
+}
+
 static cudaError_t launch_density_passes(const float4* in, uint32_t w, uint32_t h, const DeTables& T, float4* out,
                                          uint8_t* rad, const float* dw, cudaStream_t st) {
     const size_t n = (size_t)w * h;
     de_radius_kernel<<<1024, 256, 0, st>>>(in, n, T, rad);
     const int rmax = T.R > T.min_r ? T.R : T.min_r;
-    if (rmax <= 3) return launch_de_tile<3>(in, rad, w, h, dw, T, out, st);
-    if (rmax <= 6) return launch_de_tile<6>(in, rad, w, h, dw, T, out, st);
-    if (rmax <= 9) return launch_de_tile<9>(in, rad, w, h, dw, T, out, st);
-    if (rmax <= kDeMaxSmemR) return launch_de_tile<kDeMaxSmemR>(in, rad, w, h, dw, T, out, st);
-    else de_gather_global_kernel<<<dim3((w + 127) / 128, h), 128, 0, st>>>(in, rad, w, h, dw, T, out);
+    if (rmax <= kDeMaxSmemR) return launch_tile_for(rmax, in, rad, w, h, dw, T, out, st, nullptr);
+    de_gather_global_kernel<<<dim3((w + 127) / 128, h), 128, 0, st>>>(in, rad, w, h, dw, T, out);
     return cudaGetLastError();
 }
 
-// The same two passes with scratch the caller provides (a byte per bin for the radii, `dw_cap`
-// floats for the kernel weights); nothing is allocated.
-cudaError_t launch_density_scratch(const float4* in, uint32_t w, uint32_t h, int R, int min_r, float curve,
-                                   float4* out, uint8_t* rad, float* dw, size_t dw_cap, cudaStream_t st) {
+bool density_tonemap_fused(int R, int min_r, uint32_t ss) {
+    const int rmax = R > min_r ? R : min_r;
+    return rmax <= kDeMaxSmemR && ss >= 1 && kDsX % ss == 0 && kDsY % ss == 0;
+}
+
+// The image tail of a frame (main.cpp:490-535: the density-estimation raster pass, then the
+// tonemap pass) in two passes: pass 1 finds every bin's radius and, for an automatic k2, the FP64
+// density sum of the estimator's output (de_radius_sum_kernel); pass 2 estimates each 32 x 8 tile
+// in shared memory and tonemaps it there, so the estimator's FP32 output never reaches DRAM.
+// Where that does not apply (density_tonemap_fused false: ss does not divide the tile, or radii
+// beyond the shared-memory path) the estimator writes `de_scratch`, then the statistics and
+// tonemap passes run on it.  rad: a byte per bin; dw: the weight table (density_weights);
+// stats: 3 doubles.
+cudaError_t launch_density_tonemap(const float4* in, uint32_t w, uint32_t h, int R, int min_r, float curve,
+                                   uint32_t ss, float gamma, float brightness, float vibrancy, float k2,
+                                   float4* out_f32, uchar4* out8, uint8_t* rad, const float* dw, double* stats,
+                                   float4* de_scratch, cudaStream_t st) {
     DeTables T;
     std::vector<float> wts;
     de_tables(R, min_r, curve, T, wts);
-    if (wts.size() > dw_cap) return cudaErrorInvalidValue;
-    cudaError_t e = cudaMemcpyAsync(dw, wts.data(), wts.size() * sizeof(float), cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return e;
-    return launch_density_passes(in, w, h, T, out, rad, dw, st);
+    const bool need_sum = !(k2 > 0.0f);
+    cudaError_t e;
+    if (!density_tonemap_fused(R, min_r, ss)) {
+        if (!de_scratch) return cudaErrorInvalidValue;
+        e = launch_density_passes(in, w, h, T, de_scratch, rad, dw, st);
+        if (e == cudaSuccess && need_sum) e = launch_stats(de_scratch, w, h, stats, st);
+        if (e == cudaSuccess)
+            e = launch_tonemap(de_scratch, w, h, ss, gamma, brightness, vibrancy, k2, need_sum ? stats : nullptr,
+                               out_f32, out8, st);
+        return e;
+    }
+    if (need_sum) {
+        e = cudaMemsetAsync(stats, 0, 3 * sizeof(double), st);
+        if (e != cudaSuccess) return e;
+        de_radius_sum_kernel<<<1024, 256, 0, st>>>(in, w, h, T, rad, stats);
+    } else {
+        de_radius_kernel<<<1024, 256, 0, st>>>(in, (size_t)w * h, T, rad);
+    }
+    const TmArgs tm{ss, gamma, brightness, vibrancy, k2, need_sum ? stats : nullptr, out_f32, out8};
+    return launch_tile_for(R > min_r ? R : min_r, in, rad, w, h, dw, T, nullptr, st, &tm);
 }
 
 void density_weights(int R, int min_r, std::vector<float>& wts) {

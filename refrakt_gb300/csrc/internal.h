@@ -100,7 +100,8 @@ struct Genome {
     float gamma = 0, vibrancy = 0, brightness = 0;
     // flam3 fields the reference ignores, kept for output framing
     unsigned supersample = 1;
-    float filter = 0;
+    float filter = 0;      // spatial filter radius (output pixels); 0: the ss x ss box
+    int filter_shape = 0;  // rf_filter_shape
 };
 
 int genome_from_xml(const std::string& xml, const Registry& reg, Genome& g);

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "chaos_args.h"
+#include "refrakt.h"
 
 namespace rfk {
 
@@ -28,9 +29,6 @@ cudaError_t launch_probe(const uint32_t* prog, int xform, uint32_t n, const floa
 cudaError_t launch_density(const float4* in, uint32_t w, uint32_t h, int radius, int min_radius, float curve,
                            float4* out, cudaStream_t st);
 size_t density_weight_count(int radius, int min_radius);
-cudaError_t launch_density_scratch(const float4* in, uint32_t w, uint32_t h, int radius, int min_radius, float curve,
-                                   float4* out, uint8_t* radius_scratch, float* weight_scratch,
-                                   size_t weight_capacity, cudaStream_t st);
 // Kernel weights of density estimation depend on the radii alone: `density_weights` builds them on
 // the host, and `launch_density_resident` runs both passes with those weights already on the
 // device (`dw`) and a byte of radius scratch per bin (`rad`) — no allocation and no host copy,
@@ -46,5 +44,20 @@ cudaError_t launch_stats(const float4* in, uint32_t w, uint32_t h, double* out3,
 cudaError_t launch_tonemap(const float4* in, uint32_t w, uint32_t h, uint32_t ss, float gamma, float brightness,
                            float vibrancy, float k2, const double* stats, float4* out_f32, uchar4* out8,
                            cudaStream_t st);
+// The tonemap with flam3's spatial filter (rf_filter_shape) in place of the ss x ss box; taps
+// (filter_taps, at most kMaxFilterTaps: 2 * support * ss * radius < 63) normalised on the host.
+constexpr int kMaxFilterTaps = 64;
+int filter_taps(uint32_t ss, float radius, int shape, float* taps);
+cudaError_t launch_tonemap_filter(const float4* in, uint32_t w, uint32_t h, uint32_t ss, float radius, int shape,
+                                  float gamma, float brightness, float vibrancy, float k2, const double* stats,
+                                  float4* out_f32, uchar4* out8, cudaStream_t st);
+// Density estimation and tonemap in one sequence (image.cu): with density_tonemap_fused the
+// estimator's output stays on chip and `de_scratch` is not touched (may be null); otherwise it is
+// the estimator's output.  rad: a byte per bin; dw: density_weights(R, min_r); stats: 3 doubles.
+bool density_tonemap_fused(int radius, int min_radius, uint32_t ss);
+cudaError_t launch_density_tonemap(const float4* in, uint32_t w, uint32_t h, int radius, int min_radius, float curve,
+                                   uint32_t ss, float gamma, float brightness, float vibrancy, float k2,
+                                   float4* out_f32, uchar4* out8, uint8_t* rad, const float* dw, double* stats,
+                                   float4* de_scratch, cudaStream_t st);
 
 }  // namespace rfk

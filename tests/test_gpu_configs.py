@@ -227,6 +227,36 @@ def test_render_matches_stepwise(rk, compiler, genome, size, ss, reset):
     b.close()
 
 
+def test_render_applies_the_genome_spatial_filter(rk, compiler):
+    """The reference genome carries filter="1" filter_shape="gaussian": rf_render at supersample 4
+    draws the Gaussian window over the density-estimated bins, as rf_density_estimate followed by
+    rf_tonemap_filter on a simulation with the same seed."""
+    xml = _xml(SHEEP)
+    f = rk.Flame.from_xml(xml, compiler)
+    info = f.info()
+    assert info["filter"] == 1.0 and info["filter_shape"] == rk.FILTER_GAUSSIAN
+    W, H, ss, n = 100, 74, 4, 16384
+    points = 32 * W * ss * H * ss
+    a = rk.Sim(n, seed=4)
+    img, st = a.render(f, W, H, points, supersample=ss, fuse_passes=20, density_estimation=True)
+    b = rk.Sim(n, seed=4)
+    bins = torch.zeros(H * ss, W * ss, 4, device="cuda")
+    hits = torch.zeros(H * ss, W * ss, dtype=torch.int32, device="cuda")
+    b.warmup(f, 19, tss_width=0.0)
+    b.draw_to_bins(f, bins, hits, W * ss, H * ss, (points + n - 1) // n)
+    de = torch.zeros_like(bins)
+    rk.density_estimate(bins, W * ss, H * ss, info["estimator_radius"], info["estimator_min"],
+                        info["estimator_curve"], de)
+    want = torch.zeros(H, W, 4, dtype=torch.uint8, device="cuda")
+    rk.tonemap_filter(de, W * ss, H * ss, ss, info["filter"], info["filter_shape"], info["gamma"],
+                      info["brightness"], info["vibrancy"], 0.0, None, want)
+    torch.cuda.synchronize()
+    d = np.abs(img.astype(np.int32) - want.cpu().numpy().astype(np.int32))
+    assert d.max() <= 1 and (d > 0).mean() <= 1e-3
+    a.close()
+    b.close()
+
+
 def test_render_quality_stop(rk, compiler):
     """stop_on_binned: passes are drawn until the binned count reaches the target (the reference's
     accumulated < quality * W * H loop, main.cpp:411-412); walker-steps exceed it by the points

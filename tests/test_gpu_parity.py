@@ -262,6 +262,56 @@ def test_tonemap_matches_oracle(rk, orc, small_hist, ss, k2):
     assert np.max(np.abs(img8.cpu().numpy().astype(np.int32) - np.rint(ref * 255))) <= 1
 
 
+@pytest.mark.parametrize("R,mn,curve,ss,k2", [(9, 0, 0.4, 1, 0.0), (9, 0, 0.4, 2, 0.0), (5, 1, 0.6, 4, 1e-3),
+                                              (12, 0, 0.3, 8, 0.0), (3, 0, 0.5, 2, 1e-2), (20, 0, 0.3, 2, 0.0),
+                                              (6, 0, 0.4, 3, 0.0), (0, 2, 0.4, 1, 0.0)])
+def test_density_tonemap_matches_separate_passes(rk, small_hist, R, mn, curve, ss, k2):
+    """rf_density_tonemap (the estimator's output tonemapped on chip, k2 from the radius pass's
+    density sum) against rf_density_estimate followed by rf_tonemap; R = 20 and ss = 3 take the
+    unfused sequence.  The density sums differ only in FP64 summation order."""
+    W, H, bins = small_hist
+    W, H = W - W % ss, H - H % ss
+    b = bins[:H, :W].contiguous()
+    de = torch.zeros_like(b)
+    rk.density_estimate(b, W, H, R, mn, curve, de)
+    want = torch.zeros(H // ss, W // ss, 4, device="cuda")
+    want8 = torch.zeros(H // ss, W // ss, 4, dtype=torch.uint8, device="cuda")
+    rk.tonemap(de, W, H, ss, 2.2, 4.0, 0.8, k2, want, want8)
+    got = torch.zeros_like(want)
+    got8 = torch.zeros_like(want8)
+    rk.density_tonemap(b, W, H, R, mn, curve, ss, 2.2, 4.0, 0.8, k2, got, got8)
+    torch.cuda.synchronize()
+    assert np.allclose(got.cpu().numpy(), want.cpu().numpy(), atol=2e-6)
+    d = np.abs(got8.cpu().numpy().astype(np.int32) - want8.cpu().numpy().astype(np.int32))
+    assert d.max() <= 1 and (d > 0).mean() < 1e-3
+
+
+@pytest.mark.parametrize("ss,radius,shape,k2", [(2, 1.0, 0, 0.0), (4, 1.0, 0, 1e-3), (1, 0.7, 0, 0.0), (3, 1.0, 3, 0.0),
+                                               (2, 1.5, 2, 1e-2), (2, 1.0, 1, 0.0), (4, 2.5, 0, 0.0)])
+def test_flam3_spatial_filter_matches_oracle(rk, orc, small_hist, ss, radius, shape, k2):
+    """rf_tonemap_filter (flam3's filter / filter_shape, which the reference ignores) against the
+    oracle's FP64 restatement: taps, window placement at the grid's edges, log scaling, finish."""
+    W, H, bins = small_hist
+    W, H = W - W % ss, H - H % ss
+    b = bins[:H, :W].contiguous()
+    img = torch.zeros(H // ss, W // ss, 4, device="cuda")
+    img8 = torch.zeros(H // ss, W // ss, 4, dtype=torch.uint8, device="cuda")
+    rk.tonemap_filter(b, W, H, ss, radius, shape, 2.2, 4.0, 0.8, k2, img, img8)
+    torch.cuda.synchronize()
+    bb = b.cpu().numpy().astype(np.float64)
+    kk = k2 if k2 > 0 else W * H / bb[..., 3].sum()
+    ref = orc.tonemap_filter(bb, ss, radius, shape, 2.2, 4.0, 0.8, kk)
+    assert np.allclose(img.cpu().numpy(), ref, atol=2e-5)
+    assert np.max(np.abs(img8.cpu().numpy().astype(np.int32) - np.rint(ref * 255))) <= 1
+    # radius 0 is the ss x ss box of rf_tonemap
+    box = torch.zeros_like(img)
+    rk.tonemap_filter(b, W, H, ss, 0.0, shape, 2.2, 4.0, 0.8, k2, box, None)
+    want = torch.zeros_like(img)
+    rk.tonemap(b, W, H, ss, 2.2, 4.0, 0.8, k2, want, None)
+    torch.cuda.synchronize()
+    assert torch.equal(box, want)
+
+
 def test_hist_stats_fp64(rk, small_hist):
     W, H, bins = small_hist
     st = rk.hist_stats(bins, W, H)

@@ -120,3 +120,19 @@ def test_tonemap_supersample_box(orc):
     two = orc.tonemap(img, 2.2, 4.0, 1.0, 1e-2, ss=2)
     assert two.shape == (4, 4, 4)
     assert np.all((two[..., :3] >= 0) & (two[..., :3] <= 1)) and np.all(two[..., 3] == 1)
+
+
+def test_flam3_filter_box_window_is_the_supersample_box(orc):
+    """flam3's box filter of radius 1 at supersample 2 has taps (0, 1/2, 1/2, 0): the window is the
+    output pixel's own 2 x 2 block, so the filtered tonemap equals the box tonemap; the Gaussian
+    taps are symmetric and normalised, their window of the parity of ss."""
+    rng = np.random.default_rng(3)
+    img = rng.uniform(0, 5, (24, 32, 4))
+    img[rng.uniform(size=(24, 32)) < 0.3] = 0.0
+    a = orc.tonemap_filter(img, 2, 1.0, 1, 2.2, 4.0, 0.8, 0.05)
+    b = orc.tonemap(img, 2.2, 4.0, 0.8, 0.05, ss=2)
+    assert np.allclose(a, b, rtol=1e-12, atol=1e-14)
+    assert np.allclose(orc.filter_kernel(2, 1.0, 1), [0.0, 0.5, 0.5, 0.0])
+    for ss in (1, 2, 3, 4):
+        t = orc.filter_kernel(ss, 1.0, 0)
+        assert len(t) % 2 == ss % 2 and abs(t.sum() - 1.0) < 1e-12 and np.allclose(t, t[::-1])
