@@ -290,6 +290,31 @@ def algorithmic_ops_per_point(xml):
     return ops + 4.0, calls
 
 
+def splat_tile_capacity(slots):
+    """Bins of a shared-memory splat tile that fit beside `slots` walker slots (a 16 KB genome)."""
+    used = 3 * slots * 16 + 256 * 16 + 16384 + 2 * (slots // 256) * 4 + 256 * 4 + 16
+    return max(0, (232448 - used) // 20)
+
+
+def fit_splat_tile(hits, capacity):
+    """(x0, y0, w, h): the bounding box of the bins a probe histogram hit, or, when that holds more
+    than `capacity` bins, the square of that many bins around the most-hit bin."""
+    import numpy as np
+    ys, xs = np.nonzero(hits)
+    if len(xs) == 0 or capacity == 0:
+        return (0, 0, 0, 0)
+    x0, x1, y0, y1 = int(xs.min()), int(xs.max()), int(ys.min()), int(ys.max())
+    if (x1 - x0 + 1) * (y1 - y0 + 1) <= capacity:
+        return (x0, y0, x1 - x0 + 1, y1 - y0 + 1)
+    side = int(capacity ** 0.5)
+    cy, cx = np.unravel_index(int(np.argmax(hits)), hits.shape)
+    H, W = hits.shape
+    w, h = min(side, W), min(side, H)
+    x0 = min(max(0, int(cx) - w // 2), W - w)
+    y0 = min(max(0, int(cy) - h // 2), H - h)
+    return (x0, y0, w, h)
+
+
 def _traffic(workload):
     """DRAM bytes per chaos launch from the committed ncu summary of this workload (or None)."""
     v = _profile_figure(workload, "dram bytes per launch")
@@ -381,8 +406,18 @@ def run_native(args):
     img = torch.zeros(H_OUT, W_OUT, 4, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
     sim.set_stream(stream)
-    sim.set_splat({"auto": R.SPLAT_AUTO, "global": R.SPLAT_GLOBAL, "warp": R.SPLAT_WARP}[args.splat])
+    sim.set_splat({"auto": R.SPLAT_AUTO, "global": R.SPLAT_GLOBAL, "warp": R.SPLAT_WARP,
+                   "tile": R.SPLAT_TILE}[args.splat])
     sim.set_bad_value_reset(reset)
+    tile = None
+    if args.splat == "tile":  # the shared-memory tile: the attractor's bounding box from a short probe
+        sim.warmup(flame, FUSE - 1)
+        sim.set_splat_tile(0, 0, 0, 0)
+        probe = torch.zeros(H, W, dtype=torch.int32, device="cuda")
+        sim.draw_to_bins(flame, bins, probe, W, H, 4)
+        tile = fit_splat_tile(probe.cpu().numpy(), splat_tile_capacity(cta))
+        sim.set_splat_tile(*tile)
+        bins.zero_()
 
     # bins smaller than the 129 MB L2: write a 256 MB buffer before every frame
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda") if W * H * 20 <= 129e6 else None
@@ -510,7 +545,8 @@ def run_native(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic genome (%s); no dataset" % WL["genome_file"],
         "config": workload_config(reset),
         "launch": {"walkers": walkers, "cta_slots": cta, "steps_per_launch": args.steps_per_launch,
-                   "passes_per_frame": passes, "splat": args.splat, "specialized_kernel": sim.specialized(),
+                   "passes_per_frame": passes, "splat": args.splat, "splat_tile": tile,
+                   "specialized_kernel": sim.specialized(),
                    "kernel_build": build, "first_warmup_s": first_warmup_s,
                    "parallelism": "replicas" if ws > 1 else "single"},
         "s_per_frame": ms_step / 1e3,
@@ -735,6 +771,7 @@ def run_learned(args):
     # one network over all input levels, or (separate) one network per level
     groups = [[l] for l in levels] if args.learned_separate else [levels]
     nets, losses, t_train = {}, {}, 0.0
+    losses_val = {}
     loads = args.learned_load.split(",") if args.learned_load else []
     if loads:  # evaluate trained weights (one file per group) instead of training
         for grp, path in zip(groups, loads):
@@ -745,7 +782,7 @@ def run_learned(args):
         groups = []
     else:
         targets = torch.empty(n_train, S, S, 3, device="cuda")
-        LD.render_images(tr, S, S, 1000, [s * 7 + 2 for s in tr_seeds], targets)
+        LD.render_images(tr, S, S, args.learned_target_spp, [s * 7 + 2 for s in tr_seeds], targets)
     t_data = time.perf_counter() - t0
     for gi, grp in enumerate(groups):
         t0 = time.perf_counter()
@@ -757,8 +794,19 @@ def run_learned(args):
         log("training data: %d genomes x input levels %s" % (n_train, grp))
         net = R.Denoiser(4 * S * S, seed=7 + gi)
         t0 = time.perf_counter()
-        ls = LD.train(net, feats, targets, args.learned_steps, batch=args.learned_batch, lr=1e-3, log=log,
-                      crop=args.learned_crop)
+        val = None
+        if args.learned_val:  # the last genomes of the training range, kept out of its minibatches
+            nv = args.learned_val
+            vf = torch.empty(nv, S, S, 8, dtype=torch.bfloat16, device="cuda")
+            LD.render_features(tr[-nv:], S, S, grp[0], [s * 7 + 1 + 100 * levels.index(grp[0]) for s in tr_seeds[-nv:]],
+                               vf)
+            val = (vf, targets[-nv:])
+            feats = [f[:-nv] for f in feats]
+        ls = LD.train(net, feats, targets[:feats[0].shape[0]], args.learned_steps, batch=args.learned_batch, lr=1e-3,
+                      log=log, crop=args.learned_crop, val=val)
+        if val is not None:
+            ls, val_history = ls
+            losses_val[tuple(grp)] = val_history
         torch.cuda.synchronize()
         t_train += time.perf_counter() - t0
         for spp in grp:
@@ -846,6 +894,7 @@ def run_learned(args):
                    "resolution": [S, S],
                    "params": net.num_params(), "input_spp": levels, "target_spp": 1000, "reference_spp": args.learned_ref_spp,
                    "weights": "loaded" if loads else "trained in this run",
+                   "train_target_spp": args.learned_target_spp, "validation_genomes": args.learned_val,
                    "frame_spp_learned": spp_fast},
         "plain_s_per_frame": times["plain"],
         "speedup_vs_plain": times["plain"] / times["learned"],
@@ -853,7 +902,8 @@ def run_learned(args):
         "plain_spp_equivalent": equiv,
         "iteration_ratio_at_plain_1000spp_error": None,
         "train": {"data_s": t_data, "train_s": t_train, "separate_networks": bool(args.learned_separate),
-                  "loss_first_last": {str(k): v for k, v in losses.items() if v is not None}},
+                  "loss_first_last": {str(k): v for k, v in losses.items() if v is not None},
+                  "validation_l1": {str(list(k)): v for k, v in losses_val.items()}},
         "fallback": {"calibration_frames": n_cal, "scale": scale, "bound": plain[1000],
                      "correlation_with_true_l1": est_corr, "estimate_vs_true_l1": est_err[:6],
                      "policy_frames": n_cal, "policy_fallbacks": fallbacks,
@@ -881,7 +931,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-badval-reset", action="store_true",
                     help="keep walkers that leave the plane lost (the reference's default, flame.glsl:68)")
-    ap.add_argument("--splat", default="auto", choices=["auto", "global", "warp"])
+    ap.add_argument("--splat", default="auto", choices=["auto", "global", "warp", "tile"],
+                    help="splat strategy; tile: a shared-memory histogram tile over the attractor's bounding box")
     ap.add_argument("--specialize", default="auto", choices=["auto", "on", "off"],
                     help="genome-specialised chaos kernel compiled at run time")
     ap.add_argument("--learned-train", type=int, default=2000)
@@ -896,6 +947,9 @@ def main():
     ap.add_argument("--learned-load", default="", help="evaluate these trained parameter files (.npy, one per "
                                                        "network) instead of training")
     ap.add_argument("--learned-ref-spp", type=int, default=16000, help="samples per pixel of the reference images")
+    ap.add_argument("--learned-target-spp", type=int, default=1000, help="samples per pixel of the training targets")
+    ap.add_argument("--learned-val", type=int, default=0,
+                    help="training genomes kept out for validation and early stopping (0: none)")
     ap.add_argument("--workload", default="frame1080", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     select_workload(args.workload)

@@ -212,7 +212,7 @@ RF_API int  rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_wid
    when a cheap test finds two lanes sharing a bin (AUTO, the default).  The genome-specialised
    kernel is compiled with the strategy set at rf_warmup; setting another one later makes the
    next draw call fetch (or, the first time, compile) the kernel for it. */
-enum rf_splat { RF_SPLAT_AUTO = 0, RF_SPLAT_GLOBAL = 1, RF_SPLAT_WARP = 2 };
+enum rf_splat { RF_SPLAT_AUTO = 0, RF_SPLAT_GLOBAL = 1, RF_SPLAT_WARP = 2, RF_SPLAT_TILE = 3 };
 /* flame::draw_to_bins(bins, bins_width, num_iter) (flame.cpp:283-330): num_iter passes over
    every walker, drawing into caller-owned device bins.  bins_hits may be NULL.  When `drawn`
    is non-NULL the call synchronises and stores the number of points binned (the reference's
@@ -226,6 +226,13 @@ RF_API int  rf_set_bin_layout(rf_sim* s, int layout);
 RF_API int  rf_draw_to_bins(rf_sim* s, rf_flame* f, float* bins_rgba, uint32_t* bins_hits,
                      uint32_t width, uint32_t height, uint32_t num_iter, uint64_t* drawn);
 RF_API int  rf_set_splat(rf_sim* s, int splat);
+/* RF_SPLAT_TILE: a per-CTA histogram tile in shared memory for compact attractors.  The bins of
+   columns [x0, x0 + w) and rows [y0, y0 + h) (row 0 at the top, as the bins) accumulate in each
+   CTA's shared memory over a launch (aggregated within the warp where lanes share a bin) and are
+   added to the caller's bins once at the launch's end; points outside go to the L2 as
+   RF_SPLAT_GLOBAL.  The tile must lie inside the bin grid and fit beside the CTA's walkers
+   (w * h * 20 bytes: about 1,500 bins beside 4096 slots of a small genome, 6,500 beside 2048). */
+RF_API int  rf_set_splat_tile(rf_sim* s, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h);
 /* The walker reset that shaders/flame.glsl:68 keeps commented out: after an xform, a walker whose
    x or y is NaN or beyond +-1e10 (math.glsl:22 `badval`) restarts at (2u1 - 1, 2u2 - 1) from two
    randf() draws of its slot, with opacity 0 (that step is not drawn).  0 (default) = the

@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "librefrakt_gb300.so")
 
 SYNTH_SMALL, SYNTH_RANDOM, SYNTH_CONTRACT, SYNTH_SPACEFILL = 0, 1, 2, 3
-SPLAT_AUTO, SPLAT_GLOBAL, SPLAT_WARP = 0, 1, 2
+SPLAT_AUTO, SPLAT_GLOBAL, SPLAT_WARP, SPLAT_TILE = 0, 1, 2, 3
 BINS_AUTO, BINS_DIRECT, BINS_INTERLEAVED = 0, 1, 2
 FILTER_GAUSSIAN, FILTER_BOX, FILTER_TRIANGLE, FILTER_HERMITE = 0, 1, 2, 3
 
@@ -148,6 +148,7 @@ _SIGS = {
                          ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "rf_set_splat": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rf_set_bad_value_reset": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rf_set_splat_tile": ([ctypes.c_void_p] + [ctypes.c_uint32] * 4, ctypes.c_int),
     "rf_set_bin_layout": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rf_sim_counters": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "rf_density_estimate": ([ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
@@ -492,6 +493,10 @@ class Sim:
 
     def set_splat(self, splat):
         _check(library().rf_set_splat(self._h, splat))
+
+    def set_splat_tile(self, x0, y0, w, h):
+        """The bins of the shared-memory histogram tile (rf_set_splat_tile; used with SPLAT_TILE)."""
+        _check(library().rf_set_splat_tile(self._h, x0, y0, w, h))
 
     def set_bad_value_reset(self, on):
         """Restart walkers that leave the plane (rf_set_bad_value_reset; the reference keeps this

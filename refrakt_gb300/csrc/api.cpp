@@ -46,7 +46,9 @@ using namespace rfk;
 namespace {
 
 // rf_sim's splat setting as ChaosArgs.splat's code: 0 global, 1 warp-aggregated, 2 adaptive
-int splat_code(int splat) { return splat == RF_SPLAT_WARP ? 1 : (splat == RF_SPLAT_GLOBAL ? 0 : 2); }
+int splat_code(int splat) {
+    return splat == RF_SPLAT_WARP ? 1 : splat == RF_SPLAT_GLOBAL ? 0 : splat == RF_SPLAT_TILE ? 3 : 2;
+}
 
 }  // namespace
 
@@ -96,6 +98,10 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.rgba_shift = s->rgba_shift;
         a.count_shift = s->count_shift;
         if (ss) memcpy(a.ss, ss, sizeof(a.ss));
+        a.tile_x0 = s->tile[0];
+        a.tile_y0 = s->tile[1];
+        a.tile_w = s->tile[2];
+        a.tile_h = s->tile[3];
         a.W = W;
         a.H = H;
         a.bins = bins;
@@ -116,8 +122,13 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
             s->spec_splat = a.splat;
             s->spec_reset = a.reset;
         }
+        const uint32_t tile_bins = a.splat == 3 && a.draw ? a.tile_w * a.tile_h : 0u;
+        if (chaos_smem(s->slots, a.prog_words, a.steps, tile_bins) > kMaxCtaSmem)
+            return fail(RF_ERR_CAPACITY, "splat tile of " + std::to_string(tile_bins) +
+                                         " bins exceeds the shared memory beside " + std::to_string(s->slots) +
+                                         " walker slots");
         cudaError_t e = s->spec ? launch_spec(s->spec, (int)s->threads, (int)s->slots, a, grid,
-                                              chaos_smem(s->slots, a.prog_words, a.steps), s->stream)
+                                              chaos_smem(s->slots, a.prog_words, a.steps, tile_bins), s->stream)
                                 : launch_chaos((int)s->threads, (int)s->slots, a, grid, s->stream);
         if (e != cudaSuccess) return cuda_fail(e, "chaos kernel launch");
         s->cur ^= 1;
@@ -594,6 +605,16 @@ int rf_set_splat(rf_sim* s, int splat) {
     return RF_OK;
 }
 
+int rf_set_splat_tile(rf_sim* s, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h) {
+    if (!s) return fail(RF_ERR_INVALID_ARG, "rf_set_splat_tile: null sim");
+    if ((uint64_t)w * h > 65536) return fail(RF_ERR_CAPACITY, "rf_set_splat_tile: more than 65,536 bins");
+    s->tile[0] = x0;
+    s->tile[1] = y0;
+    s->tile[2] = w;
+    s->tile[3] = h;
+    return RF_OK;
+}
+
 int rf_set_bad_value_reset(rf_sim* s, int on) {
     if (!s || (on != 0 && on != 1)) return fail(RF_ERR_INVALID_ARG, "rf_set_bad_value_reset: null sim or flag not 0/1");
     s->reset = on;
@@ -608,6 +629,8 @@ int rf_draw_to_bins(rf_sim* s, rf_flame* f, float* bins_rgba, uint32_t* bins_hit
     if (rf_needs_warmup(s, f)) return fail(RF_ERR_NEEDS_WARMUP, "flame changed or not warmed up: call rf_warmup");
     if (f->g.size[1] == 0) return fail(RF_ERR_INVALID_ARG, "genome size is zero");
     if (((uintptr_t)bins_rgba) & 15) return fail(RF_ERR_INVALID_ARG, "bins_rgba must be 16-byte aligned");
+    if (s->splat == RF_SPLAT_TILE && ((uint64_t)s->tile[0] + s->tile[2] > W || (uint64_t)s->tile[1] + s->tile[3] > H))
+        return fail(RF_ERR_INVALID_ARG, "rf_draw_to_bins: the splat tile does not lie inside the bin grid");
     if (int rc = set_device(s)) return rc;
     float ss[6];
     genome_screen_affine(f->g, W, H, ss);

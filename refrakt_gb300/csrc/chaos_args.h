@@ -22,11 +22,15 @@ struct ChaosArgs {
     uint64_t seed;
     int first_run;           // pass 0 reads the start points, jitters, draws colours
     int draw;
-    int splat;               // 0: a reduction per point; 1: warp-aggregated; 2: adaptive (splat.cuh)
+    int splat;               // 0: a reduction per point; 1: warp-aggregated; 2: adaptive; 3: tile (splat.cuh)
     int reset;               // 1: walkers that leave the plane restart (reset_bad_walker, device.cuh)
     uint32_t rgba_shift;     // bin addressing (splat.cuh BinTarget): 0 and 0 for the caller's
     uint32_t count_shift;    //   planes, 1 and 3 for interleaved 32-byte records
     float ss[6];             // screen affine
+    // splat 3: the bins of columns [tile_x0, tile_x0 + tile_w) and rows [tile_y0, tile_y0 + tile_h)
+    // (rows after flame.glsl:84's flip) accumulate in the CTA's shared memory for the whole launch
+    // and are added to the bins once at its end
+    uint32_t tile_x0, tile_y0, tile_w, tile_h;
     uint32_t W, H;
     float4* bins;            // RGBA sums
     uint32_t* hits;          // counts (may be null)

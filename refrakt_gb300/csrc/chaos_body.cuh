@@ -50,14 +50,17 @@ __device__ __forceinline__ int draw_phase(int tid) {
 // Shared memory of a chaos CTA (dynamic, in this order):
 //   program words (prog_words), palette float4[256], walker exchange float4 [2][SLOTS],
 //   JSF32 states uint4[SLOTS], group xform ids int[2][SLOTS/256], per-pass permutation ids
-//   uint32[steps]
-__host__ __device__ inline size_t chaos_smem_bytes(int slots, uint32_t prog_words, uint32_t steps) {
+//   uint32[steps]; with the tile splat (16-byte aligned) the tile's float4 RGBA sums and uint32
+//   counts
+__host__ __device__ inline size_t chaos_smem_bytes(int slots, uint32_t prog_words, uint32_t steps,
+                                                   uint32_t tile_bins = 0) {
     size_t b = ((size_t)prog_words * 4 + 15) & ~(size_t)15;
     b += 256 * 16;
     b += (size_t)2 * slots * 16;
     b += (size_t)slots * 16;
     b += (size_t)2 * (slots / kGroup) * 4;
     b += (size_t)steps * 4;
+    if (tile_bins) b = ((b + 15) & ~(size_t)15) + (size_t)tile_bins * 20;
     return b;
 }
 
@@ -80,8 +83,21 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
     uint4* s_rng = reinterpret_cast<uint4*>(s_w + 2 * SLOTS);
     int* s_xid = reinterpret_cast<int*>(s_rng + SLOTS);
     uint32_t* s_perm = reinterpret_cast<uint32_t*>(s_xid + 2 * G);
+    // the tile splat's shared-memory histogram (splat 3)
+    const bool tiled = SPLAT == 3 || (SPLAT < 0 && A.splat == 3);
+    const uint32_t tile_bins = tiled && A.draw ? A.tile_w * A.tile_h : 0u;
+    TileTarget tt{nullptr, nullptr};
+    if (tile_bins) {
+        tt.rgba = reinterpret_cast<float4*>(
+            smem + ((chaos_smem_bytes(SLOTS, A.prog_words, A.steps) + 15) & ~(size_t)15));
+        tt.count = reinterpret_cast<uint32_t*>(tt.rgba + tile_bins);
+    }
 
     const int tid = threadIdx.x;
+    for (uint32_t i = tid; i < tile_bins; i += THREADS) {
+        tt.rgba[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        tt.count[i] = 0u;
+    }
     const uint32_t chunk = blockIdx.x;  // mixing domain
     const uint32_t ts = chunk / A.chunks_per_ts;
     const uint32_t gid0 = (chunk - ts * A.chunks_per_ts) * SLOTS;  // first slot within the temporal sample
@@ -181,11 +197,14 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
                 if (op > 0.0f) emitted++;
                 const float px = fmaf(A.ss[0], ex, fmaf(A.ss[2], ey, A.ss[4]));
                 const float py = fmaf(A.ss[1], ex, fmaf(A.ss[3], ey, A.ss[5]));
-                uint32_t bin = kNoBin;
+                uint32_t bin = kNoBin, local = kNoBin;
                 float4 val = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 if (px >= 0.0f && py >= 0.0f && px < W && py < H && op > 0.0f) {
                     const uint32_t bx = (uint32_t)px, by = (uint32_t)py;
-                    bin = (A.H - 1 - by) * A.W + bx;  // flame.glsl:84 row flip; W*H < 2^32 - 1
+                    const uint32_t row = A.H - 1 - by;  // flame.glsl:84 row flip; W*H < 2^32 - 1
+                    bin = row * A.W + bx;
+                    if (tile_bins && bx - A.tile_x0 < A.tile_w && row - A.tile_y0 < A.tile_h)
+                        local = (row - A.tile_y0) * A.tile_w + (bx - A.tile_x0);
                     const float4 col = s_pal[palette_index(ec)];
                     val = make_float4(col.x, col.y, col.z, op);
                     drawn++;
@@ -197,12 +216,28 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
                     splat_warp(t, bin, val);
                 } else if constexpr (SPLAT == 2) {
                     splat_adaptive(t, bin, val);
+                } else if constexpr (SPLAT == 3) {
+                    splat_tile(t, tt, bin, local, val);
                 } else {
                     if (A.splat == 1) splat_warp(t, bin, val);
                     else if (A.splat == 2) splat_adaptive(t, bin, val);
+                    else if (A.splat == 3) splat_tile(t, tt, bin, local, val);
                     else splat_global(t, bin, val);
                 }
             }
+        }
+    }
+    // the tile's non-empty bins into the histogram, once per launch
+    if (tile_bins) {
+        __syncthreads();
+        const BinTarget t{A.bins, A.hits, A.rgba_shift, A.count_shift};
+        for (uint32_t i = tid; i < tile_bins; i += THREADS) {
+            const uint32_t n = tt.count[i];
+            if (!n) continue;
+            const uint32_t row = A.tile_y0 + i / A.tile_w, col = A.tile_x0 + i % A.tile_w;
+            const float4 v = tt.rgba[i];
+            red_add_f32x4(t.at_rgba(row * A.W + col), v.x, v.y, v.z, v.w);
+            if (t.count) red_add_u32x1(t.at_count(row * A.W + col), n);
         }
     }
     // each slot's final walker and state were written by the thread that owns the slot

@@ -41,6 +41,7 @@ struct rf_sim {
     const void* spec = nullptr;  // genome-specialised kernel of the warmed flame (specialize.cpp)
     int spec_splat = -1;              // the splat strategy compiled into it (ChaosArgs.splat code)
     int reset = 0;                    // walker reset of flame.glsl:68 (rf_set_bad_value_reset)
+    uint32_t tile[4] = {0, 0, 0, 0};  // the tile splat's bins: x0, y0, w, h (rf_set_splat_tile)
     int spec_reset = -1;              // the reset setting compiled into the specialised kernel
     std::vector<uint32_t> spec_prog;  // the warmed program, to specialise again for another strategy
     int bin_layout = RF_BINS_AUTO;

@@ -68,39 +68,42 @@ __device__ __forceinline__ void block_sum_to(double s, double* out) {
     }
 }
 
-// sum of k^2 for k = lo .. hi (lo <= hi), in closed form
-__host__ __device__ __forceinline__ double square_sum(int lo, int hi) {
-    auto F = [](int m) { return (double)m * (m + 1) * (2.0 * m + 1) / 6.0; };  // 0^2 + .. + m^2, m >= 0
-    if (lo >= 0) return F(hi) - (lo > 0 ? F(lo - 1) : 0.0);
-    if (hi <= 0) return F(-lo) - (hi < 0 ? F(-hi - 1) : 0.0);
-    return F(-lo) + F(hi);
-}
-
-// The kernel weights of a disc of radius r >= 1 centred at (x, y), summed over the cells inside
-// the w x h grid, in FP64: each row ay of the disc (4 (dx^2 + ay^2) <= (2r + 1)^2, i.e.
-// dx^2 <= r^2 + r - ay^2) clipped to the grid adds nf ((1 - ay^2/rho^2) n - sum dx^2 / rho^2),
-// rho = r + 0.5, nf = 0.63661977236 / r^2 — the density_frag.glsl kernel in closed form.
-__host__ __device__ inline double disc_weight_sum(int r, int x, int y, int w, int h) {
-    const double rho2 = (r + 0.5) * (r + 0.5), nf = 0.63661977236 / (double)(r * r);
-    const int y0 = -r > -y ? -r : -y, y1 = r < h - 1 - y ? r : h - 1 - y;
-    double s = 0.0;
-    for (int dy = y0; dy <= y1; dy++) {
-        const int lim = r * r + r - dy * dy;
-        int sx = (int)sqrt((double)lim);
-        while ((sx + 1) * (sx + 1) <= lim) sx++;
-        while (sx * sx > lim) sx--;
-        const int lo = -sx > -x ? -sx : -x, hi = sx < w - 1 - x ? sx : w - 1 - x;
-        if (lo > hi) continue;
-        s += (1.0 - (double)(dy * dy) / rho2) * (double)(hi - lo + 1) - square_sum(lo, hi) / rho2;
-    }
-    return nf * s;
-}
-
 // pass 1 of the fused image tail: the radius per bin, and the total density of the estimator's
-// output, sum_out a = sum over bins of a * (the kernel weights of its disc inside the grid), in
-// FP64 — the log-density scale's sum (k2 = W * H / sum a) without a pass over the output.
+// output, sum_out a = sum over bins of a * (the kernel weights of its disc inside the grid) — the
+// log-density scale's sum (k2 = W * H / sum a) without a pass over the output.  A whole disc's
+// weights come from T.wsum (FP64); a disc cut by the grid's edge adds, per row inside the grid,
+// the difference of two prefix sums of that row's FP32 weights, staged per CTA in shared memory
+// for every radius up to kDeMaxSmemR (the fused path's radii).
+constexpr int kRowPrefixFloats = 1638;  // sum over r <= 12 of (r + 1) rows of 2r + 2 prefix sums
+
 __global__ void de_radius_sum_kernel(const float4* __restrict__ in, uint32_t w, uint32_t h, const DeTables T,
-                                     uint8_t* __restrict__ rad, double* __restrict__ sum_out) {
+                                     const float* __restrict__ weights, uint8_t* __restrict__ rad,
+                                     double* __restrict__ sum_out) {
+    __shared__ float s_pre[kRowPrefixFloats];
+    __shared__ int s_pbase[kDeMaxSmemR + 1];
+    const int rmax = min(kDeMaxSmemR, T.R > T.min_r ? T.R : T.min_r);
+    if (threadIdx.x == 0) {
+        int off = 0;
+        for (int r = 0; r <= kDeMaxSmemR; r++) {
+            s_pbase[r] = off;
+            off += (r + 1) * (2 * r + 2);
+        }
+    }
+    __syncthreads();
+    // row (r, ay): pre[j] = sum of the disc's weights at dx = -r .. -r + j - 1
+    for (int q = threadIdx.x; q < (rmax + 1) * (rmax + 1); q += blockDim.x) {
+        const int r = q / (rmax + 1), ay = q % (rmax + 1);
+        if (r < 1 || ay > r) continue;
+        float* pre = s_pre + s_pbase[r] + ay * (2 * r + 2);
+        float acc = 0.0f;
+        pre[0] = 0.0f;
+        for (int dx = -r; dx <= r; dx++) {
+            const int ax = dx < 0 ? -dx : dx;
+            if (4 * (ax * ax + ay * ay) <= (2 * r + 1) * (2 * r + 1)) acc += weights[T.wbase[r] + ay * (r + 1) + ax];
+            pre[dx + r + 1] = acc;
+        }
+    }
+    __syncthreads();
     const uint32_t n = w * h;  // < 2^32 (the caller's grids hold fewer bins)
     double s = 0.0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -111,10 +114,22 @@ __global__ void de_radius_sum_kernel(const float4* __restrict__ in, uint32_t w, 
         }
         const int r = de_radius(a, T);
         rad[i] = (uint8_t)r;
+        if (r == 0) {
+            s += (double)a;
+            continue;
+        }
         const int y = (int)(i / w), x = (int)(i - (uint32_t)y * w);
-        const bool inside = x >= r && y >= r && x + r < (int)w && y + r < (int)h;
-        const double ws = (r == 0) ? 1.0 : inside ? T.wsum[r] : disc_weight_sum(r, x, y, (int)w, (int)h);
-        s += (double)a * ws;
+        if (x >= r && y >= r && x + r < (int)w && y + r < (int)h) {
+            s += (double)a * T.wsum[r];
+            continue;
+        }
+        const int dx0 = max(-r, -x), dx1 = min(r, (int)w - 1 - x);
+        float ws = 0.0f;
+        for (int dy = max(-r, -y); dy <= min(r, (int)h - 1 - y); dy++) {
+            const float* pre = s_pre + s_pbase[r] + (dy < 0 ? -dy : dy) * (2 * r + 2);
+            ws += pre[dx1 + r + 1] - pre[dx0 + r];
+        }
+        s += (double)(a * ws);
     }
     block_sum_to(s, sum_out);
 }
@@ -197,28 +212,60 @@ constexpr int kDsX = 32, kDsY = 8, kDsThreads = 256;
 
 // With TM the tile's output stays in shared memory and the CTA tonemaps its (32/ss) x (8/ss)
 // output pixels from it (ss dividing 8): the estimator's output never goes through DRAM.
+// Shared memory of a tile CTA: NS staged colours (float4), NS list entries, NS packed source
+// records, the weight table of radii up to R, per-warp counts and the rmax slot, per staged row
+// its largest radius; with TM the tile's NO outputs.
+template <int R>
+__host__ __device__ constexpr int de_weight_count() { return (R + 1) * (R + 2) * (2 * R + 3) / 6; }  // sum (r+1)^2
+
 template <int R, bool TM = false>
 __host__ __device__ constexpr size_t de_tile_smem() {
-    return (((size_t)(kDsX + 2 * R) * (kDsY + 2 * R) * (16 + 4 + 1) + 16 + 64 + 4 * (kDsY + 2 * R) + 15) & ~(size_t)15) +
+    return (((size_t)(kDsX + 2 * R) * (kDsY + 2 * R) * (16 + 4 + 4) + 4 * (size_t)de_weight_count<R>() + 16 * 4 +
+             4 * (kDsY + 2 * R) + 15) & ~(size_t)15) +
            (TM ? (size_t)kDsX * kDsY * 16 : 0);
+}
+
+// A staged source bin as one word: the disc's squared-distance limit r^2 + r (bits 0-8: a tap at
+// squared distance d2 is inside the disc exactly when d2 <= limit, the symmetric restatement of
+// 4 d2 <= (2r + 1)^2), the offset of radius r's weights in the table (bits 9-18) and the table's
+// row length r + 1 (bits 19-23).  An empty bin is a radius-0 disc of colour zero: it adds zero.
+__device__ __forceinline__ uint32_t de_pack(int r) {
+    return (uint32_t)(r * r + r) | ((uint32_t)(r * (r + 1) * (2 * r + 1) / 6) << 9) | ((uint32_t)(r + 1) << 19);
+}
+
+// one tap: source record p at offset (ax, ay) (squared distance d2) into the accumulator
+__device__ __forceinline__ void de_tap(float4& a4, uint32_t p, int ax, int ay, int d2, const float* s_wt,
+                                       const float4& v) {
+    const bool in = d2 <= (int)(p & 0x1ffu);
+    const float wt = in ? s_wt[((p >> 9) & 0x3ffu) + ay * (int)(p >> 19) + ax] : 0.0f;
+    a4.x = fmaf(v.x, wt, a4.x);
+    a4.y = fmaf(v.y, wt, a4.y);
+    a4.z = fmaf(v.z, wt, a4.z);
+    a4.w = fmaf(v.w, wt, a4.w);
 }
 
 template <int R, bool TM = false>
 __global__ void __launch_bounds__(kDsThreads) de_tile_kernel(
     const float4* __restrict__ in, const uint8_t* __restrict__ rad, uint32_t w, uint32_t h,
     const float* __restrict__ weights, const DeTables T, float4* __restrict__ out, const TmArgs tm) {
-    constexpr int SW = kDsX + 2 * R, SH = kDsY + 2 * R, NS = SW * SH, NO = kDsX * kDsY;
+    constexpr int SW = kDsX + 2 * R, SH = kDsY + 2 * R, NS = SW * SH, NO = kDsX * kDsY, NW = de_weight_count<R>();
     extern __shared__ __align__(16) unsigned char smem[];
-    float4* s_c = reinterpret_cast<float4*>(smem);                  // NS colours
+    float4* s_c = reinterpret_cast<float4*>(smem);                  // NS colours (zero where empty)
     int* s_list = reinterpret_cast<int*>(s_c + NS);                 // indices of discs of radius >= 2
-    uint8_t* s_r = reinterpret_cast<uint8_t*>(s_list + NS);         // NS radii (255: empty)
-    int* s_stat = reinterpret_cast<int*>(s_r + ((NS + 15) & ~15));  // [0] rmax, [1..8] per-warp counts
+    uint32_t* s_pk = reinterpret_cast<uint32_t*>(s_list + NS);      // NS packed source records
+    float* s_wt = reinterpret_cast<float*>(s_pk + NS);              // weights of radii 0..R
+    int* s_stat = reinterpret_cast<int*>(s_wt + NW);                // [0] rmax, [1..8] per-warp counts
     int* s_rowmax = s_stat + 16;                                     // SH: largest radius per staged row
     float4* s_out = reinterpret_cast<float4*>(smem + ((de_tile_smem<R, false>() + 15) & ~(size_t)15));  // TM: NO outputs
     const int tx0 = blockIdx.x * kDsX, ty0 = blockIdx.y * kDsY;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_stat[0] = 0;
     for (int i = threadIdx.x; i < SH; i += kDsThreads) s_rowmax[i] = -1;
+    {  // the weight table holds radii up to this launch's largest (<= R); the rest stays zero
+        const int rl = T.R > T.min_r ? T.R : T.min_r;
+        const int nw = (rl + 1) * (rl + 2) * (2 * rl + 3) / 6;
+        for (int i = threadIdx.x; i < NW; i += kDsThreads) s_wt[i] = i < nw ? weights[i] : 0.0f;
+    }
     __syncthreads();
     int rmax = 0, nl = 0;
     // stage the tile + halo; list the large discs that reach the tile in source order (a
@@ -228,18 +275,18 @@ __global__ void __launch_bounds__(kDsThreads) de_tile_kernel(
         bool big = false;
         if (i < NS) {
             const int gx = tx0 - R + i % SW, gy = ty0 - R + i / SW;
-            uint8_t r = 255;
+            int r = 255;
             float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             if (gx >= 0 && gy >= 0 && gx < (int)w && gy < (int)h) {
                 const size_t gi = (size_t)gy * w + gx;
                 r = rad[gi];
                 if (r != 255) v = in[gi];
             }
-            s_r[i] = r;
+            s_pk[i] = de_pack(r == 255 ? 0 : r);
             s_c[i] = v;
-            if (r != 255) atomicMax(&s_rowmax[i / SW], (int)r);
+            if (r != 255) atomicMax(&s_rowmax[i / SW], r);
             if (r != 255 && gx - r <= tx0 + kDsX - 1 && gx + r >= tx0 && gy - r <= ty0 + kDsY - 1 && gy + r >= ty0) {
-                rmax = max(rmax, (int)r);
+                rmax = max(rmax, r);
                 big = r >= 2;
             }
         }
@@ -264,50 +311,29 @@ __global__ void __launch_bounds__(kDsThreads) de_tile_kernel(
         const int ox = o % kDsX, oy = o / kDsX;
         float4 a4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (use_list) {
+            // discs of radius 0 and 1 from the 3 x 3 neighbourhood, then the listed larger discs
             for (int dy = -1; dy <= 1; dy++)
                 for (int dx = -1; dx <= 1; dx++) {
                     const int si = (oy + R + dy) * SW + ox + R + dx;
-                    const int r = s_r[si];
-                    if (r > 1 || (r == 0 && (dx | dy))) continue;  // r = 255 (empty) fails r > 1
-                    const float wt = r == 0 ? 1.0f : weights[T.wbase[1] + (dy ? 1 : 0) * 2 + (dx ? 1 : 0)];
-                    const float4 v = s_c[si];
-                    a4.x = fmaf(v.x, wt, a4.x);
-                    a4.y = fmaf(v.y, wt, a4.y);
-                    a4.z = fmaf(v.z, wt, a4.z);
-                    a4.w = fmaf(v.w, wt, a4.w);
+                    const uint32_t p = s_pk[si];
+                    if ((p & 0x1ffu) > 2u) continue;  // radius >= 2: in the list
+                    de_tap(a4, p, dx * dx, dy * dy, dx * dx + dy * dy, s_wt, s_c[si]);
                 }
             for (int k = 0; k < nl; k++) {
                 const int si = s_list[k];
-                const int r = s_r[si];
                 const int ax = abs(ox + R - si % SW), ay = abs(oy + R - si / SW);
-                if (4 * (ax * ax + ay * ay) > (2 * r + 1) * (2 * r + 1)) continue;
-                const float wt = weights[T.wbase[r] + ay * (r + 1) + ax];
-                const float4 v = s_c[si];
-                a4.x = fmaf(v.x, wt, a4.x);
-                a4.y = fmaf(v.y, wt, a4.y);
-                a4.z = fmaf(v.z, wt, a4.z);
-                a4.w = fmaf(v.w, wt, a4.w);
+                if (ax > R || ay > R) continue;
+                de_tap(a4, s_pk[si], ax, ay, ax * ax + ay * ay, s_wt, s_c[si]);
             }
         } else {
             for (int dy = -rm; dy <= rm; dy++) {
                 const int ay = dy < 0 ? -dy : dy;
                 const int rr = min(rm, s_rowmax[oy + R + dy]);  // no disc of this row reaches |dy| rows
                 if (rr < ay) continue;
+                const int row = (oy + R + dy) * SW + ox + R;
                 for (int dx = -rr; dx <= rr; dx++) {
-                    const int si = (oy + R + dy) * SW + ox + R + dx;
-                    const int r = s_r[si];
                     const int ax = dx < 0 ? -dx : dx;
-                    if (r == 255 || ax > r || ay > r) continue;
-                    float wt = 1.0f;
-                    if (r > 0) {
-                        if (4 * (ax * ax + ay * ay) > (2 * r + 1) * (2 * r + 1)) continue;
-                        wt = weights[T.wbase[r] + ay * (r + 1) + ax];
-                    }
-                    const float4 v = s_c[si];
-                    a4.x = fmaf(v.x, wt, a4.x);
-                    a4.y = fmaf(v.y, wt, a4.y);
-                    a4.z = fmaf(v.z, wt, a4.z);
-                    a4.w = fmaf(v.w, wt, a4.w);
+                    de_tap(a4, s_pk[row + dx], ax, ay, ax * ax + ay * ay, s_wt, s_c[row + dx]);
                 }
             }
         }
@@ -607,8 +633,16 @@ static void de_tables(int R, int min_r, float curve, DeTables& T, std::vector<fl
                 const int d2 = ax * ax + ay * ay;
                 wts.push_back(r == 0 ? 1.0f : (float)((1.0 - (double)d2 / den) * nf));
             }
-        // the whole disc's weights (far from the grid's edges)
-        T.wsum[r] = r == 0 ? 1.0 : disc_weight_sum(r, r, r, 2 * r + 1, 2 * r + 1);
+        // the whole disc: the table's weights of every (dx, dy) with 4 (dx^2 + dy^2) <= (2r + 1)^2
+        double s = 0.0;
+        for (int dy = -r; dy <= r; dy++)
+            for (int dx = -r; dx <= r; dx++) {
+                const int ax = dx < 0 ? -dx : dx, ay = dy < 0 ? -dy : dy;
+                if (r == 0) s += 1.0;
+                else if (4 * (ax * ax + ay * ay) <= (2 * r + 1) * (2 * r + 1))
+                    s += (double)wts[T.wbase[r] + ay * (r + 1) + ax];
+            }
+        T.wsum[r] = s;
     }
 }
 
@@ -695,7 +729,7 @@ cudaError_t launch_density_tonemap(const float4* in, uint32_t w, uint32_t h, int
     if (need_sum) {
         e = cudaMemsetAsync(stats, 0, 3 * sizeof(double), st);
         if (e != cudaSuccess) return e;
-        de_radius_sum_kernel<<<1024, 256, 0, st>>>(in, w, h, T, rad, stats);
+        de_radius_sum_kernel<<<1024, 256, 0, st>>>(in, w, h, T, dw, rad, stats);
     } else {
         de_radius_kernel<<<1024, 256, 0, st>>>(in, (size_t)w * h, T, rad);
     }

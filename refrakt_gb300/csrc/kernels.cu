@@ -97,11 +97,14 @@ __global__ void probe_kernel(const uint32_t* prog, int xform, uint32_t n, const 
 // ---------------------------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------------------------
-size_t chaos_smem(int slots, uint32_t prog_words, uint32_t steps) { return chaos_smem_bytes(slots, prog_words, steps); }
+size_t chaos_smem(int slots, uint32_t prog_words, uint32_t steps, uint32_t tile_bins) {
+    return chaos_smem_bytes(slots, prog_words, steps, tile_bins);
+}
 
 template <int THREADS, int SPT>
 static cudaError_t launch_chaos_t(const ChaosArgs& a, uint32_t grid, cudaStream_t st) {
-    const size_t smem = chaos_smem_bytes(THREADS * SPT, a.prog_words, a.steps);
+    const size_t smem = chaos_smem_bytes(THREADS * SPT, a.prog_words, a.steps,
+                                         a.splat == 3 && a.draw ? a.tile_w * a.tile_h : 0u);
     auto kern = chaos_kernel<THREADS, SPT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

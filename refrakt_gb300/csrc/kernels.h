@@ -14,7 +14,8 @@ namespace rfk {
 
 
 
-size_t chaos_smem(int slots, uint32_t prog_words, uint32_t steps);
+size_t chaos_smem(int slots, uint32_t prog_words, uint32_t steps, uint32_t tile_bins = 0);
+constexpr size_t kMaxCtaSmem = 232448;  // dynamic shared memory a CTA may opt into (227 KB)
 bool chaos_shape_supported(int threads, int slots);
 cudaError_t launch_chaos(int threads, int slots, const ChaosArgs& a, uint32_t grid, cudaStream_t st);
 cudaError_t launch_merge_records(float4* rec, size_t n, float4* bins, uint32_t* hits, cudaStream_t st);

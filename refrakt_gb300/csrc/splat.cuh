@@ -14,6 +14,11 @@
 //   splat_adaptive — per warp and pass: lane pairs (2i, 2i+1) compare bins with one shuffle;
 //                  the warp takes splat_warp when any pair shares a bin (a compact attractor),
 //                  splat_global otherwise, so spread attractors pay one shuffle and one vote.
+//   splat_tile   — a per-CTA histogram tile in shared memory for compact attractors: points in
+//                  the tile's rectangle of bins go to shared-memory atomics (aggregated within
+//                  the warp as splat_adaptive does), the others to splat_global; the chaos
+//                  kernel adds the tile's non-empty bins to the histogram once per launch, so
+//                  the L2 sees a few reductions per bin per CTA instead of one per point.
 #pragma once
 
 #include "rtc_types.h"
@@ -77,6 +82,64 @@ __device__ __forceinline__ void splat_warp(const BinTarget& t, uint32_t bin, flo
     if (bin != kNoBin && (peers & ((1u << lane) - 1u)) == 0u) {  // lowest lane of its set
         red_add_f32x4(t.at_rgba(bin), v.x, v.y, v.z, v.w);
         if (t.count) red_add_u32x1(t.at_count(bin), (uint32_t)__popc(peers));
+    }
+}
+
+// The peer reduction of splat_warp: every lane of the warp calls it with its key (kNoBin for
+// none); the lowest lane of each set of equal keys returns true with the set's colour sum in v
+// and the set's size in n.
+__device__ __forceinline__ bool warp_aggregate(uint32_t key, float4& v, uint32_t& n) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    unsigned rank = __popc(peers & ((1u << lane) - 1u));
+    unsigned above = peers & (0xfffffffeu << lane);
+    while (__any_sync(0xffffffffu, above != 0u)) {
+        const int next = __ffs(above);
+        const int srcl = next ? next - 1 : (int)lane;
+        const float tx = __shfl_sync(0xffffffffu, v.x, srcl);
+        const float ty = __shfl_sync(0xffffffffu, v.y, srcl);
+        const float tz = __shfl_sync(0xffffffffu, v.z, srcl);
+        const float tw = __shfl_sync(0xffffffffu, v.w, srcl);
+        if (next) {
+            v.x += tx;
+            v.y += ty;
+            v.z += tz;
+            v.w += tw;
+        }
+        above &= __ballot_sync(0xffffffffu, (rank & 1u) == 0u);
+        rank >>= 1;
+    }
+    n = (uint32_t)__popc(peers);
+    return key != kNoBin && (peers & ((1u << lane) - 1u)) == 0u;
+}
+
+// The CTA's shared-memory histogram tile (splat_tile): RGBA sums and counts of tile_w x tile_h bins.
+struct TileTarget {
+    float4* rgba;
+    uint32_t* count;
+};
+
+// Every lane of the warp must call this; `local` is the point's index in the tile, or kNoBin when
+// the point misses the tile (then `bin`, its histogram bin or kNoBin, takes the global path).
+__device__ __forceinline__ void splat_tile(const BinTarget& t, const TileTarget& tt, uint32_t bin, uint32_t local,
+                                           float4 v) {
+    if (local == kNoBin) splat_global(t, bin, v);
+    const uint32_t other = __shfl_xor_sync(0xffffffffu, local, 1);
+    if (__any_sync(0xffffffffu, local != kNoBin && local == other)) {
+        uint32_t n;
+        if (warp_aggregate(local, v, n)) {
+            atomicAdd(&tt.rgba[local].x, v.x);
+            atomicAdd(&tt.rgba[local].y, v.y);
+            atomicAdd(&tt.rgba[local].z, v.z);
+            atomicAdd(&tt.rgba[local].w, v.w);
+            atomicAdd(&tt.count[local], n);
+        }
+    } else if (local != kNoBin) {
+        atomicAdd(&tt.rgba[local].x, v.x);
+        atomicAdd(&tt.rgba[local].y, v.y);
+        atomicAdd(&tt.rgba[local].z, v.z);
+        atomicAdd(&tt.rgba[local].w, v.w);
+        atomicAdd(&tt.count[local], 1u);
     }
 }
 

@@ -69,16 +69,29 @@ def l1(a, b):
     return (a - b).abs().flatten(1).mean(1)
 
 
-def train(net, feats, targets, steps, batch=4, lr=1e-3, seed=0, log=None, crop=0):
+def validation_l1(net, feats, targets, batch=4):
+    """Mean L1 of the network's images of `feats` against `targets` (held-out genomes)."""
+    import torch
+    out = torch.empty(feats.shape[0], feats.shape[1], feats.shape[2], 3, device=feats.device)
+    infer_all(net, feats, out, batch)
+    return float(l1(out, targets).mean())
+
+
+def train(net, feats, targets, steps, batch=4, lr=1e-3, seed=0, log=None, crop=0, val=None, val_every=500):
     """Adam on random minibatches; cosine learning-rate decay to lr / 20.  `feats` is one
     [n, h, w, 8] tensor or a list of them (one per input sample count, each against the same
     targets): every minibatch image draws its sample count at random.  With `crop` (a multiple
-    of 8) each minibatch entry is a random crop of that size, so one step sees more genomes."""
+    of 8) each minibatch entry is a random crop of that size, so one step sees more genomes.
+    With `val` = (features, targets) of genomes kept out of training, the validation L1 is
+    measured every `val_every` steps and the parameters of the best measurement are restored at
+    the end (early stopping: the network is kept from fitting its targets' own noise).  Returns
+    the training losses; with `val`, also the validation history as (step, L1) pairs."""
     import torch
     g = torch.Generator().manual_seed(seed)
     levels = feats if isinstance(feats, (list, tuple)) else [feats]
     n, H, W = levels[0].shape[:3]
     losses = []
+    history, best = [], None
     for s in range(steps):
         idx = torch.randint(0, n, (batch,), generator=g).tolist()
         lv = torch.randint(0, len(levels), (batch,), generator=g).tolist()
@@ -97,7 +110,17 @@ def train(net, feats, targets, steps, batch=4, lr=1e-3, seed=0, log=None, crop=0
         losses.append(net.train_step(f, t, a))
         if log and (s % 100 == 0 or s == steps - 1):
             log("step %d loss %.5f lr %.2e" % (s, losses[-1], a))
-    return losses
+        if val is not None and ((s + 1) % val_every == 0 or s == steps - 1):
+            v = validation_l1(net, val[0], val[1])
+            history.append((s + 1, v))
+            if best is None or v < best[0]:
+                best = (v, net.params())
+            if log:
+                log("step %d validation L1 %.5f (best %.5f)" % (s + 1, v, best[0]))
+    if val is None:
+        return losses
+    net.set_params(best[1])
+    return losses, history
 
 
 def infer_all(net, feats, out, batch=4):

@@ -101,3 +101,15 @@ def test_algorithmic_operation_count():
     small_ops, small_calls = bench.algorithmic_ops_per_point(
         '<flame size="8 8" scale="1"><xform weight="1" color="0" coefs="1 0 0 1 0 0" linear="1"/></flame>')
     assert small_calls == 0 and small_ops == 4 + 3 + 2 + 4
+
+
+def test_fit_splat_tile():
+    import numpy as np
+    h = np.zeros((100, 200), np.int32)
+    h[40:50, 120:135] = 3
+    assert bench.fit_splat_tile(h, 1000) == (120, 40, 15, 10)
+    h[0, 0] = 1  # a stray hit: the box no longer fits, the square around the densest bin is taken
+    x0, y0, w, hh = bench.fit_splat_tile(h, 100)
+    assert w == hh == 10 and x0 <= 120 <= x0 + w and y0 <= 40 <= y0 + hh
+    assert bench.fit_splat_tile(np.zeros((4, 4)), 100) == (0, 0, 0, 0)
+    assert bench.splat_tile_capacity(2048) > 5000 and bench.splat_tile_capacity(4096) > 500

@@ -133,3 +133,49 @@ def test_splat_strategies_after_warmup(rk, compiler):
     for mode, (b, h) in out.items():
         assert np.array_equal(h, h0), mode
         assert np.allclose(b, b0, rtol=1e-4, atol=1e-3), mode
+
+
+@pytest.mark.parametrize("specialize,slots,tile", [(0, 2048, (20, 30, 70, 50)), (-1, 2048, (0, 0, 128, 40)),
+                                                   (0, 4096, (40, 40, 32, 32)), (0, 2048, (0, 0, 0, 0))])
+def test_tile_splat_bit_exact(rk, orc, compiler, specialize, slots, tile):
+    """RF_SPLAT_TILE: the points inside the tile accumulate in each CTA's shared memory and reach
+    the bins once per launch, the rest go straight to the L2.  On the affine genome the counts are
+    bit-exact against the FP32 oracle on the kernel's shuffle schedule and the colour sums agree up
+    to FP32 summation order, whatever the tile (part of the grid, a band, an empty tile)."""
+    W = H = 128
+    f = rk.Flame.from_xml(LINEAR, compiler)
+    N, F, D = 8192, 20, 40
+    sim = rk.Sim(N, seed=5, cta_slots=slots, specialize=specialize)
+    sim.set_splat(rk.SPLAT_TILE)
+    sim.set_splat_tile(*tile)
+    sim.warmup(f, F - 1)
+    bins, hits = _bins(W, H)
+    sim.draw_to_bins(f, bins, hits, W, H, D)
+    r = orc.Genome(LINEAR).chaos(N, W, H, fuse=F, draw=D, seed=5, fp64=False, shuffle_mode=1, cta_slots=slots,
+                                 steps_per_launch=32, table_size=1024)
+    g = hits.cpu().numpy().astype(np.uint64)
+    x0, y0, w, h = tile
+    inside = int(g[y0:y0 + h, x0:x0 + w].sum())
+    print("tile %s: %d of %d points inside" % (tile, inside, int(g.sum())))
+    assert np.array_equal(g, r["hits"])
+    assert np.allclose(bins.cpu().numpy(), r["rgba"], rtol=1e-4, atol=1e-3)
+    if w * h:
+        assert inside > 0
+    sim.close()
+
+
+def test_tile_splat_rejects_bad_tiles(rk, compiler):
+    f = rk.Flame.from_xml(LINEAR, compiler)
+    sim = rk.Sim(8192, seed=5, cta_slots=4096)
+    sim.set_splat(rk.SPLAT_TILE)
+    sim.warmup(f, 19)
+    bins, hits = _bins(128, 128)
+    sim.set_splat_tile(100, 0, 40, 10)  # beyond the grid's right edge
+    with pytest.raises(rk.RefraktError) as e:
+        sim.draw_to_bins(f, bins, hits, 128, 128, 4)
+    assert e.value.status == 1
+    sim.set_splat_tile(0, 0, 128, 100)  # 12,800 bins do not fit beside 4096 walker slots
+    with pytest.raises(rk.RefraktError) as e:
+        sim.draw_to_bins(f, bins, hits, 128, 128, 4)
+    assert e.value.status == 5
+    sim.close()
