@@ -229,9 +229,10 @@ RF_API int  rf_set_splat(rf_sim* s, int splat);
 /* RF_SPLAT_TILE: a per-CTA histogram tile in shared memory for compact attractors.  The bins of
    columns [x0, x0 + w) and rows [y0, y0 + h) (row 0 at the top, as the bins) accumulate in each
    CTA's shared memory over a launch (aggregated within the warp where lanes share a bin) and are
-   added to the caller's bins once at the launch's end; points outside go to the L2 as
-   RF_SPLAT_GLOBAL.  The tile must lie inside the bin grid and fit beside the CTA's walkers
-   (w * h * 20 bytes: about 1,500 bins beside 4096 slots of a small genome, 6,500 beside 2048). */
+   added to the caller's bins once at the launch's end; points outside go to the L2, aggregated
+   the same way.  The tile must lie inside a bin grid of fewer than 2^31 bins and fit beside the
+   CTA's walkers (w * h * 20 bytes: about 1,500 bins beside 4096 slots of a small genome, 6,500
+   beside 2048); the batched launch does not use it (RF_SPLAT_GLOBAL there). */
 RF_API int  rf_set_splat_tile(rf_sim* s, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h);
 /* The walker reset that shaders/flame.glsl:68 keeps commented out: after an xform, a walker whose
    x or y is NaN or beyond +-1e10 (math.glsl:22 `badval`) restarts at (2u1 - 1, 2u2 - 1) from two

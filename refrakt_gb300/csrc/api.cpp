@@ -631,6 +631,8 @@ int rf_draw_to_bins(rf_sim* s, rf_flame* f, float* bins_rgba, uint32_t* bins_hit
     if (((uintptr_t)bins_rgba) & 15) return fail(RF_ERR_INVALID_ARG, "bins_rgba must be 16-byte aligned");
     if (s->splat == RF_SPLAT_TILE && ((uint64_t)s->tile[0] + s->tile[2] > W || (uint64_t)s->tile[1] + s->tile[3] > H))
         return fail(RF_ERR_INVALID_ARG, "rf_draw_to_bins: the splat tile does not lie inside the bin grid");
+    if (s->splat == RF_SPLAT_TILE && (uint64_t)W * H >= 0x80000000ull)
+        return fail(RF_ERR_CAPACITY, "rf_draw_to_bins: the tile splat takes bin grids of fewer than 2^31 bins");
     if (int rc = set_device(s)) return rc;
     float ss[6];
     genome_screen_affine(f->g, W, H, ss);

@@ -71,7 +71,7 @@ __device__ __forceinline__ void block_sum_to(double s, double* out) {
 // pass 1 of the fused image tail: the radius per bin, and the total density of the estimator's
 // output, sum_out a = sum over bins of a * (the kernel weights of its disc inside the grid) — the
 // log-density scale's sum (k2 = W * H / sum a) without a pass over the output.  A whole disc's
-// weights come from T.wsum (FP64); a disc cut by the grid's edge adds, per row inside the grid,
+// weights come from T.wsum; a disc cut by the grid's edge adds, per row inside the grid,
 // the difference of two prefix sums of that row's FP32 weights, staged per CTA in shared memory
 // for every radius up to kDeMaxSmemR (the fused path's radii).
 constexpr int kRowPrefixFloats = 1638;  // sum over r <= 12 of (r + 1) rows of 2r + 2 prefix sums
@@ -104,8 +104,13 @@ __global__ void de_radius_sum_kernel(const float4* __restrict__ in, uint32_t w, 
         }
     }
     __syncthreads();
+    // a thread's bins (a few dozen) are summed in FP32, the partial sums in FP64 (this part's
+    // FP64 rate is a small fraction of its FP32 rate)
+    __shared__ float s_wsum[kDeMaxSmemR + 1];
+    for (int r = threadIdx.x; r <= kDeMaxSmemR; r += blockDim.x) s_wsum[r] = (float)T.wsum[r];
+    __syncthreads();
     const uint32_t n = w * h;  // < 2^32 (the caller's grids hold fewer bins)
-    double s = 0.0;
+    float s = 0.0f;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float a = in[i].w;
         if (a == 0.0f || a != a) {
@@ -114,13 +119,9 @@ __global__ void de_radius_sum_kernel(const float4* __restrict__ in, uint32_t w, 
         }
         const int r = de_radius(a, T);
         rad[i] = (uint8_t)r;
-        if (r == 0) {
-            s += (double)a;
-            continue;
-        }
         const int y = (int)(i / w), x = (int)(i - (uint32_t)y * w);
-        if (x >= r && y >= r && x + r < (int)w && y + r < (int)h) {
-            s += (double)a * T.wsum[r];
+        if (x >= r && y >= r && x + r < (int)w && y + r < (int)h) {  // the whole disc (r = 0: weight 1)
+            s = fmaf(a, s_wsum[r], s);
             continue;
         }
         const int dx0 = max(-r, -x), dx1 = min(r, (int)w - 1 - x);
@@ -129,9 +130,9 @@ __global__ void de_radius_sum_kernel(const float4* __restrict__ in, uint32_t w, 
             const float* pre = s_pre + s_pbase[r] + (dy < 0 ? -dy : dy) * (2 * r + 2);
             ws += pre[dx1 + r + 1] - pre[dx0 + r];
         }
-        s += (double)(a * ws);
+        s = fmaf(a, ws, s);
     }
-    block_sum_to(s, sum_out);
+    block_sum_to((double)s, sum_out);
 }
 
 // tonemap.glsl:26: the per-bin log-density scale 0.5*brightness*log10(1 + a*k)/a (a > 0)
@@ -611,6 +612,7 @@ cudaError_t launch_tonemap_filter(const float4* in, uint32_t w, uint32_t h, uint
 
 // ---------------------------------------------------------------------------------------------
 static void de_tables(int R, int min_r, float curve, DeTables& T, std::vector<float>& wts) {
+    T = DeTables{};
     T.R = R;
     T.min_r = min_r;
     T.mode = (curve > 0.0f) ? 0 : (curve < 0.0f ? 1 : 2);

@@ -119,27 +119,34 @@ struct TileTarget {
     uint32_t* count;
 };
 
-// Every lane of the warp must call this; `local` is the point's index in the tile, or kNoBin when
-// the point misses the tile (then `bin`, its histogram bin or kNoBin, takes the global path).
-__device__ __forceinline__ void splat_tile(const BinTarget& t, const TileTarget& tt, uint32_t bin, uint32_t local,
-                                           float4 v) {
-    if (local == kNoBin) splat_global(t, bin, v);
-    const uint32_t other = __shfl_xor_sync(0xffffffffu, local, 1);
-    if (__any_sync(0xffffffffu, local != kNoBin && local == other)) {
-        uint32_t n;
-        if (warp_aggregate(local, v, n)) {
-            atomicAdd(&tt.rgba[local].x, v.x);
-            atomicAdd(&tt.rgba[local].y, v.y);
-            atomicAdd(&tt.rgba[local].z, v.z);
-            atomicAdd(&tt.rgba[local].w, v.w);
-            atomicAdd(&tt.count[local], n);
-        }
-    } else if (local != kNoBin) {
+__device__ __forceinline__ void tile_or_global_add(const BinTarget& t, const TileTarget& tt, uint32_t key, float4 v,
+                                                   uint32_t n) {
+    if (key & 0x80000000u) {  // a tile bin
+        const uint32_t local = key & 0x7fffffffu;
         atomicAdd(&tt.rgba[local].x, v.x);
         atomicAdd(&tt.rgba[local].y, v.y);
         atomicAdd(&tt.rgba[local].z, v.z);
         atomicAdd(&tt.rgba[local].w, v.w);
-        atomicAdd(&tt.count[local], 1u);
+        atomicAdd(&tt.count[local], n);
+    } else {
+        red_add_f32x4(t.at_rgba(key), v.x, v.y, v.z, v.w);
+        if (t.count) red_add_u32x1(t.at_count(key), n);
+    }
+}
+
+// Every lane of the warp must call this; `local` is the point's index in the tile, or kNoBin when
+// the point misses the tile (then `bin`, its histogram bin or kNoBin, takes the L2).  Tile bins
+// and histogram bins are aggregated within the warp alike (as splat_adaptive), under keys that
+// cannot collide (tile bins carry the top bit; the bin grid holds fewer than 2^31 bins).
+__device__ __forceinline__ void splat_tile(const BinTarget& t, const TileTarget& tt, uint32_t bin, uint32_t local,
+                                           float4 v) {
+    const uint32_t key = local != kNoBin ? (local | 0x80000000u) : bin;
+    const uint32_t other = __shfl_xor_sync(0xffffffffu, key, 1);
+    if (__any_sync(0xffffffffu, key != kNoBin && key == other)) {
+        uint32_t n;
+        if (warp_aggregate(key, v, n)) tile_or_global_add(t, tt, key, v, n);
+    } else if (key != kNoBin) {
+        tile_or_global_add(t, tt, key, v, 1u);
     }
 }
 

@@ -135,7 +135,7 @@ def test_splat_strategies_after_warmup(rk, compiler):
         assert np.allclose(b, b0, rtol=1e-4, atol=1e-3), mode
 
 
-@pytest.mark.parametrize("specialize,slots,tile", [(0, 2048, (20, 30, 70, 50)), (-1, 2048, (0, 0, 128, 40)),
+@pytest.mark.parametrize("specialize,slots,tile", [(0, 2048, (20, 30, 70, 50)), (-1, 2048, (0, 50, 128, 30)),
                                                    (0, 4096, (40, 40, 32, 32)), (0, 2048, (0, 0, 0, 0))])
 def test_tile_splat_bit_exact(rk, orc, compiler, specialize, slots, tile):
     """RF_SPLAT_TILE: the points inside the tile accumulate in each CTA's shared memory and reach
