@@ -49,7 +49,8 @@ WORKLOADS = {
     "contract": dict(name="contracting genome (seed 4, 6 xforms), 1920x1080 bins, 2^34 points",
                      genome=dict(kind=2, seed=4, n_xforms=0, final_xform=False, force_parametric=False),
                      genome_file="contract.flam3",
-                     out=(1920, 1080), ss=1, points=2 ** 34, de=None, image=False),
+                     out=(1920, 1080), ss=1, points=2 ** 34, de=None, image=False,
+                     splat="tile"),  # 26 hot bins: a shared-memory tile over them beats the L2
     "spacefill": dict(name="space-filling genome (seed 5, 16 xforms), 8192x8192 bins, 2^34 points",
                       genome=dict(kind=3, seed=5, n_xforms=0, final_xform=False, force_parametric=False),
                       genome_file="spacefill.flam3",
@@ -931,8 +932,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-badval-reset", action="store_true",
                     help="keep walkers that leave the plane lost (the reference's default, flame.glsl:68)")
-    ap.add_argument("--splat", default="auto", choices=["auto", "global", "warp", "tile"],
-                    help="splat strategy; tile: a shared-memory histogram tile over the attractor's bounding box")
+    ap.add_argument("--splat", default=None, choices=["auto", "global", "warp", "tile"],
+                    help="splat strategy (default: the workload's, else auto); tile: a shared-memory histogram "
+                         "tile over the attractor's bounding box")
     ap.add_argument("--specialize", default="auto", choices=["auto", "on", "off"],
                     help="genome-specialised chaos kernel compiled at run time")
     ap.add_argument("--learned-train", type=int, default=2000)
@@ -953,6 +955,8 @@ def main():
     ap.add_argument("--workload", default="frame1080", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     select_workload(args.workload)
+    if args.splat is None:
+        args.splat = WL.get("splat", "auto")
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch":
