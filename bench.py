@@ -928,7 +928,8 @@ def main():
     ap.add_argument("--cta-slots", type=int, default=0, help="walker slots per CTA (0: the workload's default)")
     ap.add_argument("--cta-threads", type=int, default=0)
     ap.add_argument("--ctas-per-sm", type=int, default=4)
-    ap.add_argument("--steps-per-launch", type=int, default=32)
+    ap.add_argument("--steps-per-launch", type=int, default=256,
+                    help="passes per chaos launch (the library's default; at most 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-badval-reset", action="store_true",
                     help="keep walkers that leave the plane lost (the reference's default, flame.glsl:68)")

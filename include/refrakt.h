@@ -186,8 +186,12 @@ typedef struct {
                                    256, 512, 1024, 2048 or 4096 (0 = 4096) */
     uint32_t cta_threads;       /* threads per CTA: 256, 512 or 1024, dividing cta_slots
                                    (0 = min(cta_slots, 1024)) */
-    uint32_t steps_per_launch;  /* passes per persistent launch L (0 = 32; 1 = the reference's
-                                   per-pass global gather) */
+    uint32_t steps_per_launch;  /* passes per persistent launch L, at most 256 (0 = 256; 1 = the
+                                   reference's per-pass global gather).  Walkers mix within their
+                                   CTA's slots every pass and across CTAs every L passes; L does
+                                   not change the histogram's noise (the domains are independent
+                                   chaos games), and longer launches spend less on the launch
+                                   boundary (the 1080p frame: 47.8 Gpoints/s at 32, 50.8 at 256) */
     int32_t  device;            /* CUDA device ordinal */
     int32_t  specialize;        /* genome-specialised kernels compiled at run time (NVRTC) for each
                                    genome structure rf_warmup meets: 0 = when the run-time compiler

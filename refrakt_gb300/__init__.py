@@ -451,7 +451,7 @@ class Sim:
     per-flame ``warmup`` / ``draw_to_bins`` (src/flame.cpp:105-330)."""
 
     def __init__(self, walkers, temporal_samples=1, shuffle_count=1024, seed=0, cta_slots=4096, cta_threads=0,
-                 steps_per_launch=32, device=0, specialize=0):
+                 steps_per_launch=0, device=0, specialize=0):
         d = SimDesc(walkers, temporal_samples, shuffle_count, seed, cta_slots, cta_threads, steps_per_launch, device,
                     specialize)
         h = ctypes.c_void_p()

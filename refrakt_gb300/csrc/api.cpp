@@ -458,7 +458,7 @@ int rf_sim_create(const rf_sim_desc* d, rf_sim** out) {
     s->ppts = (uint32_t)ppts;
     s->slots = slots;
     s->threads = threads;
-    s->L = d->steps_per_launch ? std::min<uint32_t>(d->steps_per_launch, 256) : 32;
+    s->L = d->steps_per_launch ? std::min<uint32_t>(d->steps_per_launch, 256) : 256;
     s->table_size = d->shuffle_count ? d->shuffle_count : 1024;
     auto cleanup = [&](int rc) { rf_sim_destroy(s); return rc; };
     if (int rc = set_device(s)) { delete s; return rc; }

@@ -29,8 +29,8 @@ def _run(rk, f, N, W, H, F, D, seed, specialize, trace=0, **kw):
 def test_affine_genome_bit_exact(rk, orc, compiler, cta, threads):
     f = rk.Flame.from_xml(LINEAR, compiler)
     N, F, D = 8192, 20, 40
-    a = _run(rk, f, N, 256, 256, F, D, 3, 1, cta_slots=cta, cta_threads=threads)
-    b = _run(rk, f, N, 256, 256, F, D, 3, -1, cta_slots=cta, cta_threads=threads)
+    a = _run(rk, f, N, 256, 256, F, D, 3, 1, cta_slots=cta, cta_threads=threads, steps_per_launch=32)
+    b = _run(rk, f, N, 256, 256, F, D, 3, -1, cta_slots=cta, cta_threads=threads, steps_per_launch=32)
     assert np.array_equal(a["hits"], b["hits"])
     assert np.allclose(a["rgba"], b["rgba"], rtol=1e-4, atol=1e-3)
     r = orc.Genome(LINEAR).chaos(N, 256, 256, fuse=F, draw=D, seed=3, fp64=False, shuffle_mode=1, cta_slots=cta,
@@ -86,7 +86,7 @@ def test_temporal_samples_with_rotation(rk, orc, compiler, specialize):
     xml = LINEAR.replace('linear="1"/>', 'linear="1" animate="1"/>', 1)
     f = rk.Flame.from_xml(xml, compiler)
     N, F, D, T, tss = 16384, 20, 32, 4, 0.5
-    sim = rk.Sim(N, temporal_samples=T, seed=6, specialize=specialize)
+    sim = rk.Sim(N, temporal_samples=T, seed=6, specialize=specialize, steps_per_launch=32)
     sim.warmup(f, F - 1, tss_width=tss)
     bins, hits = _bins(256, 256)
     sim.draw_to_bins(f, bins, hits, 256, 256, D)
@@ -101,7 +101,7 @@ def test_temporal_samples_with_rotation(rk, orc, compiler, specialize):
     assert l1 <= 1.5 * floor
     # static genome (no animate): the temporal samples do not rotate and stay bit-exact
     f2 = rk.Flame.from_xml(LINEAR, compiler)
-    sim2 = rk.Sim(N, temporal_samples=T, seed=6, specialize=specialize)
+    sim2 = rk.Sim(N, temporal_samples=T, seed=6, specialize=specialize, steps_per_launch=32)
     sim2.warmup(f2, F - 1, tss_width=tss)
     bins2, hits2 = _bins(256, 256)
     sim2.draw_to_bins(f2, bins2, hits2, 256, 256, D)
@@ -145,7 +145,7 @@ def test_tile_splat_bit_exact(rk, orc, compiler, specialize, slots, tile):
     W = H = 128
     f = rk.Flame.from_xml(LINEAR, compiler)
     N, F, D = 8192, 20, 40
-    sim = rk.Sim(N, seed=5, cta_slots=slots, specialize=specialize)
+    sim = rk.Sim(N, seed=5, cta_slots=slots, specialize=specialize, steps_per_launch=32)
     sim.set_splat(rk.SPLAT_TILE)
     sim.set_splat_tile(*tile)
     sim.warmup(f, F - 1)
