@@ -217,14 +217,15 @@ def _profile_figure(workload, key, summary="chaos_kernel_%s.md"):
         return None
 
 
-def kernel_build_id(flame):
+def kernel_build_id(flame, variant=""):
     """Identifies the chaos kernel a run launches: a hash of the genome-specialised kernel's
-    generated source and the device headers it is compiled from.  The committed ncu summary
+    generated source, the device headers it is compiled from and the launch's compile-time
+    choices (`variant`: splat strategy, walker reset, exchange).  The committed ncu summary
     records the id of the build it captured; bench.py uses its figures only when they match."""
     import hashlib
     sys.path.insert(0, os.path.join(ROOT, "refrakt_gb300"))
     from nvbuild import RTC_HEADERS
-    h = hashlib.sha256(flame.kernel_source().encode())
+    h = hashlib.sha256(flame.kernel_source().encode() + variant.encode())
     for name in RTC_HEADERS + ["chaos_body.cuh"]:
         with open(os.path.join(ROOT, "refrakt_gb300", "csrc", name), "rb") as f:
             h.update(f.read())
@@ -410,6 +411,10 @@ def run_native(args):
     sim.set_splat({"auto": R.SPLAT_AUTO, "global": R.SPLAT_GLOBAL, "warp": R.SPLAT_WARP,
                    "tile": R.SPLAT_TILE}[args.splat])
     sim.set_bad_value_reset(reset)
+    sim.set_pipelined_exchange(args.exchange == "pipelined")
+    threads = args.cta_threads or min(cta, 1024)
+    exchange = "pipelined" if args.exchange == "pipelined" and args.splat != "tile" and cta // threads >= 3 \
+        else "barrier"
     tile = None
     if args.splat == "tile":  # the shared-memory tile: the attractor's bounding box from a short probe
         sim.warmup(flame, FUSE - 1)
@@ -513,7 +518,7 @@ def run_native(args):
     pts_per_launch = walkers * args.steps_per_launch
     pts_s = pts_per_launch / (per_launch_ms * 1e-3)
     prof_key = {"frame1080": "1080p"}.get(args.workload, args.workload)
-    build = kernel_build_id(flame) if sim.specialized() else None
+    build = kernel_build_id(flame, "%s/%d/%s" % (args.splat, int(reset), exchange)) if sim.specialized() else None
     same_build = build is not None and build == _profile_build(prof_key)
     inst = _profile_figure(prof_key, "warp instructions per point") if same_build else None
     traffic = _traffic(prof_key) if same_build else None
@@ -547,6 +552,7 @@ def run_native(args):
         "config": workload_config(reset),
         "launch": {"walkers": walkers, "cta_slots": cta, "steps_per_launch": args.steps_per_launch,
                    "passes_per_frame": passes, "splat": args.splat, "splat_tile": tile,
+                   "exchange": exchange if sim.specialized() else "barrier",
                    "specialized_kernel": sim.specialized(),
                    "kernel_build": build, "first_warmup_s": first_warmup_s,
                    "parallelism": "replicas" if ws > 1 else "single"},
@@ -936,6 +942,9 @@ def main():
     ap.add_argument("--splat", default=None, choices=["auto", "global", "warp", "tile"],
                     help="splat strategy (default: the workload's, else auto); tile: a shared-memory histogram "
                          "tile over the attractor's bounding box")
+    ap.add_argument("--exchange", default="pipelined", choices=["pipelined", "barrier"],
+                    help="walker exchange of the specialised chaos kernel: mbarrier-pipelined (default) or one "
+                         "CTA barrier per pass")
     ap.add_argument("--specialize", default="auto", choices=["auto", "on", "off"],
                     help="genome-specialised chaos kernel compiled at run time")
     ap.add_argument("--learned-train", type=int, default=2000)

@@ -45,7 +45,9 @@ enum rf_status {
     RF_ERR_CUDA = 6,          /* a CUDA runtime call failed */
     RF_ERR_NEEDS_WARMUP = 7,  /* rf_draw_to_bins before rf_warmup for this flame (flame.hpp:86) */
     RF_ERR_IO = 8,            /* file could not be read or written */
-    RF_ERR_NO_DEVICE = 9      /* no CUDA device of the supported architecture */
+    RF_ERR_NO_DEVICE = 9,     /* no CUDA device of the supported architecture */
+    RF_ERR_TIMEOUT = 10       /* a bounded device-side wait gave up (a chaos launch's walker exchange);
+                                 the results of that launch are invalid */
 };
 
 typedef struct rf_compiler rf_compiler;
@@ -245,6 +247,16 @@ RF_API int  rf_set_splat_tile(rf_sim* s, uint32_t x0, uint32_t y0, uint32_t w, u
    passes a genome with singular variations (spherical, julian ...) binns fewer and fewer points.
    Takes effect from the next rf_warmup / rf_draw_to_bins launch. */
 RF_API int  rf_set_bad_value_reset(rf_sim* s, int on);
+/* The walker exchange of the genome-specialised chaos kernel.  1 (default): pipelined — a Sim with
+   four slots per thread builds its shuffle table so that the first phase of a pass takes
+   its walkers only from the previous pass's earlier phases, and a thread starts the next pass as
+   soon as every thread has finished those (CTA-wide mbarriers instead of a barrier per pass; the
+   walkers triple-buffered in shared memory).  Not with the tile splat, nor for a genome program
+   too large for the third buffer: those launches, and 0, take one CTA barrier per pass.  Both
+   forms give identical results for the same table.  A wait that runs out (bounded) makes the next
+   synchronising call (rf_draw_to_bins with `drawn`, rf_sim_counters, rf_render) return
+   RF_ERR_TIMEOUT.  Takes effect from the next launch. */
+RF_API int  rf_set_pipelined_exchange(rf_sim* s, int on);
 /* [0] points binned and [1] points emitted (opacity > 0) by the last rf_draw_to_bins call,
    [2] walker-steps since rf_warmup. */
 RF_API int  rf_sim_counters(rf_sim* s, uint64_t out[3]);

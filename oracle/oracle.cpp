@@ -817,6 +817,29 @@ inline uint32_t palette_index(double c) {  // flame.glsl:84: min(255, uint(ceil(
 // ---------------------------------------------------------------------------------------------
 // Chaos game — flame.glsl:41-90, flame.cpp:228-330
 // ---------------------------------------------------------------------------------------------
+// Permutation k of the CUDA kernel's shuffle table over a CTA's n slots.  phases = S > 1: the
+// pipelined table — destinations [0, P), P = n/S (the first phase of a pass), take sources from
+// [0, M), M = n - P (the previous pass's first S-1 phases), in one keyed order; the other
+// destinations take the remaining M sources (the rest of that order, then [M, n)) in a second.
+void shuffle_table(uint64_t seed, uint32_t k, uint32_t n, uint32_t phases, uint32_t* out) {
+    const uint32_t P = phases > 1 ? n / phases : 0;
+    if (!P) {
+        const uint64_t key = derive_key(seed, k, 0, TAG_TABLE);
+        for (uint32_t j = 0; j < n; j++) out[j] = feistel(j, n, key);
+        return;
+    }
+    const uint32_t M = n - P;
+    const uint64_t k1 = derive_key(seed, k, 1, TAG_TABLE), k2 = derive_key(seed, k, 2, TAG_TABLE);
+    for (uint32_t d = 0; d < n; d++) {
+        if (d < P) {
+            out[d] = feistel(d, M, k1);
+        } else {
+            const uint32_t r = feistel(d - P, M, k2);
+            out[d] = r < M - P ? feistel(P + r, M, k1) : M + (r - (M - P));
+        }
+    }
+}
+
 template <class T>
 int chaos(const orc_genome* g, const orc_chaos_cfg* cfg, double* rgba, uint64_t* hits, uint8_t* trace,
           uint64_t* counters) {
@@ -852,10 +875,8 @@ int chaos(const orc_genome* g, const orc_chaos_cfg* cfg, double* rgba, uint64_t*
     const uint32_t cs_ = cfg->cta_slots;
     if (cfg->shuffle_mode == 1) {
         table.assign(cfg->table_size, std::vector<uint32_t>(cs_));
-        for (uint32_t k = 0; k < cfg->table_size; k++) {
-            uint64_t key = derive_key(cfg->table_seed_set ? cfg->table_seed : cfg->seed, k, 0, TAG_TABLE);
-            for (uint32_t j = 0; j < cs_; j++) table[k][j] = feistel(j, cs_, key);
-        }
+        const uint64_t tseed = cfg->table_seed_set ? cfg->table_seed : cfg->seed;
+        for (uint32_t k = 0; k < cfg->table_size; k++) shuffle_table(tseed, k, cs_, cfg->table_phases, table[k].data());
     }
     auto is_launch_start = [&](uint32_t p) {
         const uint32_t F = cfg->fuse_passes, L = cfg->steps_per_launch;
@@ -988,6 +1009,9 @@ void orc_sample_points(uint32_t count, float* out4) {
 }
 uint32_t orc_feistel(uint32_t x, uint32_t n, uint64_t key) { return feistel(x, n, key); }
 uint64_t orc_derive_key(uint64_t seed, uint64_t a, uint64_t b, uint64_t tag) { return derive_key(seed, a, b, tag); }
+void orc_shuffle_table(uint32_t n, uint32_t count, uint64_t seed, uint32_t phases, uint32_t* out) {
+    for (uint32_t k = 0; k < count; k++) shuffle_table(seed, k, n, phases, out + (size_t)k * n);
+}
 
 int orc_genome_from_xml(const char* xml, orc_genome** out, char* err, int errlen) {
     auto* g = new orc_genome();

@@ -34,6 +34,9 @@ void orc_sample_points(uint32_t count, float* out4);
 /* Keyed permutations used by the kernel's walker-shuffle schedule. */
 uint32_t orc_feistel(uint32_t x, uint32_t n, uint64_t key);
 uint64_t orc_derive_key(uint64_t seed, uint64_t a, uint64_t b, uint64_t tag);
+/* `count` permutations of the kernel's shuffle table over n slots (out: count * n); phases as
+   orc_chaos_cfg.table_phases */
+void orc_shuffle_table(uint32_t n, uint32_t count, uint64_t seed, uint32_t phases, uint32_t* out);
 
 /* Genome: reference flam3 loader semantics (src/flame.cpp:160-226). */
 int  orc_genome_from_xml(const char* xml, orc_genome** out, char* err, int errlen);
@@ -84,6 +87,10 @@ typedef struct {
     int      table_seed_set;   /* shuffle_mode 1: 1 = the local table is keyed by table_seed, */
     uint64_t table_seed;       /*   0 = by seed (the batched launch shares one table) */
     int      badval_reset;     /* 1: the walker reset flame.glsl:68 keeps commented out */
+    uint32_t table_phases;     /* shuffle_mode 1: 0 = uniform table permutations; S > 1 = the
+                                  pipelined table of S phases per pass: the first cta_slots/S
+                                  destinations draw their sources from the first
+                                  cta_slots*(S-1)/S slots only (the library uses S = 4) */
 } orc_chaos_cfg;
 
 /* rgba: W*H*4 doubles (may be NULL), hits: W*H u64 (may be NULL),

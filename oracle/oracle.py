@@ -45,7 +45,7 @@ class ChaosCfg(ctypes.Structure):
                 ("cta_slots", ctypes.c_uint32), ("steps_per_launch", ctypes.c_uint32),
                 ("table_size", ctypes.c_uint32), ("tss_width", ctypes.c_float),
                 ("threads", ctypes.c_int), ("table_seed_set", ctypes.c_int), ("table_seed", ctypes.c_uint64),
-                ("badval_reset", ctypes.c_int)]
+                ("badval_reset", ctypes.c_int), ("table_phases", ctypes.c_uint32)]
 
 
 def lib():
@@ -65,6 +65,9 @@ def lib():
         L.orc_feistel.restype = ctypes.c_uint32
         L.orc_derive_key.argtypes = [ctypes.c_uint64] * 4
         L.orc_derive_key.restype = ctypes.c_uint64
+        L.orc_shuffle_table.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32,
+                                        ctypes.c_void_p]
+        L.orc_shuffle_table.restype = None
         L.orc_genome_from_xml.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_char_p, ctypes.c_int]
         L.orc_genome_free.argtypes = [ctypes.c_void_p]
         L.orc_genome_num_xforms.argtypes = [ctypes.c_void_p]
@@ -158,6 +161,13 @@ def derive_key(seed, a, b, tag):
     return lib().orc_derive_key(seed, a, b, tag)
 
 
+def shuffle_table(n, count, seed, phases=0):
+    """The kernel's shuffle table: `count` permutations of a CTA's n slots ([count, n] uint32)."""
+    out = np.zeros((count, n), np.uint32)
+    lib().orc_shuffle_table(n, count, seed, phases, _ptr(out))
+    return out
+
+
 class Genome:
     def __init__(self, xml):
         h = ctypes.c_void_p()
@@ -233,10 +243,16 @@ class Genome:
 
     def chaos(self, walkers, width, height, fuse=20, draw=16, seed=0, temporal_samples=1, fp64=True,
               shuffle_mode=0, cta_slots=1024, steps_per_launch=32, table_size=1024, tss_width=0.02,
-              trace=False, want_rgba=True, table_seed=None, badval_reset=False, threads=1):
+              trace=False, want_rgba=True, table_seed=None, badval_reset=False, threads=1, table_phases=None,
+              cta_threads=None):
+        # the library's Sim builds its shuffle table for slots / threads phases per pass when that
+        # is 4 (threads = min(slots, 1024) unless given); the batched launch's table is uniform
+        if table_phases is None:
+            spt = cta_slots // (cta_threads or min(cta_slots, 1024))
+            table_phases = 0 if table_seed is not None or spt < 3 else spt
         cfg = ChaosCfg(walkers, temporal_samples, seed, fuse, draw, width, height, int(fp64), shuffle_mode,
                        cta_slots, steps_per_launch, table_size, tss_width, threads, int(table_seed is not None),
-                       table_seed or 0, int(bool(badval_reset)))
+                       table_seed or 0, int(bool(badval_reset)), table_phases)
         rgba = np.zeros((height, width, 4), np.float64) if want_rgba else None
         hits = np.zeros((height, width), np.uint64)
         tr = np.zeros((fuse + draw, walkers // 256), np.uint8) if trace else None

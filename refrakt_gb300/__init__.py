@@ -148,6 +148,7 @@ _SIGS = {
                          ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "rf_set_splat": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rf_set_bad_value_reset": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rf_set_pipelined_exchange": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rf_set_splat_tile": ([ctypes.c_void_p] + [ctypes.c_uint32] * 4, ctypes.c_int),
     "rf_set_bin_layout": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rf_sim_counters": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
@@ -502,6 +503,11 @@ class Sim:
         """Restart walkers that leave the plane (rf_set_bad_value_reset; the reference keeps this
         step commented out at shaders/flame.glsl:68, so the default is off)."""
         _check(library().rf_set_bad_value_reset(self._h, int(bool(on))))
+
+    def set_pipelined_exchange(self, on):
+        """Pipelined walker exchange of the specialised chaos kernel (rf_set_pipelined_exchange;
+        default on): the same results as one CTA barrier per pass, with less waiting."""
+        _check(library().rf_set_pipelined_exchange(self._h, int(bool(on))))
 
     def set_bin_layout(self, layout):
         """BINS_AUTO, BINS_DIRECT or BINS_INTERLEAVED (rf_set_bin_layout)."""

@@ -71,6 +71,25 @@ size_t copy_out(const std::string& s, char* buf, size_t cap) {
     return s.size() + 1;
 }
 
+// The pipelined walker exchange (chaos_body.cuh, PIPE) runs in the specialised kernels when the
+// Sim's shuffle table was built for it (4 slots per thread), the splat is not the tile
+// splat (whose shared-memory histogram needs the room of the third walker buffer) and the
+// genome program fits beside the triple-buffered walkers.
+bool use_pipe(const rf_sim* s, int splat) {
+    return s->pipe && s->table_phases >= 3 && splat != 3 &&
+           chaos_smem(s->slots, s->prog_words, s->L, 0, 1) <= kMaxCtaSmem;
+}
+
+// RF_ERR_TIMEOUT when a pipelined exchange wait in an earlier launch ran out (counters[3]); call
+// after the stream was synchronised
+int check_exchange(rf_sim* s) {
+    unsigned long long n = 0;
+    RF_CUDA(cudaMemcpy(&n, s->counters + 3, sizeof n, cudaMemcpyDeviceToHost));
+    if (n) return fail(RF_ERR_TIMEOUT, std::to_string(n) + " walker-exchange waits of the chaos kernel ran out; "
+                                       "the histogram of those launches is invalid");
+    return RF_OK;
+}
+
 // the chaos kernel reads these counters as unsigned long long
 int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4* bins, uint32_t* hits,
                   uint32_t W, uint32_t H, const float ss[6]) {
@@ -112,15 +131,17 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.trace_passes = s->trace_passes;
         a.n_groups = (uint32_t)(s->N / kGroup);
         const uint32_t grid = (uint32_t)(s->N / s->slots);
-        if (s->spec && (s->spec_splat != a.splat || s->spec_reset != a.reset)) {
-            // the splat strategy or the reset changed since warmup: the kernel compiled for them
+        const int pipe = s->spec && use_pipe(s, a.splat) ? 1 : 0;
+        if (s->spec && (s->spec_splat != a.splat || s->spec_reset != a.reset || s->spec_pipe != pipe)) {
+            // the splat strategy, the reset or the exchange changed since warmup: the kernel compiled for them
             const void* k = nullptr;
             if (int rc = spec_kernel(s->spec_prog, (int)s->threads, (int)s->slots, s->device, &k, SpecKind::Chaos,
-                                     a.splat, a.reset))
+                                     a.splat, a.reset, pipe))
                 return rc;
             s->spec = k;
             s->spec_splat = a.splat;
             s->spec_reset = a.reset;
+            s->spec_pipe = pipe;
         }
         const uint32_t tile_bins = a.splat == 3 && a.draw ? a.tile_w * a.tile_h : 0u;
         if (chaos_smem(s->slots, a.prog_words, a.steps, tile_bins) > kMaxCtaSmem)
@@ -128,7 +149,7 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
                                          " bins exceeds the shared memory beside " + std::to_string(s->slots) +
                                          " walker slots");
         cudaError_t e = s->spec ? launch_spec(s->spec, (int)s->threads, (int)s->slots, a, grid,
-                                              chaos_smem(s->slots, a.prog_words, a.steps, tile_bins), s->stream)
+                                              chaos_smem(s->slots, a.prog_words, a.steps, tile_bins, pipe), s->stream)
                                 : launch_chaos((int)s->threads, (int)s->slots, a, grid, s->stream);
         if (e != cudaSuccess) return cuda_fail(e, "chaos kernel launch");
         s->cur ^= 1;
@@ -476,7 +497,10 @@ int rf_sim_create(const rf_sim_desc* d, rf_sim** out) {
     ALLOC(s->counters, 8 * sizeof(unsigned long long));
 #undef ALLOC
     if ((e = launch_init_rng(s->rng, s->N, d->seed, s->stream)) != cudaSuccess) return cleanup(cuda_fail(e, "rng init"));
-    if ((e = launch_shuffle_table(s->table, slots, s->table_size, d->seed, s->stream)) != cudaSuccess)
+    // the pipelined exchange's permutations, for 4 slots per thread (with 2 the first phase would
+    // take exactly the first phase's walkers and the domain would split in two)
+    s->table_phases = slots / threads >= 3 ? slots / threads : 0;
+    if ((e = launch_shuffle_table(s->table, slots, s->table_size, d->seed, s->stream, s->table_phases)) != cudaSuccess)
         return cleanup(cuda_fail(e, "shuffle table"));
     if ((e = cudaMemsetAsync(s->counters, 0, 8 * sizeof(unsigned long long), s->stream)) != cudaSuccess)
         return cleanup(cuda_fail(e, "memset"));
@@ -540,12 +564,14 @@ int rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_width) {
     s->spec = nullptr;
     if (s->d.specialize >= 0) {
         const void* k = nullptr;
+        const int pipe = use_pipe(s, splat_code(s->splat)) ? 1 : 0;
         const int rc = spec_kernel(prog, (int)s->threads, (int)s->slots, s->device, &k, SpecKind::Chaos,
-                                   splat_code(s->splat), s->reset);
+                                   splat_code(s->splat), s->reset, pipe);
         if (rc == RF_OK) {
             s->spec = k;
             s->spec_splat = splat_code(s->splat);
             s->spec_reset = s->reset;
+            s->spec_pipe = pipe;
             s->spec_prog = prog;
         } else if (s->d.specialize > 0) {
             return rc;  // required
@@ -621,6 +647,12 @@ int rf_set_bad_value_reset(rf_sim* s, int on) {
     return RF_OK;
 }
 
+int rf_set_pipelined_exchange(rf_sim* s, int on) {
+    if (!s || (on != 0 && on != 1)) return fail(RF_ERR_INVALID_ARG, "rf_set_pipelined_exchange: null sim or flag not 0/1");
+    s->pipe = on;
+    return RF_OK;
+}
+
 int rf_draw_to_bins(rf_sim* s, rf_flame* f, float* bins_rgba, uint32_t* bins_hits, uint32_t W, uint32_t H,
                     uint32_t num_iter, uint64_t* drawn) {
     if (!s || !f || !bins_rgba) return fail(RF_ERR_INVALID_ARG, "rf_draw_to_bins: null argument");
@@ -642,6 +674,7 @@ int rf_draw_to_bins(rf_sim* s, rf_flame* f, float* bins_rgba, uint32_t* bins_hit
     if (drawn) {
         unsigned long long c[1];
         RF_CUDA(cudaStreamSynchronize(s->stream));
+        if (int rc = check_exchange(s)) return rc;
         RF_CUDA(cudaMemcpy(c, s->counters, sizeof c, cudaMemcpyDeviceToHost));
         *drawn = c[0];
     }
@@ -653,6 +686,7 @@ int rf_sim_counters(rf_sim* s, uint64_t out[3]) {
     if (int rc = set_device(s)) return rc;
     unsigned long long c[3];
     RF_CUDA(cudaStreamSynchronize(s->stream));
+    if (int rc = check_exchange(s)) return rc;
     RF_CUDA(cudaMemcpy(c, s->counters, sizeof c, cudaMemcpyDeviceToHost));
     for (int i = 0; i < 3; i++) out[i] = c[i];
     return RF_OK;
@@ -898,6 +932,7 @@ int rf_render(rf_sim* s, rf_flame* f, const rf_render_desc* d, uint8_t* out, dou
     if (e == cudaSuccess) e = cudaEventRecord(e1, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) return done(cuda_fail(e, "rf_render"));
+    if (int rc = check_exchange(s)) return done(rc);
     if (stats) {
         unsigned long long c[2];
         float ms = 0;

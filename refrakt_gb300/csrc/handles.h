@@ -32,7 +32,7 @@ struct rf_sim {
     uint32_t* progs = nullptr;
     uint32_t prog_stride = 0, prog_words = 0;
     float4* palette = nullptr;
-    unsigned long long* counters = nullptr;  // [0] drawn [1] emitted [2] steps [3] call drawn [4] call emitted
+    unsigned long long* counters = nullptr;  // [0] drawn [1] emitted [2] walker-steps [3] exchange waits that ran out
     uint8_t* trace = nullptr;
     uint32_t trace_passes = 0;
     uint64_t warmed_uid = 0, warmed_version = 0;
@@ -43,6 +43,9 @@ struct rf_sim {
     int reset = 0;                    // walker reset of flame.glsl:68 (rf_set_bad_value_reset)
     uint32_t tile[4] = {0, 0, 0, 0};  // the tile splat's bins: x0, y0, w, h (rf_set_splat_tile)
     int spec_reset = -1;              // the reset setting compiled into the specialised kernel
+    int spec_pipe = 0;                // 1: the specialised kernel has the pipelined walker exchange
+    uint32_t table_phases = 0;        // phases per pass the shuffle table is pipelined for (0: uniform)
+    int pipe = 1;                     // pipelined exchange allowed (rf_set_pipelined_exchange)
     std::vector<uint32_t> spec_prog;  // the warmed program, to specialise again for another strategy
     int bin_layout = RF_BINS_AUTO;
     uint32_t rgba_shift = 0, count_shift = 0;  // BinTarget addressing of the next launches

@@ -46,12 +46,29 @@ __global__ void init_rng_kernel(uint4* rng, uint64_t n, uint64_t seed) {
     rng[i] = make_uint4(s.a, s.b, s.c, s.d);
 }
 
-// the walker-shuffle table: `count` keyed permutations of [0, n)
-__global__ void shuffle_table_kernel(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed) {
+// the walker-shuffle table: `count` keyed permutations of [0, n).  phases = S > 1 gives the
+// pipelined exchange's permutations (chaos_body.cuh, PIPE): destinations [0, n/S) — the first
+// phase of a pass — take their sources from [0, M), M = n - n/S, the slots of the previous pass's
+// first S-1 phases, in one keyed order; the other destinations take the remaining M sources (the
+// rest of that order, then [M, n)) in a second keyed order.  Every permutation stays a bijection;
+// with S >= 3 every phase's walkers reach every phase (S = 2 would split the domain in two).
+__global__ void shuffle_table_kernel(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed, uint32_t phases) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (uint64_t)n * count) return;
     const uint32_t k = (uint32_t)(i / n), j = (uint32_t)(i - (uint64_t)k * n);
-    out[i] = (uint16_t)feistel(j, n, derive_key(seed, k, 0, TAG_TABLE));
+    const uint32_t P = phases > 1 ? n / phases : 0;
+    if (!P) {
+        out[i] = (uint16_t)feistel(j, n, derive_key(seed, k, 0, TAG_TABLE));
+        return;
+    }
+    const uint32_t M = n - P;
+    const uint64_t k1 = derive_key(seed, k, 1, TAG_TABLE);
+    if (j < P) {
+        out[i] = (uint16_t)feistel(j, M, k1);
+    } else {
+        const uint32_t r = feistel(j - P, M, derive_key(seed, k, 2, TAG_TABLE));
+        out[i] = (uint16_t)(r < M - P ? feistel(P + r, M, k1) : M + (r - (M - P)));
+    }
 }
 
 // animate.tpl.glsl:18-96 — one program copy per temporal sample, each xform's linear part
@@ -97,8 +114,8 @@ __global__ void probe_kernel(const uint32_t* prog, int xform, uint32_t n, const 
 // ---------------------------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------------------------
-size_t chaos_smem(int slots, uint32_t prog_words, uint32_t steps, uint32_t tile_bins) {
-    return chaos_smem_bytes(slots, prog_words, steps, tile_bins);
+size_t chaos_smem(int slots, uint32_t prog_words, uint32_t steps, uint32_t tile_bins, int pipe) {
+    return chaos_smem_bytes(slots, prog_words, steps, tile_bins, pipe);
 }
 
 template <int THREADS, int SPT>
@@ -140,10 +157,11 @@ cudaError_t launch_init_rng(uint4* rng, uint64_t n, uint64_t seed, cudaStream_t 
     return cudaGetLastError();
 }
 
-cudaError_t launch_shuffle_table(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed, cudaStream_t st) {
+cudaError_t launch_shuffle_table(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed, cudaStream_t st,
+                                 uint32_t phases) {
     const uint64_t total = (uint64_t)n * count;
     const uint32_t b = 256;
-    shuffle_table_kernel<<<(unsigned)((total + b - 1) / b), b, 0, st>>>(out, n, count, seed);
+    shuffle_table_kernel<<<(unsigned)((total + b - 1) / b), b, 0, st>>>(out, n, count, seed, phases);
     return cudaGetLastError();
 }
 

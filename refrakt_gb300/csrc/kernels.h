@@ -14,13 +14,14 @@ namespace rfk {
 
 
 
-size_t chaos_smem(int slots, uint32_t prog_words, uint32_t steps, uint32_t tile_bins = 0);
+size_t chaos_smem(int slots, uint32_t prog_words, uint32_t steps, uint32_t tile_bins = 0, int pipe = 0);
 constexpr size_t kMaxCtaSmem = 232448;  // dynamic shared memory a CTA may opt into (227 KB)
 bool chaos_shape_supported(int threads, int slots);
 cudaError_t launch_chaos(int threads, int slots, const ChaosArgs& a, uint32_t grid, cudaStream_t st);
 cudaError_t launch_merge_records(float4* rec, size_t n, float4* bins, uint32_t* hits, cudaStream_t st);
 cudaError_t launch_init_rng(uint4* rng, uint64_t n, uint64_t seed, cudaStream_t st);
-cudaError_t launch_shuffle_table(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed, cudaStream_t st);
+cudaError_t launch_shuffle_table(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed, cudaStream_t st,
+                                 uint32_t phases = 0);
 cudaError_t launch_animate(const uint32_t* base, uint32_t words, uint32_t T, float tss, uint32_t* out,
                            uint32_t stride, cudaStream_t st);
 cudaError_t launch_probe(const uint32_t* prog, int xform, uint32_t n, const float* in, uint32_t* rng,

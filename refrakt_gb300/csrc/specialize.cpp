@@ -146,7 +146,8 @@ static std::string gen_eval(const std::vector<uint32_t>& prog) {
     return o.str();
 }
 
-std::string spec_source(const std::vector<uint32_t>& prog, int threads, int spt, SpecKind kind, int splat, int reset) {
+std::string spec_source(const std::vector<uint32_t>& prog, int threads, int spt, SpecKind kind, int splat, int reset,
+                        int pipe) {
     std::ostringstream o;
     o << "// generated: genome-specialised " << (kind == SpecKind::Batch ? "batch" : "chaos") << " kernel\n"
       << (kind == SpecKind::Batch ? "#include \"batch_body.cuh\"\n" : "#include \"chaos_body.cuh\"\n")
@@ -158,7 +159,8 @@ std::string spec_source(const std::vector<uint32_t>& prog, int threads, int spt,
     else
         o << "extern \"C\" __global__ void __launch_bounds__(" << threads << ", " << 1024 / threads
           << ") rfk_chaos_spec(const rfk::ChaosArgs A) {\n  rfk::chaos_body<" << threads << ", " << spt
-          << ", rfk::GenEval, " << (splat >= 0 ? splat : -1) << ", " << (reset >= 0 ? reset : -1) << ">(A);\n}\n";
+          << ", rfk::GenEval, " << (splat >= 0 ? splat : -1) << ", " << (reset >= 0 ? reset : -1) << ", "
+          << (pipe ? 1 : 0) << ">(A);\n}\n";
     return o.str();
 }
 
@@ -195,11 +197,11 @@ int spec_compile(const std::string& src, std::vector<char>& cubin) {
 }
 
 int spec_kernel(const std::vector<uint32_t>& prog, int threads, int slots, int device, const void** out,
-                SpecKind kind, int splat, int reset) {
+                SpecKind kind, int splat, int reset, int pipe) {
     *out = nullptr;
     if (prog.size() < (size_t)H_XOFF || prog[H_MAGIC] != kProgMagic)
         return fail(RF_ERR_INVALID_ARG, "spec_kernel: not a compiled genome");
-    const std::string src = spec_source(prog, threads, slots / threads, kind, splat, reset);
+    const std::string src = spec_source(prog, threads, slots / threads, kind, splat, reset, pipe);
     const std::string key = std::to_string(device) + "\n" + src;
     {
         std::lock_guard<std::mutex> lk(g_mu);

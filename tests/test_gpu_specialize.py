@@ -10,8 +10,9 @@ from test_gpu_parity import LINEAR, _bins, _l1
 pytestmark = pytest.mark.gpu
 
 
-def _run(rk, f, N, W, H, F, D, seed, specialize, trace=0, **kw):
+def _run(rk, f, N, W, H, F, D, seed, specialize, trace=0, pipe=True, **kw):
     sim = rk.Sim(N, seed=seed, specialize=specialize, **kw)
+    sim.set_pipelined_exchange(pipe)
     if trace:
         sim.enable_xid_trace(trace)
     sim.warmup(f, F - 1)
@@ -25,17 +26,39 @@ def _run(rk, f, N, W, H, F, D, seed, specialize, trace=0, **kw):
     return out
 
 
-@pytest.mark.parametrize("cta,threads", [(4096, 1024), (2048, 512), (1024, 1024)])
+@pytest.mark.parametrize("cta,threads", [(4096, 1024), (2048, 512), (2048, 1024), (1024, 1024)])
 def test_affine_genome_bit_exact(rk, orc, compiler, cta, threads):
+    """Specialised kernel with the pipelined walker exchange, specialised kernel with a barrier per
+    pass, interpreted kernel: the same counts as the FP32 oracle on the Sim's shuffle table (built
+    for threads / slots phases per pass), for every CTA shape."""
     f = rk.Flame.from_xml(LINEAR, compiler)
     N, F, D = 8192, 20, 40
-    a = _run(rk, f, N, 256, 256, F, D, 3, 1, cta_slots=cta, cta_threads=threads, steps_per_launch=32)
-    b = _run(rk, f, N, 256, 256, F, D, 3, -1, cta_slots=cta, cta_threads=threads, steps_per_launch=32)
-    assert np.array_equal(a["hits"], b["hits"])
-    assert np.allclose(a["rgba"], b["rgba"], rtol=1e-4, atol=1e-3)
+    kw = dict(cta_slots=cta, cta_threads=threads, steps_per_launch=32)
+    a = _run(rk, f, N, 256, 256, F, D, 3, 1, **kw)
+    p = _run(rk, f, N, 256, 256, F, D, 3, 1, pipe=False, **kw)
+    b = _run(rk, f, N, 256, 256, F, D, 3, -1, **kw)
     r = orc.Genome(LINEAR).chaos(N, 256, 256, fuse=F, draw=D, seed=3, fp64=False, shuffle_mode=1, cta_slots=cta,
-                                 steps_per_launch=32, table_size=1024)
-    assert np.array_equal(a["hits"], r["hits"])
+                                 cta_threads=threads, steps_per_launch=32, table_size=1024)
+    for o in (a, p, b):
+        assert np.array_equal(o["hits"], r["hits"])
+        assert np.allclose(o["rgba"], a["rgba"], rtol=1e-4, atol=1e-3)
+
+
+@pytest.mark.parametrize("L", [1, 2, 7, 256])
+def test_pipelined_exchange_equals_barrier_exchange(rk, compiler, L):
+    """On a nonlinear genome with the walker reset and a final xform, the pipelined exchange draws
+    the same xform-id streams and the same counts as the barrier form, for launches of any length
+    (the first pass of each launch is the gather, the last one draws no next xform)."""
+    W = H = 128
+    f = rk.Flame.synthesize(compiler, 1, 9, W, H, n_xforms=8, final_xform=True, force_parametric=True)
+    out = []
+    for pipe in (True, False):
+        o = _run(rk, f, 8192, W, H, 20, 24, 7, 1, trace=44, pipe=pipe, steps_per_launch=L)
+        out.append(o)
+    assert np.array_equal(out[0]["trace"], out[1]["trace"])
+    assert out[0]["counters"] == out[1]["counters"]
+    assert np.array_equal(out[0]["hits"], out[1]["hits"])
+    assert np.allclose(out[0]["rgba"], out[1]["rgba"], rtol=1e-4, atol=1e-3)
 
 
 @pytest.mark.parametrize("kind,seed,nx", [(1, 1, 8), (1, 9, 12), (0, 0, 0), (2, 4, 0), (3, 5, 0)])

@@ -339,7 +339,7 @@ def test_specialised_kernel_source_and_compile(rk, compiler):
     lay = f.param_layout()
     nvar = sum(len(x["variations"]) for x in lay["xforms"]) + len(lay["final_xform"]["variations"])
     assert src.count("vary_impl(") == nvar  # one inlined call per (xform, variation)
-    assert "case -1:" in src and "chaos_body<1024, 4, rfk::GenEval, -1, -1>" in src
+    assert "case -1:" in src and "chaos_body<1024, 4, rfk::GenEval, -1, -1, 0>" in src
     assert f.kernel_source(1024, 4096) == src  # deterministic: the cache key
     g = rk.Flame.synthesize(compiler, rk.SYNTH_SMALL, 0, 256, 256)
     assert g.kernel_source(512, 2048).count("case ") == 2  # 3 xforms: cases 0, 1 and default
