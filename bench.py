@@ -667,7 +667,7 @@ def run_batch(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic genomes (seeds 2, 3, 100-163); no dataset",
         "config": workload_config(reset),
         "launch": {"images": n_img, "points_per_batch": st["points"], "requested_points": points,
-                   "autotuned": info, "parallelism": "replicas" if ws > 1 else "single"},
+                   "autotuned": info, "exchange": "barrier", "parallelism": "replicas" if ws > 1 else "single"},
         "frames_per_s": n_img / (ms_step * 1e-3),
         "binned_fraction": st["binned"] / st["points"],
         "binned_gpoints_s": value * st["binned"] / st["points"],
