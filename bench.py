@@ -411,10 +411,8 @@ def run_native(args):
     sim.set_splat({"auto": R.SPLAT_AUTO, "global": R.SPLAT_GLOBAL, "warp": R.SPLAT_WARP,
                    "tile": R.SPLAT_TILE}[args.splat])
     sim.set_bad_value_reset(reset)
-    sim.set_pipelined_exchange(args.exchange == "pipelined")
-    threads = args.cta_threads or min(cta, 1024)
-    exchange = "pipelined" if args.exchange == "pipelined" and args.splat != "tile" and cta // threads >= 3 \
-        else "barrier"
+    sim.set_exchange({"auto": R.EXCHANGE_AUTO, "pipelined": R.EXCHANGE_PIPELINED,
+                      "barrier": R.EXCHANGE_BARRIER}[args.exchange])
     tile = None
     if args.splat == "tile":  # the shared-memory tile: the attractor's bounding box from a short probe
         sim.warmup(flame, FUSE - 1)
@@ -518,6 +516,7 @@ def run_native(args):
     pts_per_launch = walkers * args.steps_per_launch
     pts_s = pts_per_launch / (per_launch_ms * 1e-3)
     prof_key = {"frame1080": "1080p"}.get(args.workload, args.workload)
+    exchange = "pipelined" if sim.exchange() == R.EXCHANGE_PIPELINED else "barrier"
     build = kernel_build_id(flame, "%s/%d/%s" % (args.splat, int(reset), exchange)) if sim.specialized() else None
     same_build = build is not None and build == _profile_build(prof_key)
     inst = _profile_figure(prof_key, "warp instructions per point") if same_build else None
@@ -552,7 +551,7 @@ def run_native(args):
         "config": workload_config(reset),
         "launch": {"walkers": walkers, "cta_slots": cta, "steps_per_launch": args.steps_per_launch,
                    "passes_per_frame": passes, "splat": args.splat, "splat_tile": tile,
-                   "exchange": exchange if sim.specialized() else "barrier",
+                   "exchange": exchange, "exchange_mode": args.exchange,
                    "specialized_kernel": sim.specialized(),
                    "kernel_build": build, "first_warmup_s": first_warmup_s,
                    "parallelism": "replicas" if ws > 1 else "single"},
@@ -942,9 +941,9 @@ def main():
     ap.add_argument("--splat", default=None, choices=["auto", "global", "warp", "tile"],
                     help="splat strategy (default: the workload's, else auto); tile: a shared-memory histogram "
                          "tile over the attractor's bounding box")
-    ap.add_argument("--exchange", default="pipelined", choices=["pipelined", "barrier"],
-                    help="walker exchange of the specialised chaos kernel: mbarrier-pipelined (default) or one "
-                         "CTA barrier per pass")
+    ap.add_argument("--exchange", default="auto", choices=["auto", "pipelined", "barrier"],
+                    help="walker exchange of the specialised chaos kernel: the faster of the two timed on the first "
+                         "drawing launches (default), mbarrier-pipelined, or one CTA barrier per pass")
     ap.add_argument("--specialize", default="auto", choices=["auto", "on", "off"],
                     help="genome-specialised chaos kernel compiled at run time")
     ap.add_argument("--learned-train", type=int, default=2000)

@@ -247,16 +247,23 @@ RF_API int  rf_set_splat_tile(rf_sim* s, uint32_t x0, uint32_t y0, uint32_t w, u
    passes a genome with singular variations (spherical, julian ...) binns fewer and fewer points.
    Takes effect from the next rf_warmup / rf_draw_to_bins launch. */
 RF_API int  rf_set_bad_value_reset(rf_sim* s, int on);
-/* The walker exchange of the genome-specialised chaos kernel.  1 (default): pipelined — a Sim with
-   four slots per thread builds its shuffle table so that the first phase of a pass takes
-   its walkers only from the previous pass's earlier phases, and a thread starts the next pass as
-   soon as every thread has finished those (CTA-wide mbarriers instead of a barrier per pass; the
-   walkers triple-buffered in shared memory).  Not with the tile splat, nor for a genome program
-   too large for the third buffer: those launches, and 0, take one CTA barrier per pass.  Both
-   forms give identical results for the same table.  A wait that runs out (bounded) makes the next
-   synchronising call (rf_draw_to_bins with `drawn`, rf_sim_counters, rf_render) return
-   RF_ERR_TIMEOUT.  Takes effect from the next launch. */
-RF_API int  rf_set_pipelined_exchange(rf_sim* s, int on);
+/* The walker exchange of the genome-specialised chaos kernel.  A Sim with four slots per thread
+   builds its shuffle table so that a pass's first phase takes no walker of the previous pass's
+   last phase and its last phase none of the first (the histogram noise is that of uniform
+   permutations).  RF_EXCHANGE_BARRIER: one CTA barrier per pass.  RF_EXCHANGE_PIPELINED: two
+   CTA-wide mbarriers instead — a warp starts the next pass as soon as every warp has finished
+   three phases of this one, so the slowest warps' last phase overlaps the next pass (faster on
+   genomes of unequal, costly xforms; slower on cheap ones with contended splats).
+   RF_EXCHANGE_AUTO (default): after a warmup of a new genome structure (or a change of splat,
+   tile or walker reset) the first two full drawing launches run one form each, timed with CUDA
+   events, and the faster runs from then on (decided without a host wait, once the second launch
+   has finished; not during stream capture, where the pipelined form runs).  All forms give
+   identical results.  A pipelined wait that runs out (bounded) makes the next synchronising call
+   (rf_draw_to_bins with `drawn`, rf_sim_counters, rf_render) return RF_ERR_TIMEOUT. */
+enum rf_exchange { RF_EXCHANGE_BARRIER = 0, RF_EXCHANGE_PIPELINED = 1, RF_EXCHANGE_AUTO = 2 };
+RF_API int  rf_set_exchange(rf_sim* s, int mode);
+/* The form the Sim's next full drawing launch runs: 0 barrier, 1 pipelined (-1: null sim). */
+RF_API int  rf_sim_exchange(const rf_sim* s);
 /* [0] points binned and [1] points emitted (opacity > 0) by the last rf_draw_to_bins call,
    [2] walker-steps since rf_warmup. */
 RF_API int  rf_sim_counters(rf_sim* s, uint64_t out[3]);

@@ -817,26 +817,36 @@ inline uint32_t palette_index(double c) {  // flame.glsl:84: min(255, uint(ceil(
 // ---------------------------------------------------------------------------------------------
 // Chaos game — flame.glsl:41-90, flame.cpp:228-330
 // ---------------------------------------------------------------------------------------------
-// Permutation k of the CUDA kernel's shuffle table over a CTA's n slots.  phases = S > 1: the
-// pipelined table — destinations [0, P), P = n/S (the first phase of a pass), take sources from
-// [0, M), M = n - P (the previous pass's first S-1 phases), in one keyed order; the other
-// destinations take the remaining M sources (the rest of that order, then [M, n)) in a second.
+// Permutation k of the CUDA kernel's shuffle table over a CTA's n slots (kernels.cu
+// shuffle_table_kernel).  phases = S >= 3: the pipelined table, P = n/S slots per phase — the
+// last phase's destinations [n-P, n) take the first P of a keyed order of [P, n) (never the
+// previous pass's first phase), the first phase's destinations [0, P) the first P not yet taken of
+// a keyed order of [0, n-P) (never its last phase), the middle destinations the rest in a keyed
+// order of [0, n).
 void shuffle_table(uint64_t seed, uint32_t k, uint32_t n, uint32_t phases, uint32_t* out) {
-    const uint32_t P = phases > 1 ? n / phases : 0;
+    const uint32_t P = phases >= 3 ? n / phases : 0;
     if (!P) {
         const uint64_t key = derive_key(seed, k, 0, TAG_TABLE);
         for (uint32_t j = 0; j < n; j++) out[j] = feistel(j, n, key);
         return;
     }
-    const uint32_t M = n - P;
-    const uint64_t k1 = derive_key(seed, k, 1, TAG_TABLE), k2 = derive_key(seed, k, 2, TAG_TABLE);
-    for (uint32_t d = 0; d < n; d++) {
-        if (d < P) {
-            out[d] = feistel(d, M, k1);
-        } else {
-            const uint32_t r = feistel(d - P, M, k2);
-            out[d] = r < M - P ? feistel(P + r, M, k1) : M + (r - (M - P));
-        }
+    std::vector<char> taken(n, 0);
+    const uint64_t k3 = derive_key(seed, k, 3, TAG_TABLE), k1 = derive_key(seed, k, 1, TAG_TABLE),
+                   k2 = derive_key(seed, k, 2, TAG_TABLE);
+    for (uint32_t d = 0; d < P; d++) {
+        const uint32_t src = P + feistel(d, n - P, k3);
+        out[n - P + d] = src;
+        taken[src] = 1;
+    }
+    uint32_t d = 0;
+    for (uint32_t i = 0; i < n - P && d < P; i++) {
+        const uint32_t src = feistel(i, n - P, k1);
+        if (!taken[src]) { out[d++] = src; taken[src] = 1; }
+    }
+    d = P;
+    for (uint32_t i = 0; i < n && d < n - P; i++) {
+        const uint32_t src = feistel(i, n, k2);
+        if (!taken[src]) { out[d++] = src; taken[src] = 1; }
     }
 }
 

@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "librefrakt_gb300.so")
 
 SYNTH_SMALL, SYNTH_RANDOM, SYNTH_CONTRACT, SYNTH_SPACEFILL = 0, 1, 2, 3
 SPLAT_AUTO, SPLAT_GLOBAL, SPLAT_WARP, SPLAT_TILE = 0, 1, 2, 3
+EXCHANGE_BARRIER, EXCHANGE_PIPELINED, EXCHANGE_AUTO = 0, 1, 2
 BINS_AUTO, BINS_DIRECT, BINS_INTERLEAVED = 0, 1, 2
 FILTER_GAUSSIAN, FILTER_BOX, FILTER_TRIANGLE, FILTER_HERMITE = 0, 1, 2, 3
 
@@ -148,7 +149,8 @@ _SIGS = {
                          ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "rf_set_splat": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rf_set_bad_value_reset": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
-    "rf_set_pipelined_exchange": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rf_set_exchange": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rf_sim_exchange": ([ctypes.c_void_p], ctypes.c_int),
     "rf_set_splat_tile": ([ctypes.c_void_p] + [ctypes.c_uint32] * 4, ctypes.c_int),
     "rf_set_bin_layout": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rf_sim_counters": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
@@ -504,10 +506,15 @@ class Sim:
         step commented out at shaders/flame.glsl:68, so the default is off)."""
         _check(library().rf_set_bad_value_reset(self._h, int(bool(on))))
 
-    def set_pipelined_exchange(self, on):
-        """Pipelined walker exchange of the specialised chaos kernel (rf_set_pipelined_exchange;
-        default on): the same results as one CTA barrier per pass, with less waiting."""
-        _check(library().rf_set_pipelined_exchange(self._h, int(bool(on))))
+    def set_exchange(self, mode):
+        """Walker exchange of the specialised chaos kernel (rf_set_exchange): EXCHANGE_BARRIER,
+        EXCHANGE_PIPELINED or EXCHANGE_AUTO (default: the faster of the two, timed on the first
+        two full drawing launches); every form gives the same results."""
+        _check(library().rf_set_exchange(self._h, int(mode)))
+
+    def exchange(self):
+        """The form the next full drawing launch runs: EXCHANGE_BARRIER or EXCHANGE_PIPELINED."""
+        return library().rf_sim_exchange(self._h)
 
     def set_bin_layout(self, layout):
         """BINS_AUTO, BINS_DIRECT or BINS_INTERLEAVED (rf_set_bin_layout)."""

@@ -72,12 +72,44 @@ size_t copy_out(const std::string& s, char* buf, size_t cap) {
 }
 
 // The pipelined walker exchange (chaos_body.cuh, PIPE) runs in the specialised kernels when the
-// Sim's shuffle table was built for it (4 slots per thread), the splat is not the tile
-// splat (whose shared-memory histogram needs the room of the third walker buffer) and the
-// genome program fits beside the triple-buffered walkers.
-bool use_pipe(const rf_sim* s, int splat) {
-    return s->pipe && s->table_phases >= 3 && splat != 3 &&
-           chaos_smem(s->slots, s->prog_words, s->L, 0, 1) <= kMaxCtaSmem;
+// Sim's shuffle table was built for it (4 slots per thread) and its two mbarriers fit in shared
+// memory beside the tile splat's bins.
+bool use_pipe(const rf_sim* s, uint32_t tile_bins) {
+    return s->table_phases >= 3 && chaos_smem(s->slots, s->prog_words, s->L, tile_bins, 1) <= kMaxCtaSmem;
+}
+
+// RF_EXCHANGE_AUTO starts over (a new genome structure, splat, tile or reset changes the kernels)
+void reset_exchange_tuning(rf_sim* s) {
+    s->tune_step = 0;
+    s->tune_pipe = 1;
+}
+
+// The exchange form of the next launch (1 pipelined); *measure = 0 / 1 when RF_EXCHANGE_AUTO times
+// this launch as the barrier / pipelined form, else -1.
+int exchange_for_launch(rf_sim* s, bool full_draw, int* measure) {
+    *measure = -1;
+    if (s->exchange != RF_EXCHANGE_AUTO) return s->exchange == RF_EXCHANGE_PIPELINED ? 1 : 0;
+    if (s->tune_step == 2) {  // both forms timed: decide once the second launch has finished
+        const cudaError_t q = cudaEventQuery(s->tune_ev[3]);
+        if (q == cudaSuccess) {
+            float tb = 0.0f, tp = 0.0f;
+            if (cudaEventElapsedTime(&tb, s->tune_ev[0], s->tune_ev[1]) == cudaSuccess &&
+                cudaEventElapsedTime(&tp, s->tune_ev[2], s->tune_ev[3]) == cudaSuccess)
+                s->tune_pipe = tp <= tb ? 1 : 0;
+            s->tune_step = 3;
+        } else if (q == cudaErrorNotReady) {
+            cudaGetLastError();  // not sticky; clear it
+        } else {
+            s->tune_step = 3;  // the events failed: keep the default
+        }
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (s->tune_step < 2 && full_draw && s->tune_ev[0] && cudaStreamIsCapturing(s->stream, &cs) == cudaSuccess &&
+        cs == cudaStreamCaptureStatusNone) {
+        *measure = s->tune_step;
+        return s->tune_step;
+    }
+    return s->tune_pipe;
 }
 
 // RF_ERR_TIMEOUT when a pipelined exchange wait in an earlier launch ran out (counters[3]); call
@@ -131,7 +163,10 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.trace_passes = s->trace_passes;
         a.n_groups = (uint32_t)(s->N / kGroup);
         const uint32_t grid = (uint32_t)(s->N / s->slots);
-        const int pipe = s->spec && use_pipe(s, a.splat) ? 1 : 0;
+        const uint32_t tile_bins = a.splat == 3 && a.draw ? a.tile_w * a.tile_h : 0u;
+        int measure = -1;
+        const int want = s->spec ? exchange_for_launch(s, a.draw && steps == s->L, &measure) : 0;
+        const int pipe = want && s->spec && use_pipe(s, tile_bins) ? 1 : 0;
         if (s->spec && (s->spec_splat != a.splat || s->spec_reset != a.reset || s->spec_pipe != pipe)) {
             // the splat strategy, the reset or the exchange changed since warmup: the kernel compiled for them
             const void* k = nullptr;
@@ -143,15 +178,17 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
             s->spec_reset = a.reset;
             s->spec_pipe = pipe;
         }
-        const uint32_t tile_bins = a.splat == 3 && a.draw ? a.tile_w * a.tile_h : 0u;
         if (chaos_smem(s->slots, a.prog_words, a.steps, tile_bins) > kMaxCtaSmem)
             return fail(RF_ERR_CAPACITY, "splat tile of " + std::to_string(tile_bins) +
                                          " bins exceeds the shared memory beside " + std::to_string(s->slots) +
                                          " walker slots");
+        if (measure >= 0 && cudaEventRecord(s->tune_ev[2 * measure], s->stream) != cudaSuccess) measure = -1;
         cudaError_t e = s->spec ? launch_spec(s->spec, (int)s->threads, (int)s->slots, a, grid,
                                               chaos_smem(s->slots, a.prog_words, a.steps, tile_bins, pipe), s->stream)
                                 : launch_chaos((int)s->threads, (int)s->slots, a, grid, s->stream);
         if (e != cudaSuccess) return cuda_fail(e, "chaos kernel launch");
+        if (measure >= 0 && cudaEventRecord(s->tune_ev[2 * measure + 1], s->stream) == cudaSuccess)
+            s->tune_step = measure + 1;
         s->cur ^= 1;
         s->pass += steps;
         done += steps;
@@ -497,13 +534,14 @@ int rf_sim_create(const rf_sim_desc* d, rf_sim** out) {
     ALLOC(s->counters, 8 * sizeof(unsigned long long));
 #undef ALLOC
     if ((e = launch_init_rng(s->rng, s->N, d->seed, s->stream)) != cudaSuccess) return cleanup(cuda_fail(e, "rng init"));
-    // the pipelined exchange's permutations, for 4 slots per thread (with 2 the first phase would
-    // take exactly the first phase's walkers and the domain would split in two)
+    // the pipelined exchange's permutations, for 4 slots per thread
     s->table_phases = slots / threads >= 3 ? slots / threads : 0;
     if ((e = launch_shuffle_table(s->table, slots, s->table_size, d->seed, s->stream, s->table_phases)) != cudaSuccess)
         return cleanup(cuda_fail(e, "shuffle table"));
     if ((e = cudaMemsetAsync(s->counters, 0, 8 * sizeof(unsigned long long), s->stream)) != cudaSuccess)
         return cleanup(cuda_fail(e, "memset"));
+    for (auto& ev : s->tune_ev)
+        if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cleanup(cuda_fail(e, "event"));
     if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cleanup(cuda_fail(e, "sim init"));
     *out = s;
     return RF_OK;
@@ -517,6 +555,8 @@ int rf_sim_destroy(rf_sim* s) {
                     s->trace, s->r_bins, s->r_hits, s->r_de, s->r_img, s->r_stats, s->r_rad, s->r_dw};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    for (auto ev : s->tune_ev)
+        if (ev) cudaEventDestroy(ev);
     delete s;
     return RF_OK;
 }
@@ -562,9 +602,10 @@ int rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_width) {
     if (int rc = genome_validate(f->g, *f->reg)) return rc;
     s->prog_words = (uint32_t)prog.size();
     s->spec = nullptr;
+    if (prog != s->spec_prog) reset_exchange_tuning(s);
     if (s->d.specialize >= 0) {
         const void* k = nullptr;
-        const int pipe = use_pipe(s, splat_code(s->splat)) ? 1 : 0;
+        const int pipe = s->exchange != RF_EXCHANGE_BARRIER && use_pipe(s, 0) ? 1 : 0;
         const int rc = spec_kernel(prog, (int)s->threads, (int)s->slots, s->device, &k, SpecKind::Chaos,
                                    splat_code(s->splat), s->reset, pipe);
         if (rc == RF_OK) {
@@ -627,6 +668,7 @@ int rf_set_bin_layout(rf_sim* s, int layout) {
 
 int rf_set_splat(rf_sim* s, int splat) {
     if (!s) return fail(RF_ERR_INVALID_ARG, "rf_set_splat: null sim");
+    if (splat != s->splat) reset_exchange_tuning(s);
     s->splat = splat;
     return RF_OK;
 }
@@ -634,6 +676,7 @@ int rf_set_splat(rf_sim* s, int splat) {
 int rf_set_splat_tile(rf_sim* s, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h) {
     if (!s) return fail(RF_ERR_INVALID_ARG, "rf_set_splat_tile: null sim");
     if ((uint64_t)w * h > 65536) return fail(RF_ERR_CAPACITY, "rf_set_splat_tile: more than 65,536 bins");
+    reset_exchange_tuning(s);
     s->tile[0] = x0;
     s->tile[1] = y0;
     s->tile[2] = w;
@@ -643,14 +686,25 @@ int rf_set_splat_tile(rf_sim* s, uint32_t x0, uint32_t y0, uint32_t w, uint32_t 
 
 int rf_set_bad_value_reset(rf_sim* s, int on) {
     if (!s || (on != 0 && on != 1)) return fail(RF_ERR_INVALID_ARG, "rf_set_bad_value_reset: null sim or flag not 0/1");
+    if (on != s->reset) reset_exchange_tuning(s);
     s->reset = on;
     return RF_OK;
 }
 
-int rf_set_pipelined_exchange(rf_sim* s, int on) {
-    if (!s || (on != 0 && on != 1)) return fail(RF_ERR_INVALID_ARG, "rf_set_pipelined_exchange: null sim or flag not 0/1");
-    s->pipe = on;
+int rf_set_exchange(rf_sim* s, int mode) {
+    if (!s || mode < RF_EXCHANGE_BARRIER || mode > RF_EXCHANGE_AUTO)
+        return fail(RF_ERR_INVALID_ARG, "rf_set_exchange: null sim or unknown mode");
+    s->exchange = mode;
+    reset_exchange_tuning(s);
     return RF_OK;
+}
+
+int rf_sim_exchange(const rf_sim* s) {
+    if (!s) return -1;
+    const uint32_t tile_bins = s->splat == RF_SPLAT_TILE ? s->tile[2] * s->tile[3] : 0u;
+    if (!s->spec || !use_pipe(s, tile_bins)) return 0;
+    if (s->exchange != RF_EXCHANGE_AUTO) return s->exchange == RF_EXCHANGE_PIPELINED ? 1 : 0;
+    return s->tune_pipe;
 }
 
 int rf_draw_to_bins(rf_sim* s, rf_flame* f, float* bins_rgba, uint32_t* bins_hits, uint32_t W, uint32_t H,

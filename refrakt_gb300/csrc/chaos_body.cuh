@@ -48,16 +48,15 @@ __device__ __forceinline__ int draw_phase(int tid) {
 }
 
 // Shared memory of a chaos CTA (dynamic, in this order):
-//   program words (prog_words), palette float4[256], walker exchange (float4 [2][SLOTS]; with
-//   the pipelined exchange float [3][3][SLOTS]: three buffers of x, y and colour planes),
+//   program words (prog_words), palette float4[256], walker exchange float4 [2][SLOTS],
 //   JSF32 states uint4[SLOTS], group xform ids int[2][SLOTS/256], per-pass permutation ids
-//   uint32[steps], (pipelined exchange, 8-byte aligned) two mbarriers; with the tile splat
+//   uint32[steps], (8-byte aligned) the pipelined exchange's two mbarriers; with the tile splat
 //   (16-byte aligned) the tile's float4 RGBA sums and uint32 counts
 __host__ __device__ inline size_t chaos_smem_bytes(int slots, uint32_t prog_words, uint32_t steps,
                                                    uint32_t tile_bins = 0, int pipe = 0) {
     size_t b = ((size_t)prog_words * 4 + 15) & ~(size_t)15;
     b += 256 * 16;
-    b += pipe ? (size_t)9 * slots * 4 : (size_t)2 * slots * 16;
+    b += (size_t)2 * slots * 16;
     b += (size_t)slots * 16;
     b += (size_t)2 * (slots / kGroup) * 4;
     b += (size_t)steps * 4;
@@ -101,37 +100,35 @@ __device__ __forceinline__ bool xbar_wait(uint64_t* b, uint32_t parity) {
 // so the hot loop carries only that one; -1 dispatches on A.splat.  RESET >= 0 likewise fixes
 // the walker reset of flame.glsl:68 (reset_bad_walker); -1 reads A.reset.
 //
-// PIPE = 1 (SPT >= 3, no tile splat) replaces the pass barrier by the pipelined exchange: the
-// shuffle table's permutations send the first phase's slots only walkers of the previous pass's
-// first SPT-1 phases (shuffle_table_kernel, `phases`), so a thread starts the next pass as soon
-// as every thread has finished those phases (mbarrier 0) and waits for the whole previous pass
-// (mbarrier 1) only before its second phase — the slowest warps' last phase overlaps the others'
-// next pass.  The walkers are triple-buffered (a thread may write pass s + 1's walkers while
-// another still reads pass s's sources), as x, y and colour planes to fit shared memory, and a
-// group's xform for pass s + 1 is drawn right after its first slot's pass-s evaluation (the same
-// point of that slot's RNG stream).
+// PIPE = 1 (SPT >= 3) replaces the pass barrier by the pipelined exchange.  The shuffle table's
+// permutations (shuffle_table_pipe_kernel) send the first phase's slots no walker of the previous
+// pass's last phase and the last phase's slots no walker of its first phase.  So a warp starts the
+// next pass as soon as every warp has finished the first SPT-1 phases of this one (mbarrier 0:
+// the first phase's sources are written, and the first phase's slots — which it overwrites — are
+// no longer read), and waits for the whole previous pass (mbarrier 1) only before its second
+// phase: the slowest warps' last phase overlaps the others' next pass, with the walkers still
+// double-buffered.  A group's xform for pass s + 1 is drawn right after its first slot's pass-s
+// evaluation (the same point of that slot's RNG stream) into the other xform-id buffer.
 template <int THREADS, int SPT, class Eval, int SPLAT = -1, int RESET = -1, int PIPE = 0>
 __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
-    static_assert(!PIPE || (SPT >= 3 && SPLAT != 3), "the pipelined exchange needs three phases and no tile splat");
+    static_assert(!PIPE || SPT >= 3, "the pipelined exchange needs three phases");
     constexpr uint32_t SLOTS = (uint32_t)THREADS * SPT;
     constexpr int G = SLOTS / kGroup;
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t* s_prog = reinterpret_cast<uint32_t*>(smem);
     float4* s_pal = reinterpret_cast<float4*>(smem + (((size_t)A.prog_words * 4 + 15) & ~(size_t)15));
-    float4* s_w = s_pal + 256;                          // PIPE = 0: float4 [2][SLOTS]
-    float* s_wf = reinterpret_cast<float*>(s_pal + 256);  // PIPE = 1: float [3 buffers][x, y, c][SLOTS]
-    uint4* s_rng = reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(s_pal + 256) +
-                                            (PIPE ? (size_t)9 * SLOTS * 4 : (size_t)2 * SLOTS * 16));
+    float4* s_w = s_pal + 256;
+    uint4* s_rng = reinterpret_cast<uint4*>(s_w + 2 * SLOTS);
     int* s_xid = reinterpret_cast<int*>(s_rng + SLOTS);
     uint32_t* s_perm = reinterpret_cast<uint32_t*>(s_xid + 2 * G);
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(((unsigned long long)(s_perm + A.steps) + 7) & ~7ull);
     // the tile splat's shared-memory histogram (splat 3)
     const bool tiled = SPLAT == 3 || (SPLAT < 0 && A.splat == 3);
-    const uint32_t tile_bins = !PIPE && tiled && A.draw ? A.tile_w * A.tile_h : 0u;
+    const uint32_t tile_bins = tiled && A.draw ? A.tile_w * A.tile_h : 0u;
     TileTarget tt{nullptr, nullptr};
     if (tile_bins) {
         tt.rgba = reinterpret_cast<float4*>(
-            smem + ((chaos_smem_bytes(SLOTS, A.prog_words, A.steps) + 15) & ~(size_t)15));
+            smem + ((chaos_smem_bytes(SLOTS, A.prog_words, A.steps, 0, PIPE) + 15) & ~(size_t)15));
         tt.count = reinterpret_cast<uint32_t*>(tt.rgba + tile_bins);
     }
 
@@ -171,13 +168,7 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
         } else {
             w = A.walk_in[ts_base + src];
         }
-        if (PIPE) {
-            s_wf[ls] = w.x;
-            s_wf[SLOTS + ls] = w.y;
-            s_wf[2 * SLOTS + ls] = w.z;
-        } else {
-            s_w[ls] = w;
-        }
+        s_w[ls] = w;
     }
 
     const uint32_t foff = s_prog[H_FINAL];
@@ -202,14 +193,12 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
         s_rng[ls] = make_uint4(rng.a, rng.b, rng.c, rng.d);
     }
     __syncthreads();
-    int rd = 0;  // PIPE: the walker buffer this pass reads (pass s reads s % 3, writes (s + 1) % 3)
     // PIPE: false after a wait ran out — the thread counts it (the host reports RF_ERR_TIMEOUT)
     // and waits no more, so the launch still ends
     bool synced = true;
 
     for (uint32_t s = 0; s < A.steps; s++) {
         const int buf = s & 1;
-        const int wr = rd == 2 ? 0 : rd + 1;
         // this pass's sources in the exchange buffer (identity on the gather pass)
         uint32_t src[SPT];
 #pragma unroll
@@ -238,18 +227,8 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
                 synced = false;
                 atomicAdd(A.counters + 3, 1ull);
             }
-            float x, y, c;
-            if (PIPE) {
-                const float* b = s_wf + (size_t)rd * 3 * SLOTS;
-                x = b[j];
-                y = b[SLOTS + j];
-                c = b[2 * SLOTS + j];
-            } else {
-                const float4 v = s_w[buf * SLOTS + j];
-                x = v.x;
-                y = v.y;
-                c = v.z;
-            }
+            const float4 v = s_w[buf * SLOTS + j];
+            float x = v.x, y = v.y, c = v.z;
             const uint4 r4 = s_rng[ls];
             Jsf rng{r4.x, r4.y, r4.z, r4.w};
             const int xi = s_xid[buf * G + ls / kGroup];
@@ -278,17 +257,10 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
                 if (it == 1 || !has_final) break;
                 fr = false;
             }
-            if (PIPE) {
-                float* b = s_wf + (size_t)wr * 3 * SLOTS;
-                b[ls] = x;
-                b[SLOTS + ls] = y;
-                b[2 * SLOTS + ls] = c;
-                // the group's xform for the next pass, at the point of the slot's stream where
-                // the pass-barrier form draws it
-                if (k == dphase && s + 1 < A.steps) draw_group_xform(s + 1, ls, rng);
-            } else {
-                s_w[(buf ^ 1) * SLOTS + ls] = make_float4(x, y, c, 0.0f);
-            }
+            s_w[(buf ^ 1) * SLOTS + ls] = make_float4(x, y, c, 0.0f);
+            // the group's xform for the next pass, at the point of the slot's stream where the
+            // pass-barrier form draws it
+            if (PIPE && k == dphase && s + 1 < A.steps) draw_group_xform(s + 1, ls, rng);
             s_rng[ls] = make_uint4(rng.a, rng.b, rng.c, rng.d);
             if (PIPE && k >= SPT - 2) xbar_arrive(s_bar + (k - (SPT - 2)));
             if (A.draw) {
@@ -324,7 +296,6 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
                 }
             }
         }
-        rd = wr;
     }
     // the tile's non-empty bins into the histogram, once per launch
     if (tile_bins) {
@@ -343,12 +314,7 @@ __device__ __forceinline__ void chaos_body(const ChaosArgs& A) {
     const int out_buf = A.steps & 1;
     for (int k = 0; k < SPT; k++) {
         const uint32_t ls = phase_slot<THREADS>(k, tid);
-        if (PIPE) {
-            const float* b = s_wf + (size_t)rd * 3 * SLOTS;
-            A.walk_out[ts_base + gid0 + ls] = make_float4(b[ls], b[SLOTS + ls], b[2 * SLOTS + ls], 0.0f);
-        } else {
-            A.walk_out[ts_base + gid0 + ls] = s_w[out_buf * SLOTS + ls];
-        }
+        A.walk_out[ts_base + gid0 + ls] = s_w[out_buf * SLOTS + ls];
         A.rng[ts_base + gid0 + ls] = s_rng[ls];
     }
 

@@ -45,7 +45,12 @@ struct rf_sim {
     int spec_reset = -1;              // the reset setting compiled into the specialised kernel
     int spec_pipe = 0;                // 1: the specialised kernel has the pipelined walker exchange
     uint32_t table_phases = 0;        // phases per pass the shuffle table is pipelined for (0: uniform)
-    int pipe = 1;                     // pipelined exchange allowed (rf_set_pipelined_exchange)
+    int exchange = RF_EXCHANGE_AUTO;  // rf_set_exchange
+    // RF_EXCHANGE_AUTO: 0/1 — the next full drawing launch is timed as the barrier / pipelined form;
+    // 2 — both timed, deciding when the second has finished; 3 — decided (tune_pipe)
+    int tune_step = 0;
+    int tune_pipe = 1;                // the form chosen (the pipelined one until decided)
+    cudaEvent_t tune_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<uint32_t> spec_prog;  // the warmed program, to specialise again for another strategy
     int bin_layout = RF_BINS_AUTO;
     uint32_t rgba_shift = 0, count_shift = 0;  // BinTarget addressing of the next launches

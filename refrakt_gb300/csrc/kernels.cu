@@ -46,28 +46,51 @@ __global__ void init_rng_kernel(uint4* rng, uint64_t n, uint64_t seed) {
     rng[i] = make_uint4(s.a, s.b, s.c, s.d);
 }
 
-// the walker-shuffle table: `count` keyed permutations of [0, n).  phases = S > 1 gives the
-// pipelined exchange's permutations (chaos_body.cuh, PIPE): destinations [0, n/S) — the first
-// phase of a pass — take their sources from [0, M), M = n - n/S, the slots of the previous pass's
-// first S-1 phases, in one keyed order; the other destinations take the remaining M sources (the
-// rest of that order, then [M, n)) in a second keyed order.  Every permutation stays a bijection;
-// with S >= 3 every phase's walkers reach every phase (S = 2 would split the domain in two).
-__global__ void shuffle_table_kernel(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed, uint32_t phases) {
+// the walker-shuffle table: `count` keyed permutations of [0, n), one entry per thread
+__global__ void shuffle_table_kernel(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (uint64_t)n * count) return;
     const uint32_t k = (uint32_t)(i / n), j = (uint32_t)(i - (uint64_t)k * n);
-    const uint32_t P = phases > 1 ? n / phases : 0;
-    if (!P) {
-        out[i] = (uint16_t)feistel(j, n, derive_key(seed, k, 0, TAG_TABLE));
-        return;
+    out[i] = (uint16_t)feistel(j, n, derive_key(seed, k, 0, TAG_TABLE));
+}
+
+// The pipelined exchange's table (chaos_body.cuh, PIPE), one permutation per thread: with P = n/S
+// slots per phase, the last phase's destinations [n-P, n) take the first P of a keyed order of
+// [P, n) — never a walker of the previous pass's first phase, whose slots a fast thread may
+// already overwrite — and the first phase's destinations [0, P) the first P not yet taken of a
+// keyed order of [0, n-P) — never a walker of the previous pass's last phase, which a slow thread
+// may still be computing; the middle destinations take the rest in a keyed order of [0, n).
+// n <= kMaxPipeSlots, S >= 3 (then enough sources stay free for the first phase).
+constexpr uint32_t kMaxPipeSlots = 4096;
+__global__ void shuffle_table_pipe_kernel(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed, uint32_t phases) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const uint32_t P = n / phases;
+    uint32_t taken[kMaxPipeSlots / 32];
+    for (uint32_t w = 0; w < kMaxPipeSlots / 32; w++) taken[w] = 0;
+    uint16_t* o = out + (size_t)k * n;
+    const uint64_t k3 = derive_key(seed, k, 3, TAG_TABLE), k1 = derive_key(seed, k, 1, TAG_TABLE),
+                   k2 = derive_key(seed, k, 2, TAG_TABLE);
+    for (uint32_t d = 0; d < P; d++) {
+        const uint32_t src = P + feistel(d, n - P, k3);
+        o[n - P + d] = (uint16_t)src;
+        taken[src >> 5] |= 1u << (src & 31);
     }
-    const uint32_t M = n - P;
-    const uint64_t k1 = derive_key(seed, k, 1, TAG_TABLE);
-    if (j < P) {
-        out[i] = (uint16_t)feistel(j, M, k1);
-    } else {
-        const uint32_t r = feistel(j - P, M, derive_key(seed, k, 2, TAG_TABLE));
-        out[i] = (uint16_t)(r < M - P ? feistel(P + r, M, k1) : M + (r - (M - P)));
+    uint32_t d = 0;
+    for (uint32_t i = 0; i < n - P && d < P; i++) {
+        const uint32_t src = feistel(i, n - P, k1);
+        if (!(taken[src >> 5] >> (src & 31) & 1u)) {
+            o[d++] = (uint16_t)src;
+            taken[src >> 5] |= 1u << (src & 31);
+        }
+    }
+    d = P;
+    for (uint32_t i = 0; i < n && d < n - P; i++) {
+        const uint32_t src = feistel(i, n, k2);
+        if (!(taken[src >> 5] >> (src & 31) & 1u)) {
+            o[d++] = (uint16_t)src;
+            taken[src >> 5] |= 1u << (src & 31);
+        }
     }
 }
 
@@ -161,7 +184,12 @@ cudaError_t launch_shuffle_table(uint16_t* out, uint32_t n, uint32_t count, uint
                                  uint32_t phases) {
     const uint64_t total = (uint64_t)n * count;
     const uint32_t b = 256;
-    shuffle_table_kernel<<<(unsigned)((total + b - 1) / b), b, 0, st>>>(out, n, count, seed, phases);
+    if (phases >= 3) {
+        if (n > kMaxPipeSlots || n % phases) return cudaErrorInvalidValue;
+        shuffle_table_pipe_kernel<<<(count + 63) / 64, 64, 0, st>>>(out, n, count, seed, phases);
+        return cudaGetLastError();
+    }
+    shuffle_table_kernel<<<(unsigned)((total + b - 1) / b), b, 0, st>>>(out, n, count, seed);
     return cudaGetLastError();
 }
 

@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 
 def _run(rk, f, N, W, H, F, D, seed, specialize, trace=0, pipe=True, **kw):
     sim = rk.Sim(N, seed=seed, specialize=specialize, **kw)
-    sim.set_pipelined_exchange(pipe)
+    sim.set_exchange(rk.EXCHANGE_PIPELINED if pipe is True else rk.EXCHANGE_BARRIER if pipe is False else pipe)
     if trace:
         sim.enable_xid_trace(trace)
     sim.warmup(f, F - 1)
@@ -46,19 +46,21 @@ def test_affine_genome_bit_exact(rk, orc, compiler, cta, threads):
 
 @pytest.mark.parametrize("L", [1, 2, 7, 256])
 def test_pipelined_exchange_equals_barrier_exchange(rk, compiler, L):
-    """On a nonlinear genome with the walker reset and a final xform, the pipelined exchange draws
-    the same xform-id streams and the same counts as the barrier form, for launches of any length
-    (the first pass of each launch is the gather, the last one draws no next xform)."""
+    """On a nonlinear genome with the walker reset and a final xform, the pipelined exchange and
+    the automatic choice (which times both forms on its first two full drawing launches) draw the
+    same xform-id streams and the same counts as the barrier form, for launches of any length (the
+    first pass of each launch is the gather, the last one draws no next xform)."""
     W = H = 128
     f = rk.Flame.synthesize(compiler, 1, 9, W, H, n_xforms=8, final_xform=True, force_parametric=True)
     out = []
-    for pipe in (True, False):
+    for pipe in (True, False, rk.EXCHANGE_AUTO):
         o = _run(rk, f, 8192, W, H, 20, 24, 7, 1, trace=44, pipe=pipe, steps_per_launch=L)
         out.append(o)
-    assert np.array_equal(out[0]["trace"], out[1]["trace"])
-    assert out[0]["counters"] == out[1]["counters"]
-    assert np.array_equal(out[0]["hits"], out[1]["hits"])
-    assert np.allclose(out[0]["rgba"], out[1]["rgba"], rtol=1e-4, atol=1e-3)
+    for o in out[1:]:
+        assert np.array_equal(out[0]["trace"], o["trace"])
+        assert out[0]["counters"] == o["counters"]
+        assert np.array_equal(out[0]["hits"], o["hits"])
+        assert np.allclose(out[0]["rgba"], o["rgba"], rtol=1e-4, atol=1e-3)
 
 
 @pytest.mark.parametrize("kind,seed,nx", [(1, 1, 8), (1, 9, 12), (0, 0, 0), (2, 4, 0), (3, 5, 0)])
