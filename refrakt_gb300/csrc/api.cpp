@@ -98,7 +98,7 @@ int exchange_for_launch(rf_sim* s, bool full_draw, int* measure) {
                 s->tune_pipe = tp <= tb ? 1 : 0;
             s->tune_step = 3;
         } else if (q == cudaErrorNotReady) {
-            cudaGetLastError();  // not sticky; clear it
+            if (cudaPeekAtLastError() == cudaErrorNotReady) cudaGetLastError();  // clear only this status
         } else {
             s->tune_step = 3;  // the events failed: keep the default
         }
