@@ -768,7 +768,8 @@ def run_learned(args):
     log = lambda m: print(m, file=sys.stderr, flush=True)
     S = 512
     n_train, n_test = args.learned_train, args.learned_test
-    tr_seeds = list(range(1000, 1000 + n_train))
+    # training seeds 1000-2999, then from 4000 on: never the held-out 3000-3199
+    tr_seeds = list(range(1000, 1000 + min(n_train, 2000))) + list(range(4000, 4000 + max(0, n_train - 2000)))
     te_seeds = list(range(3000, 3000 + n_test))
     t0 = time.perf_counter()
     tr = [LD.genome(R, comp, s, S, S) for s in tr_seeds]
