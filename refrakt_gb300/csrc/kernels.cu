@@ -54,44 +54,55 @@ __global__ void shuffle_table_kernel(uint16_t* out, uint32_t n, uint32_t count, 
     out[i] = (uint16_t)feistel(j, n, derive_key(seed, k, 0, TAG_TABLE));
 }
 
-// The pipelined exchange's table (chaos_body.cuh, PIPE), one permutation per thread: with P = n/S
-// slots per phase, the last phase's destinations [n-P, n) take the first P of a keyed order of
-// [P, n) — never a walker of the previous pass's first phase, whose slots a fast thread may
-// already overwrite — and the first phase's destinations [0, P) the first P not yet taken of a
-// keyed order of [0, n-P) — never a walker of the previous pass's last phase, which a slow thread
-// may still be computing; the middle destinations take the rest in a keyed order of [0, n).
+// The pipelined exchange's table (chaos_body.cuh, PIPE): with P = n/S slots per phase, the last
+// phase's destinations [n-P, n) take the first P of a keyed order of [P, n) — never a walker of
+// the previous pass's first phase, whose slots a fast thread may already overwrite — and the first
+// phase's destinations [0, P) the first P not yet taken of a keyed order of [0, n-P) — never a
+// walker of the previous pass's last phase, which a slow thread may still be computing; the middle
+// destinations take the rest in a keyed order of [0, n).  One warp per permutation: the lanes walk
+// each keyed order 32 entries at a time and a ballot ranks the free ones, so the result is the
+// sequential scan's.  The taken-slot bitmap is in shared memory (n / 32 words per warp).
 // n <= kMaxPipeSlots, S >= 3 (then enough sources stay free for the first phase).
 constexpr uint32_t kMaxPipeSlots = 4096;
-__global__ void shuffle_table_pipe_kernel(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed, uint32_t phases) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= count) return;
+constexpr int kPipeTableWarps = 8;  // permutations per CTA
+__global__ void __launch_bounds__(32 * kPipeTableWarps)
+    shuffle_table_pipe_kernel(uint16_t* out, uint32_t n, uint32_t count, uint64_t seed, uint32_t phases) {
+    __shared__ uint32_t s_taken[kPipeTableWarps][kMaxPipeSlots / 32];
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t k = blockIdx.x * kPipeTableWarps + w;
+    if (k >= count) return;  // whole warps leave together
+    uint32_t* taken = s_taken[w];
+    for (uint32_t i = lane; i < n / 32; i += 32) taken[i] = 0;
+    __syncwarp();
     const uint32_t P = n / phases;
-    uint32_t taken[kMaxPipeSlots / 32];
-    for (uint32_t w = 0; w < kMaxPipeSlots / 32; w++) taken[w] = 0;
     uint16_t* o = out + (size_t)k * n;
     const uint64_t k3 = derive_key(seed, k, 3, TAG_TABLE), k1 = derive_key(seed, k, 1, TAG_TABLE),
                    k2 = derive_key(seed, k, 2, TAG_TABLE);
-    for (uint32_t d = 0; d < P; d++) {
+    for (uint32_t d = lane; d < P; d += 32) {
         const uint32_t src = P + feistel(d, n - P, k3);
         o[n - P + d] = (uint16_t)src;
-        taken[src >> 5] |= 1u << (src & 31);
+        atomicOr(&taken[src >> 5], 1u << (src & 31));
     }
-    uint32_t d = 0;
-    for (uint32_t i = 0; i < n - P && d < P; i++) {
-        const uint32_t src = feistel(i, n - P, k1);
-        if (!(taken[src >> 5] >> (src & 31) & 1u)) {
-            o[d++] = (uint16_t)src;
-            taken[src >> 5] |= 1u << (src & 31);
+    __syncwarp();
+    // the untaken entries of a keyed order of [0, len), in order, to destinations [d0, d1)
+    auto scan = [&](uint32_t len, uint64_t key, uint32_t d0, uint32_t d1) {
+        uint32_t d = d0;
+        for (uint32_t base = 0; base < len && d < d1; base += 32) {
+            const uint32_t i = base + lane;
+            const uint32_t src = i < len ? feistel(i, len, key) : 0u;
+            const bool free = i < len && !((taken[src >> 5] >> (src & 31)) & 1u);
+            const uint32_t ballot = __ballot_sync(0xffffffffu, free);
+            const uint32_t rank = __popc(ballot & ((1u << lane) - 1u));
+            if (free && d + rank < d1) {
+                o[d + rank] = (uint16_t)src;
+                atomicOr(&taken[src >> 5], 1u << (src & 31));
+            }
+            d = min(d + (uint32_t)__popc(ballot), d1);
+            __syncwarp();
         }
-    }
-    d = P;
-    for (uint32_t i = 0; i < n && d < n - P; i++) {
-        const uint32_t src = feistel(i, n, k2);
-        if (!(taken[src >> 5] >> (src & 31) & 1u)) {
-            o[d++] = (uint16_t)src;
-            taken[src >> 5] |= 1u << (src & 31);
-        }
-    }
+    };
+    scan(n - P, k1, 0, P);
+    scan(n, k2, P, n - P);
 }
 
 // animate.tpl.glsl:18-96 — one program copy per temporal sample, each xform's linear part
@@ -186,7 +197,8 @@ cudaError_t launch_shuffle_table(uint16_t* out, uint32_t n, uint32_t count, uint
     const uint32_t b = 256;
     if (phases >= 3) {
         if (n > kMaxPipeSlots || n % phases) return cudaErrorInvalidValue;
-        shuffle_table_pipe_kernel<<<(count + 63) / 64, 64, 0, st>>>(out, n, count, seed, phases);
+        shuffle_table_pipe_kernel<<<(count + kPipeTableWarps - 1) / kPipeTableWarps, 32 * kPipeTableWarps, 0, st>>>(
+            out, n, count, seed, phases);
         return cudaGetLastError();
     }
     shuffle_table_kernel<<<(unsigned)((total + b - 1) / b), b, 0, st>>>(out, n, count, seed);
