@@ -520,6 +520,7 @@ def run_native(args):
     build = kernel_build_id(flame, "%s/%d/%s" % (args.splat, int(reset), exchange)) if sim.specialized() else None
     same_build = build is not None and build == _profile_build(prof_key)
     inst = _profile_figure(prof_key, "warp instructions per point") if same_build else None
+    l2_busy = _profile_figure(prof_key, "l2 atomic unit busy") if same_build else None
     traffic = _traffic(prof_key) if same_build else None
     issue_bound = sms * 4 * clk_mhz * 1e6 / inst if inst else None  # points/s at one warp-inst per SMSP-cycle
     payload = 20.0 * binned_fraction  # float4 RGBA + u32 count reduced per binned point
@@ -536,7 +537,9 @@ def run_native(args):
                        "no ncu summary of this kernel build (%s)" % build,
         "points_per_launch": pts_per_launch, "launch_ms": per_launch_ms,
         "l2_reduction": {"bytes_per_point": payload, "gbs": payload * pts_s / 1e9,
-                         "note": "20 B (float4 RGBA + u32 count) per binned point"},
+                         "atomic_unit_busy": l2_busy / 100.0 if l2_busy is not None else None,
+                         "note": "20 B (float4 RGBA + u32 count) per binned point; atomic_unit_busy = the L2 "
+                                 "atomic units' active fraction (ncu, same kernel build): the splat's roofline"},
         "hbm": {"achieved": (traffic / (per_launch_ms * 1e-3) / 1e9) if traffic else None, "peak": peak,
                 "unit": "GB/s", "peak_source": peak_kind},
         "algorithmic": {"fp32_ops_per_point": ops, "library_calls_per_point": calls,
