@@ -160,17 +160,20 @@ def test_splat_strategies_after_warmup(rk, compiler):
         assert np.allclose(b, b0, rtol=1e-4, atol=1e-3), mode
 
 
-@pytest.mark.parametrize("specialize,slots,tile", [(0, 2048, (20, 30, 70, 50)), (-1, 2048, (0, 50, 128, 30)),
-                                                   (0, 4096, (40, 40, 32, 32)), (0, 2048, (0, 0, 0, 0))])
-def test_tile_splat_bit_exact(rk, orc, compiler, specialize, slots, tile):
+@pytest.mark.parametrize("specialize,slots,tile,exchange", [(0, 2048, (20, 30, 70, 50), 2), (-1, 2048, (0, 50, 128, 30), 2),
+                                                            (0, 4096, (40, 40, 32, 32), 2), (0, 2048, (0, 0, 0, 0), 2),
+                                                            (0, 4096, (40, 40, 32, 32), 1), (0, 4096, (32, 50, 64, 20), 0)])
+def test_tile_splat_bit_exact(rk, orc, compiler, specialize, slots, tile, exchange):
     """RF_SPLAT_TILE: the points inside the tile accumulate in each CTA's shared memory and reach
     the bins once per launch, the rest go straight to the L2.  On the affine genome the counts are
     bit-exact against the FP32 oracle on the kernel's shuffle schedule and the colour sums agree up
-    to FP32 summation order, whatever the tile (part of the grid, a band, an empty tile)."""
+    to FP32 summation order, whatever the tile (part of the grid, a band, an empty tile) and the
+    walker exchange (0 barrier, 1 pipelined, 2 chosen by timing)."""
     W = H = 128
     f = rk.Flame.from_xml(LINEAR, compiler)
     N, F, D = 8192, 20, 40
     sim = rk.Sim(N, seed=5, cta_slots=slots, specialize=specialize, steps_per_launch=32)
+    sim.set_exchange(exchange)
     sim.set_splat(rk.SPLAT_TILE)
     sim.set_splat_tile(*tile)
     sim.warmup(f, F - 1)
