@@ -49,8 +49,8 @@ WORKLOADS = {
     "contract": dict(name="contracting genome (seed 4, 6 xforms), 1920x1080 bins, 2^34 points",
                      genome=dict(kind=2, seed=4, n_xforms=0, final_xform=False, force_parametric=False),
                      genome_file="contract.flam3",
-                     out=(1920, 1080), ss=1, points=2 ** 34, de=None, image=False,
-                     splat="tile"),  # 26 hot bins: a shared-memory tile over them beats the L2
+                     out=(1920, 1080), ss=1, points=2 ** 34, de=None, image=False),
+    # (AUTO splat: the library fits a shared-memory tile over the attractor's hottest bins)
     "spacefill": dict(name="space-filling genome (seed 5, 16 xforms), 8192x8192 bins, 2^34 points",
                       genome=dict(kind=3, seed=5, n_xforms=0, final_xform=False, force_parametric=False),
                       genome_file="spacefill.flam3",
@@ -553,7 +553,7 @@ def run_native(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic genome (%s); no dataset" % WL["genome_file"],
         "config": workload_config(reset),
         "launch": {"walkers": walkers, "cta_slots": cta, "steps_per_launch": args.steps_per_launch,
-                   "passes_per_frame": passes, "splat": args.splat, "splat_tile": tile,
+                   "passes_per_frame": passes, "splat": args.splat, "splat_tile": tile or sim.splat_tile(),
                    "exchange": exchange, "exchange_mode": args.exchange,
                    "specialized_kernel": sim.specialized(),
                    "kernel_build": build, "first_warmup_s": first_warmup_s,

@@ -215,9 +215,16 @@ RF_API int  rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_wid
 
 /* Splat strategy for rf_draw_to_bins: one L2 reduction per point (GLOBAL), warp-aggregated
    reductions of the points that share a bin (WARP), or per warp and pass the aggregated form
-   when a cheap test finds two lanes sharing a bin (AUTO, the default).  The genome-specialised
-   kernel is compiled with the strategy set at rf_warmup; setting another one later makes the
-   next draw call fetch (or, the first time, compile) the kernel for it. */
+   when a cheap test finds two lanes sharing a bin (AUTO, the default).  AUTO also serves compact
+   attractors with the shared-memory tile splat (RF_SPLAT_TILE below): after the first full
+   drawing launch on a bin grid, when the caller passes a count plane (direct layout, not during
+   stream capture), the call synchronises once, reads the counts back, fits the tile that fits
+   beside the walkers and holds the most hits (the hit bins' bounding box, else the best
+   square-ish window), and draws through it from then on if it holds >= 25 % of the hits
+   (rf_sim_splat_tile reports it).  Counts never change with the strategy; colour sums only in
+   FP32 summation order.  The genome-specialised kernel is compiled with the strategy set at
+   rf_warmup; setting another one later makes the next draw call fetch (or, the first time,
+   compile) the kernel for it. */
 enum rf_splat { RF_SPLAT_AUTO = 0, RF_SPLAT_GLOBAL = 1, RF_SPLAT_WARP = 2, RF_SPLAT_TILE = 3 };
 /* flame::draw_to_bins(bins, bins_width, num_iter) (flame.cpp:283-330): num_iter passes over
    every walker, drawing into caller-owned device bins.  bins_hits may be NULL.  When `drawn`
@@ -264,6 +271,9 @@ enum rf_exchange { RF_EXCHANGE_BARRIER = 0, RF_EXCHANGE_PIPELINED = 1, RF_EXCHAN
 RF_API int  rf_set_exchange(rf_sim* s, int mode);
 /* The form the Sim's next full drawing launch runs: 0 barrier, 1 pipelined (-1: null sim). */
 RF_API int  rf_sim_exchange(const rf_sim* s);
+/* The shared-memory tile the drawing passes use (RF_SPLAT_TILE's, or the one RF_SPLAT_AUTO chose):
+   1 and x0, y0, w, h in out, 0 when there is none, -1 on a null argument. */
+RF_API int  rf_sim_splat_tile(const rf_sim* s, uint32_t out[4]);
 /* [0] points binned and [1] points emitted (opacity > 0) by the last rf_draw_to_bins call,
    [2] walker-steps since rf_warmup. */
 RF_API int  rf_sim_counters(rf_sim* s, uint64_t out[3]);

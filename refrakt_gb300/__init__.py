@@ -151,6 +151,7 @@ _SIGS = {
     "rf_set_bad_value_reset": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rf_set_exchange": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rf_sim_exchange": ([ctypes.c_void_p], ctypes.c_int),
+    "rf_sim_splat_tile": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rf_set_splat_tile": ([ctypes.c_void_p] + [ctypes.c_uint32] * 4, ctypes.c_int),
     "rf_set_bin_layout": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "rf_sim_counters": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
@@ -515,6 +516,11 @@ class Sim:
     def exchange(self):
         """The form the next full drawing launch runs: EXCHANGE_BARRIER or EXCHANGE_PIPELINED."""
         return library().rf_sim_exchange(self._h)
+
+    def splat_tile(self):
+        """(x0, y0, w, h) of the shared-memory tile the drawing passes use, or None."""
+        t = (ctypes.c_uint32 * 4)()
+        return tuple(t) if library().rf_sim_splat_tile(self._h, t) == 1 else None
 
     def set_bin_layout(self, layout):
         """BINS_AUTO, BINS_DIRECT or BINS_INTERLEAVED (rf_set_bin_layout)."""

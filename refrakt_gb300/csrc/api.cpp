@@ -78,6 +78,72 @@ bool use_pipe(const rf_sim* s, uint32_t tile_bins) {
     return s->table_phases >= 3 && chaos_smem(s->slots, s->prog_words, s->L, tile_bins, 1) <= kMaxCtaSmem;
 }
 
+void reset_exchange_tuning(rf_sim* s);
+
+bool capturing(cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
+}
+
+// The tile (x0, y0, w, h) of at most `cap` bins that holds the most hits — the bounding box of the
+// hit bins when it fits, else the window of about sqrt(cap) x sqrt(cap) bins with the largest sum
+// (2D prefix sums) — and the share of all hits inside it.
+double fit_splat_tile(const std::vector<uint32_t>& h, uint32_t W, uint32_t H, uint32_t cap, uint32_t t[4]) {
+    uint64_t total = 0;
+    uint32_t x0 = W, x1 = 0, y0 = H, y1 = 0;
+    for (uint32_t y = 0; y < H; y++)
+        for (uint32_t x = 0; x < W; x++)
+            if (const uint32_t v = h[(size_t)y * W + x]) {
+                total += v;
+                x0 = std::min(x0, x); x1 = std::max(x1, x);
+                y0 = std::min(y0, y); y1 = std::max(y1, y);
+            }
+    if (!total || !cap) return 0.0;
+    if ((uint64_t)(x1 - x0 + 1) * (y1 - y0 + 1) <= cap) {
+        t[0] = x0; t[1] = y0; t[2] = x1 - x0 + 1; t[3] = y1 - y0 + 1;
+        return 1.0;
+    }
+    const uint32_t w = std::min<uint32_t>(W, std::max<uint32_t>(1, (uint32_t)std::sqrt((double)cap)));
+    const uint32_t hh = std::min<uint32_t>(H, cap / w);
+    std::vector<uint64_t> P((size_t)(W + 1) * (H + 1), 0);
+    for (uint32_t y = 0; y < H; y++) {
+        uint64_t row = 0;
+        for (uint32_t x = 0; x < W; x++) {
+            row += h[(size_t)y * W + x];
+            P[(size_t)(y + 1) * (W + 1) + x + 1] = P[(size_t)y * (W + 1) + x + 1] + row;
+        }
+    }
+    uint64_t best = 0;
+    t[0] = t[1] = 0; t[2] = w; t[3] = hh;
+    for (uint32_t y = 0; y + hh <= H; y++)
+        for (uint32_t x = 0; x + w <= W; x++) {
+            const uint64_t v = P[(size_t)(y + hh) * (W + 1) + x + w] - P[(size_t)y * (W + 1) + x + w] -
+                               P[(size_t)(y + hh) * (W + 1) + x] + P[(size_t)y * (W + 1) + x];
+            if (v > best) { best = v; t[0] = x; t[1] = y; }
+        }
+    return (double)best / (double)total;
+}
+
+// RF_SPLAT_AUTO's decision for a compact attractor, from the hits of the first full drawing
+// launch on this grid: the tile splat over the fitted tile when it holds >= 25 % of the hits.
+int decide_auto_tile(rf_sim* s, const uint32_t* hits, uint32_t W, uint32_t H) {
+    s->auto_tile_state = -1;
+    s->auto_tile_wh[0] = W;
+    s->auto_tile_wh[1] = H;
+    std::vector<uint32_t> h((size_t)W * H);
+    RF_CUDA(cudaStreamSynchronize(s->stream));
+    RF_CUDA(cudaMemcpy(h.data(), hits, h.size() * 4, cudaMemcpyDeviceToHost));
+    const size_t used = (chaos_smem(s->slots, s->prog_words, s->L, 0, 1) + 15) & ~(size_t)15;
+    const uint32_t cap = used < kMaxCtaSmem ? (uint32_t)std::min<size_t>((kMaxCtaSmem - used) / 20, 65536) : 0u;
+    uint32_t t[4];
+    if (fit_splat_tile(h, W, H, cap, t) >= 0.25) {
+        s->auto_tile_state = 1;
+        memcpy(s->auto_tile, t, sizeof t);
+        reset_exchange_tuning(s);  // the kernel changes: time both exchange forms again
+    }
+    return RF_OK;
+}
+
 // RF_EXCHANGE_AUTO starts over (a new genome structure, splat, tile or reset changes the kernels)
 void reset_exchange_tuning(rf_sim* s) {
     s->tune_step = 0;
@@ -103,9 +169,7 @@ int exchange_for_launch(rf_sim* s, bool full_draw, int* measure) {
             s->tune_step = 3;  // the events failed: keep the default
         }
     }
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    if (s->tune_step < 2 && full_draw && s->tune_ev[0] && cudaStreamIsCapturing(s->stream, &cs) == cudaSuccess &&
-        cs == cudaStreamCaptureStatusNone) {
+    if (s->tune_step < 2 && full_draw && s->tune_ev[0] && !capturing(s->stream)) {
         *measure = s->tune_step;
         return s->tune_step;
     }
@@ -144,15 +208,18 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.seed = s->d.seed;
         a.first_run = (first_run && done == 0) ? 1 : 0;
         a.draw = draw ? 1 : 0;
-        a.splat = splat_code(s->splat);
+        const bool auto_tile = draw && s->splat == RF_SPLAT_AUTO && s->auto_tile_state == 1 && s->rgba_shift == 0 &&
+                               s->auto_tile_wh[0] == W && s->auto_tile_wh[1] == H;
+        a.splat = auto_tile ? 3 : splat_code(s->splat);
         a.reset = s->reset;
         a.rgba_shift = s->rgba_shift;
         a.count_shift = s->count_shift;
         if (ss) memcpy(a.ss, ss, sizeof(a.ss));
-        a.tile_x0 = s->tile[0];
-        a.tile_y0 = s->tile[1];
-        a.tile_w = s->tile[2];
-        a.tile_h = s->tile[3];
+        const uint32_t* tl = auto_tile ? s->auto_tile : s->tile;
+        a.tile_x0 = tl[0];
+        a.tile_y0 = tl[1];
+        a.tile_w = tl[2];
+        a.tile_h = tl[3];
         a.W = W;
         a.H = H;
         a.bins = bins;
@@ -192,6 +259,9 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         s->cur ^= 1;
         s->pass += steps;
         done += steps;
+        if (draw && steps == s->L && s->splat == RF_SPLAT_AUTO && hits && s->rgba_shift == 0 &&
+            (s->auto_tile_state == 0 || s->auto_tile_wh[0] != W || s->auto_tile_wh[1] != H) && !capturing(s->stream))
+            if (int rc = decide_auto_tile(s, hits, W, H)) return rc;
     }
     return RF_OK;
 }
@@ -602,7 +672,10 @@ int rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_width) {
     if (int rc = genome_validate(f->g, *f->reg)) return rc;
     s->prog_words = (uint32_t)prog.size();
     s->spec = nullptr;
-    if (prog != s->spec_prog) reset_exchange_tuning(s);
+    if (prog != s->spec_prog) {
+        reset_exchange_tuning(s);
+        s->auto_tile_state = 0;
+    }
     if (s->d.specialize >= 0) {
         const void* k = nullptr;
         const int pipe = s->exchange != RF_EXCHANGE_BARRIER && use_pipe(s, 0) ? 1 : 0;
@@ -669,6 +742,7 @@ int rf_set_bin_layout(rf_sim* s, int layout) {
 int rf_set_splat(rf_sim* s, int splat) {
     if (!s) return fail(RF_ERR_INVALID_ARG, "rf_set_splat: null sim");
     if (splat != s->splat) reset_exchange_tuning(s);
+    s->auto_tile_state = 0;
     s->splat = splat;
     return RF_OK;
 }
@@ -699,9 +773,20 @@ int rf_set_exchange(rf_sim* s, int mode) {
     return RF_OK;
 }
 
+int rf_sim_splat_tile(const rf_sim* s, uint32_t out[4]) {
+    if (!s || !out) return -1;
+    const uint32_t* t = s->splat == RF_SPLAT_TILE ? s->tile
+                        : (s->splat == RF_SPLAT_AUTO && s->auto_tile_state == 1) ? s->auto_tile : nullptr;
+    if (!t) return 0;
+    memcpy(out, t, 4 * sizeof(uint32_t));
+    return 1;
+}
+
 int rf_sim_exchange(const rf_sim* s) {
     if (!s) return -1;
-    const uint32_t tile_bins = s->splat == RF_SPLAT_TILE ? s->tile[2] * s->tile[3] : 0u;
+    const uint32_t tile_bins = s->splat == RF_SPLAT_TILE                              ? s->tile[2] * s->tile[3]
+                               : s->splat == RF_SPLAT_AUTO && s->auto_tile_state == 1 ? s->auto_tile[2] * s->auto_tile[3]
+                                                                                      : 0u;
     if (!s->spec || !use_pipe(s, tile_bins)) return 0;
     if (s->exchange != RF_EXCHANGE_AUTO) return s->exchange == RF_EXCHANGE_PIPELINED ? 1 : 0;
     return s->tune_pipe;

@@ -42,6 +42,11 @@ struct rf_sim {
     int spec_splat = -1;              // the splat strategy compiled into it (ChaosArgs.splat code)
     int reset = 0;                    // walker reset of flame.glsl:68 (rf_set_bad_value_reset)
     uint32_t tile[4] = {0, 0, 0, 0};  // the tile splat's bins: x0, y0, w, h (rf_set_splat_tile)
+    // RF_SPLAT_AUTO on a compact attractor: 0 undecided, 1 the tile splat over auto_tile, -1 not;
+    // decided on the bin grid auto_tile_wh from the hits after the first full drawing launch
+    int auto_tile_state = 0;
+    uint32_t auto_tile[4] = {0, 0, 0, 0};
+    uint32_t auto_tile_wh[2] = {0, 0};
     int spec_reset = -1;              // the reset setting compiled into the specialised kernel
     int spec_pipe = 0;                // 1: the specialised kernel has the pipelined walker exchange
     uint32_t table_phases = 0;        // phases per pass the shuffle table is pipelined for (0: uniform)
