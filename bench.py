@@ -517,7 +517,8 @@ def run_native(args):
     pts_s = pts_per_launch / (per_launch_ms * 1e-3)
     prof_key = {"frame1080": "1080p"}.get(args.workload, args.workload)
     exchange = "pipelined" if sim.exchange() == R.EXCHANGE_PIPELINED else "barrier"
-    build = kernel_build_id(flame, "%s/%d/%s" % (args.splat, int(reset), exchange)) if sim.specialized() else None
+    splat_used = "tile" if sim.splat_tile() else args.splat  # AUTO may have fitted a tile
+    build = kernel_build_id(flame, "%s/%d/%s" % (splat_used, int(reset), exchange)) if sim.specialized() else None
     same_build = build is not None and build == _profile_build(prof_key)
     inst = _profile_figure(prof_key, "warp instructions per point") if same_build else None
     l2_busy = _profile_figure(prof_key, "l2 atomic unit busy") if same_build else None
