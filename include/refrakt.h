@@ -216,9 +216,10 @@ RF_API int  rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_wid
 /* Splat strategy for rf_draw_to_bins: one L2 reduction per point (GLOBAL), warp-aggregated
    reductions of the points that share a bin (WARP), or per warp and pass the aggregated form
    when a cheap test finds two lanes sharing a bin (AUTO, the default).  AUTO also serves compact
-   attractors with the shared-memory tile splat (RF_SPLAT_TILE below): after the first full
-   drawing launch on a bin grid, when the caller passes a count plane (direct layout, not during
-   stream capture), the call synchronises once, reads the counts back, fits the tile that fits
+   attractors with the shared-memory tile splat (RF_SPLAT_TILE below): after the first drawing
+   launch of >= 32 passes on a bin grid of at most 2^24 bins, when the caller passes a count plane
+   (direct layout, not during stream capture), the call synchronises once, reads the counts
+   back, fits the tile that fits
    beside the walkers and holds the most hits (the hit bins' bounding box, else the best
    square-ish window), and draws through it from then on if it holds >= 25 % of the hits
    (rf_sim_splat_tile reports it).  Counts never change with the strategy; colour sums only in
@@ -262,14 +263,15 @@ RF_API int  rf_set_bad_value_reset(rf_sim* s, int on);
    three phases of this one, so the slowest warps' last phase overlaps the next pass (faster on
    genomes of unequal, costly xforms; slower on cheap ones with contended splats).
    RF_EXCHANGE_AUTO (default): after a warmup of a new genome structure (or a change of splat,
-   tile or walker reset) the first two full drawing launches run one form each, timed with CUDA
-   events, and the faster runs from then on (decided without a host wait, once the second launch
-   has finished; not during stream capture, where the pipelined form runs).  All forms give
+   tile or walker reset) the first two drawing launches of >= 32 passes and equal length run one
+   form each, timed with CUDA events, and the faster runs from then on (decided without a host
+   wait, once the second launch has finished; not during stream capture, where the pipelined form
+   runs).  All forms give
    identical results.  A pipelined wait that runs out (bounded) makes the next synchronising call
    (rf_draw_to_bins with `drawn`, rf_sim_counters, rf_render) return RF_ERR_TIMEOUT. */
 enum rf_exchange { RF_EXCHANGE_BARRIER = 0, RF_EXCHANGE_PIPELINED = 1, RF_EXCHANGE_AUTO = 2 };
 RF_API int  rf_set_exchange(rf_sim* s, int mode);
-/* The form the Sim's next full drawing launch runs: 0 barrier, 1 pipelined (-1: null sim). */
+/* The form the Sim's next drawing launch runs: 0 barrier, 1 pipelined (-1: null sim). */
 RF_API int  rf_sim_exchange(const rf_sim* s);
 /* The shared-memory tile the drawing passes use (RF_SPLAT_TILE's, or the one RF_SPLAT_AUTO chose):
    1 and x0, y0, w, h in out, 0 when there is none, -1 on a null argument. */

@@ -510,11 +510,11 @@ class Sim:
     def set_exchange(self, mode):
         """Walker exchange of the specialised chaos kernel (rf_set_exchange): EXCHANGE_BARRIER,
         EXCHANGE_PIPELINED or EXCHANGE_AUTO (default: the faster of the two, timed on the first
-        two full drawing launches); every form gives the same results."""
+        two drawing launches of >= 32 passes); every form gives the same results."""
         _check(library().rf_set_exchange(self._h, int(mode)))
 
     def exchange(self):
-        """The form the next full drawing launch runs: EXCHANGE_BARRIER or EXCHANGE_PIPELINED."""
+        """The form the next drawing launch runs: EXCHANGE_BARRIER or EXCHANGE_PIPELINED."""
         return library().rf_sim_exchange(self._h)
 
     def splat_tile(self):

@@ -124,8 +124,11 @@ double fit_splat_tile(const std::vector<uint32_t>& h, uint32_t W, uint32_t H, ui
     return (double)best / (double)total;
 }
 
-// RF_SPLAT_AUTO's decision for a compact attractor, from the hits of the first full drawing
-// launch on this grid: the tile splat over the fitted tile when it holds >= 25 % of the hits.
+// RF_SPLAT_AUTO's decision for a compact attractor, from the hits of the first drawing launch of
+// >= 32 passes on this grid: the tile splat over the fitted tile when it holds >= 25 % of the hits.
+// Grids above kAutoTileMaxBins are not read back (their planes go through interleaved records
+// by default anyway).
+constexpr uint64_t kAutoTileMaxBins = 1ull << 24;
 int decide_auto_tile(rf_sim* s, const uint32_t* hits, uint32_t W, uint32_t H) {
     s->auto_tile_state = -1;
     s->auto_tile_wh[0] = W;
@@ -151,8 +154,9 @@ void reset_exchange_tuning(rf_sim* s) {
 }
 
 // The exchange form of the next launch (1 pipelined); *measure = 0 / 1 when RF_EXCHANGE_AUTO times
-// this launch as the barrier / pipelined form, else -1.
-int exchange_for_launch(rf_sim* s, bool full_draw, int* measure) {
+// this launch as the barrier / pipelined form, else -1.  Drawing launches of >= 32 passes are
+// timed, the second one only at the first one's length.
+int exchange_for_launch(rf_sim* s, bool draw, uint32_t steps, int* measure) {
     *measure = -1;
     if (s->exchange != RF_EXCHANGE_AUTO) return s->exchange == RF_EXCHANGE_PIPELINED ? 1 : 0;
     if (s->tune_step == 2) {  // both forms timed: decide once the second launch has finished
@@ -169,7 +173,9 @@ int exchange_for_launch(rf_sim* s, bool full_draw, int* measure) {
             s->tune_step = 3;  // the events failed: keep the default
         }
     }
-    if (s->tune_step < 2 && full_draw && s->tune_ev[0] && !capturing(s->stream)) {
+    if (s->tune_step < 2 && draw && steps >= 32 && (s->tune_step == 0 || steps == s->tune_passes) && s->tune_ev[0] &&
+        !capturing(s->stream)) {
+        if (s->tune_step == 0) s->tune_passes = steps;
         *measure = s->tune_step;
         return s->tune_step;
     }
@@ -232,7 +238,7 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         const uint32_t grid = (uint32_t)(s->N / s->slots);
         const uint32_t tile_bins = a.splat == 3 && a.draw ? a.tile_w * a.tile_h : 0u;
         int measure = -1;
-        const int want = s->spec ? exchange_for_launch(s, a.draw && steps == s->L, &measure) : 0;
+        const int want = s->spec ? exchange_for_launch(s, a.draw, steps, &measure) : 0;
         const int pipe = want && s->spec && use_pipe(s, tile_bins) ? 1 : 0;
         if (s->spec && (s->spec_splat != a.splat || s->spec_reset != a.reset || s->spec_pipe != pipe)) {
             // the splat strategy, the reset or the exchange changed since warmup: the kernel compiled for them
@@ -259,7 +265,8 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         s->cur ^= 1;
         s->pass += steps;
         done += steps;
-        if (draw && steps == s->L && s->splat == RF_SPLAT_AUTO && hits && s->rgba_shift == 0 &&
+        if (draw && steps >= 32 && s->splat == RF_SPLAT_AUTO && hits && s->rgba_shift == 0 &&
+            (uint64_t)W * H <= kAutoTileMaxBins &&
             (s->auto_tile_state == 0 || s->auto_tile_wh[0] != W || s->auto_tile_wh[1] != H) && !capturing(s->stream))
             if (int rc = decide_auto_tile(s, hits, W, H)) return rc;
     }

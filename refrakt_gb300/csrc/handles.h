@@ -54,6 +54,7 @@ struct rf_sim {
     // RF_EXCHANGE_AUTO: 0/1 — the next full drawing launch is timed as the barrier / pipelined form;
     // 2 — both timed, deciding when the second has finished; 3 — decided (tune_pipe)
     int tune_step = 0;
+    uint32_t tune_passes = 0;         // the length of the first timed launch (the second must match)
     int tune_pipe = 1;                // the form chosen (the pipelined one until decided)
     cudaEvent_t tune_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<uint32_t> spec_prog;  // the warmed program, to specialise again for another strategy

@@ -47,7 +47,7 @@ def test_affine_genome_bit_exact(rk, orc, compiler, cta, threads):
 @pytest.mark.parametrize("L", [1, 2, 7, 256])
 def test_pipelined_exchange_equals_barrier_exchange(rk, compiler, L):
     """On a nonlinear genome with the walker reset and a final xform, the pipelined exchange and
-    the automatic choice (which times both forms on its first two full drawing launches) draw the
+    the automatic choice (which times both forms on its first two drawing launches of >= 32 passes) draw the
     same xform-id streams and the same counts as the barrier form, for launches of any length (the
     first pass of each launch is the gather, the last one draws no next xform)."""
     W = H = 128
@@ -194,7 +194,7 @@ def test_tile_splat_bit_exact(rk, orc, compiler, specialize, slots, tile, exchan
 
 @pytest.mark.parametrize("genome,W,H,want_tile", [("contract", 480, 270, True), ("frame1080", 1920, 1080, False)])
 def test_auto_splat_fits_a_tile_to_compact_attractors(rk, orc, compiler, genome, W, H, want_tile):
-    """RF_SPLAT_AUTO switches to a fitted shared-memory tile after the first full drawing launch
+    """RF_SPLAT_AUTO switches to a fitted shared-memory tile after the first drawing launch of >= 32 passes
     when the attractor is compact (the contracting genome) and keeps warp aggregation when it is
     spread (the 1080p genome).  Counts stay exact: on the affine contracting genome they equal the
     FP32 oracle's on the kernel's schedule."""
