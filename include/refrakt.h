@@ -216,13 +216,14 @@ RF_API int  rf_warmup(rf_sim* s, rf_flame* f, uint32_t num_passes, float tss_wid
 /* Splat strategy for rf_draw_to_bins: one L2 reduction per point (GLOBAL), warp-aggregated
    reductions of the points that share a bin (WARP), or per warp and pass the aggregated form
    when a cheap test finds two lanes sharing a bin (AUTO, the default).  AUTO also serves compact
-   attractors with the shared-memory tile splat (RF_SPLAT_TILE below): after the first drawing
+   attractors with the shared-memory tile splat (RF_SPLAT_TILE below): after the second drawing
    launch of >= 32 passes on a bin grid of at most 2^24 bins, when the caller passes a count plane
-   (direct layout, not during stream capture), the call synchronises once, reads the counts
-   back, fits the tile that fits
-   beside the walkers and holds the most hits (the hit bins' bounding box, else the best
-   square-ish window), and draws through it from then on if it holds >= 25 % of the hits
-   (rf_sim_splat_tile reports it).  Counts never change with the strategy; colour sums only in
+   (direct layout, not during stream capture), the call synchronises once, reads the counts back
+   and fits the tile that fits beside the walkers and holds the most hits (the hit bins'
+   bounding box, else the best square-ish window); if it holds >= 25 % of the hits, the next
+   drawing launch of the same length runs through it, timed against the first, and the faster
+   splat is kept (decided without a host wait once that launch has finished; rf_sim_splat_tile
+   reports it).  Counts never change with the strategy; colour sums only in
    FP32 summation order.  The genome-specialised kernel is compiled with the strategy set at
    rf_warmup; setting another one later makes the next draw call fetch (or, the first time,
    compile) the kernel for it. */
@@ -274,8 +275,9 @@ RF_API int  rf_set_exchange(rf_sim* s, int mode);
 /* The form the Sim's next drawing launch runs: 0 barrier, 1 pipelined (-1: null sim). */
 RF_API int  rf_sim_exchange(const rf_sim* s);
 /* The shared-memory tile the drawing passes use (RF_SPLAT_TILE's, or the one RF_SPLAT_AUTO chose):
-   1 and x0, y0, w, h in out, 0 when there is none, -1 on a null argument. */
-RF_API int  rf_sim_splat_tile(const rf_sim* s, uint32_t out[4]);
+   1 and x0, y0, w, h in out, 0 when there is none, -1 on a null argument or a failed call.
+   Synchronises the Sim's stream when RF_SPLAT_AUTO's timing of a fitted tile is still pending. */
+RF_API int  rf_sim_splat_tile(rf_sim* s, uint32_t out[4]);
 /* [0] points binned and [1] points emitted (opacity > 0) by the last rf_draw_to_bins call,
    [2] walker-steps since rf_warmup. */
 RF_API int  rf_sim_counters(rf_sim* s, uint64_t out[3]);

@@ -124,15 +124,14 @@ double fit_splat_tile(const std::vector<uint32_t>& h, uint32_t W, uint32_t H, ui
     return (double)best / (double)total;
 }
 
-// RF_SPLAT_AUTO's decision for a compact attractor, from the hits of the first drawing launch of
-// >= 32 passes on this grid: the tile splat over the fitted tile when it holds >= 25 % of the hits.
-// Grids above kAutoTileMaxBins are not read back (their planes go through interleaved records
-// by default anyway).
+// RF_SPLAT_AUTO for compact attractors.  After the second drawing launch of >= 32 passes on a grid
+// (timed; the first warms the grid up), the counts are read back once and a tile fitted; if it
+// holds >= 25 % of the hits, the next launch of the same length runs with it (timed) and the
+// faster form is kept.  Grids above
+// kAutoTileMaxBins are not read back (their planes go through interleaved records by default).
 constexpr uint64_t kAutoTileMaxBins = 1ull << 24;
-int decide_auto_tile(rf_sim* s, const uint32_t* hits, uint32_t W, uint32_t H) {
+int fit_auto_tile(rf_sim* s, const uint32_t* hits, uint32_t W, uint32_t H) {
     s->auto_tile_state = -1;
-    s->auto_tile_wh[0] = W;
-    s->auto_tile_wh[1] = H;
     std::vector<uint32_t> h((size_t)W * H);
     RF_CUDA(cudaStreamSynchronize(s->stream));
     RF_CUDA(cudaMemcpy(h.data(), hits, h.size() * 4, cudaMemcpyDeviceToHost));
@@ -140,11 +139,24 @@ int decide_auto_tile(rf_sim* s, const uint32_t* hits, uint32_t W, uint32_t H) {
     const uint32_t cap = used < kMaxCtaSmem ? (uint32_t)std::min<size_t>((kMaxCtaSmem - used) / 20, 65536) : 0u;
     uint32_t t[4];
     if (fit_splat_tile(h, W, H, cap, t) >= 0.25) {
-        s->auto_tile_state = 1;
+        s->auto_tile_state = 3;
         memcpy(s->auto_tile, t, sizeof t);
-        reset_exchange_tuning(s);  // the kernel changes: time both exchange forms again
     }
     return RF_OK;
+}
+
+// state 4: keep the tile if its timed launch was faster, once that launch has finished
+void decide_auto_tile(rf_sim* s) {
+    const cudaError_t q = cudaEventQuery(s->tile_ev[3]);
+    if (q == cudaErrorNotReady) {
+        if (cudaPeekAtLastError() == cudaErrorNotReady) cudaGetLastError();  // clear only this status
+        return;
+    }
+    float t0 = 0.0f, t1 = 0.0f;
+    const bool ok = q == cudaSuccess && cudaEventElapsedTime(&t0, s->tile_ev[0], s->tile_ev[1]) == cudaSuccess &&
+                    cudaEventElapsedTime(&t1, s->tile_ev[2], s->tile_ev[3]) == cudaSuccess;
+    s->auto_tile_state = ok && t1 < t0 ? 1 : -1;
+    reset_exchange_tuning(s);  // time the exchange forms on the kernel that stays
 }
 
 // RF_EXCHANGE_AUTO starts over (a new genome structure, splat, tile or reset changes the kernels)
@@ -156,7 +168,7 @@ void reset_exchange_tuning(rf_sim* s) {
 // The exchange form of the next launch (1 pipelined); *measure = 0 / 1 when RF_EXCHANGE_AUTO times
 // this launch as the barrier / pipelined form, else -1.  Drawing launches of >= 32 passes are
 // timed, the second one only at the first one's length.
-int exchange_for_launch(rf_sim* s, bool draw, uint32_t steps, int* measure) {
+int exchange_for_launch(rf_sim* s, bool draw, uint32_t steps, bool may_measure, int* measure) {
     *measure = -1;
     if (s->exchange != RF_EXCHANGE_AUTO) return s->exchange == RF_EXCHANGE_PIPELINED ? 1 : 0;
     if (s->tune_step == 2) {  // both forms timed: decide once the second launch has finished
@@ -174,7 +186,7 @@ int exchange_for_launch(rf_sim* s, bool draw, uint32_t steps, int* measure) {
         }
     }
     if (s->tune_step < 2 && draw && steps >= 32 && (s->tune_step == 0 || steps == s->tune_passes) && s->tune_ev[0] &&
-        !capturing(s->stream)) {
+        may_measure && !capturing(s->stream)) {
         if (s->tune_step == 0) s->tune_passes = steps;
         *measure = s->tune_step;
         return s->tune_step;
@@ -214,8 +226,21 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         a.seed = s->d.seed;
         a.first_run = (first_run && done == 0) ? 1 : 0;
         a.draw = draw ? 1 : 0;
-        const bool auto_tile = draw && s->splat == RF_SPLAT_AUTO && s->auto_tile_state == 1 && s->rgba_shift == 0 &&
-                               s->auto_tile_wh[0] == W && s->auto_tile_wh[1] == H;
+        // RF_SPLAT_AUTO's tile: settle a pending decision, then see whether this launch is timed
+        const bool tile_grid = draw && s->splat == RF_SPLAT_AUTO && s->rgba_shift == 0 && hits &&
+                               (uint64_t)W * H <= kAutoTileMaxBins && s->tile_ev[0] && !capturing(s->stream);
+        if (tile_grid && (s->auto_tile_wh[0] != W || s->auto_tile_wh[1] != H)) {
+            s->auto_tile_state = 0;  // a new grid
+            s->auto_tile_wh[0] = W;
+            s->auto_tile_wh[1] = H;
+        }
+        if (s->auto_tile_state == 4) decide_auto_tile(s);
+        int tile_timed = -1;  // 0: the untiled launch, 1: the tiled one
+        const bool tile_warmup = tile_grid && steps >= 32 && s->auto_tile_state == 0;  // not timed: the grid's first
+        if (tile_grid && steps >= 32 && s->auto_tile_state == 2) tile_timed = 0;
+        if (tile_grid && steps == s->auto_tile_passes && s->auto_tile_state == 3) tile_timed = 1;
+        const bool auto_tile = draw && s->splat == RF_SPLAT_AUTO && s->rgba_shift == 0 && s->auto_tile_wh[0] == W &&
+                               s->auto_tile_wh[1] == H && (s->auto_tile_state == 1 || tile_timed == 1);
         a.splat = auto_tile ? 3 : splat_code(s->splat);
         a.reset = s->reset;
         a.rgba_shift = s->rgba_shift;
@@ -238,7 +263,9 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
         const uint32_t grid = (uint32_t)(s->N / s->slots);
         const uint32_t tile_bins = a.splat == 3 && a.draw ? a.tile_w * a.tile_h : 0u;
         int measure = -1;
-        const int want = s->spec ? exchange_for_launch(s, a.draw, steps, &measure) : 0;
+        // (RF_SPLAT_AUTO's tile is timed first, in the pipelined form; the exchange after it)
+        const bool tile_busy = tile_warmup || tile_timed >= 0 || (s->splat == RF_SPLAT_AUTO && s->auto_tile_state >= 2);
+        const int want = s->spec ? exchange_for_launch(s, a.draw, steps, !tile_busy, &measure) : 0;
         const int pipe = want && s->spec && use_pipe(s, tile_bins) ? 1 : 0;
         if (s->spec && (s->spec_splat != a.splat || s->spec_reset != a.reset || s->spec_pipe != pipe)) {
             // the splat strategy, the reset or the exchange changed since warmup: the kernel compiled for them
@@ -256,19 +283,28 @@ int launch_passes(rf_sim* s, uint32_t passes, bool first_run, bool draw, float4*
                                          " bins exceeds the shared memory beside " + std::to_string(s->slots) +
                                          " walker slots");
         if (measure >= 0 && cudaEventRecord(s->tune_ev[2 * measure], s->stream) != cudaSuccess) measure = -1;
+        if (tile_timed >= 0 && cudaEventRecord(s->tile_ev[2 * tile_timed], s->stream) != cudaSuccess) tile_timed = -1;
         cudaError_t e = s->spec ? launch_spec(s->spec, (int)s->threads, (int)s->slots, a, grid,
                                               chaos_smem(s->slots, a.prog_words, a.steps, tile_bins, pipe), s->stream)
                                 : launch_chaos((int)s->threads, (int)s->slots, a, grid, s->stream);
         if (e != cudaSuccess) return cuda_fail(e, "chaos kernel launch");
         if (measure >= 0 && cudaEventRecord(s->tune_ev[2 * measure + 1], s->stream) == cudaSuccess)
             s->tune_step = measure + 1;
+        const bool tile_recorded = tile_timed >= 0 && cudaEventRecord(s->tile_ev[2 * tile_timed + 1], s->stream) == cudaSuccess;
         s->cur ^= 1;
         s->pass += steps;
         done += steps;
-        if (draw && steps >= 32 && s->splat == RF_SPLAT_AUTO && hits && s->rgba_shift == 0 &&
-            (uint64_t)W * H <= kAutoTileMaxBins &&
-            (s->auto_tile_state == 0 || s->auto_tile_wh[0] != W || s->auto_tile_wh[1] != H) && !capturing(s->stream))
-            if (int rc = decide_auto_tile(s, hits, W, H)) return rc;
+        if (tile_warmup) s->auto_tile_state = 2;
+        if (tile_timed == 0) {
+            if (!tile_recorded) {
+                s->auto_tile_state = -1;
+            } else {
+                s->auto_tile_passes = steps;
+                if (int rc = fit_auto_tile(s, hits, W, H)) return rc;  // -> 3 (a candidate) or -1
+            }
+        } else if (tile_timed == 1) {
+            s->auto_tile_state = tile_recorded ? 4 : -1;
+        }
     }
     return RF_OK;
 }
@@ -619,6 +655,8 @@ int rf_sim_create(const rf_sim_desc* d, rf_sim** out) {
         return cleanup(cuda_fail(e, "memset"));
     for (auto& ev : s->tune_ev)
         if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cleanup(cuda_fail(e, "event"));
+    for (auto& ev : s->tile_ev)
+        if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cleanup(cuda_fail(e, "event"));
     if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cleanup(cuda_fail(e, "sim init"));
     *out = s;
     return RF_OK;
@@ -633,6 +671,8 @@ int rf_sim_destroy(rf_sim* s) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto ev : s->tune_ev)
+        if (ev) cudaEventDestroy(ev);
+    for (auto ev : s->tile_ev)
         if (ev) cudaEventDestroy(ev);
     delete s;
     return RF_OK;
@@ -780,8 +820,12 @@ int rf_set_exchange(rf_sim* s, int mode) {
     return RF_OK;
 }
 
-int rf_sim_splat_tile(const rf_sim* s, uint32_t out[4]) {
+int rf_sim_splat_tile(rf_sim* s, uint32_t out[4]) {
     if (!s || !out) return -1;
+    if (s->auto_tile_state == 4) {  // the timed tile launch: settle the decision
+        if (set_device(s) != RF_OK || cudaStreamSynchronize(s->stream) != cudaSuccess) return -1;
+        decide_auto_tile(s);
+    }
     const uint32_t* t = s->splat == RF_SPLAT_TILE ? s->tile
                         : (s->splat == RF_SPLAT_AUTO && s->auto_tile_state == 1) ? s->auto_tile : nullptr;
     if (!t) return 0;

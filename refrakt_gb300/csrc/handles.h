@@ -42,11 +42,16 @@ struct rf_sim {
     int spec_splat = -1;              // the splat strategy compiled into it (ChaosArgs.splat code)
     int reset = 0;                    // walker reset of flame.glsl:68 (rf_set_bad_value_reset)
     uint32_t tile[4] = {0, 0, 0, 0};  // the tile splat's bins: x0, y0, w, h (rf_set_splat_tile)
-    // RF_SPLAT_AUTO on a compact attractor: 0 undecided, 1 the tile splat over auto_tile, -1 not;
-    // decided on the bin grid auto_tile_wh from the hits after the first full drawing launch
+    // RF_SPLAT_AUTO on a compact attractor, per bin grid auto_tile_wh: 0 undecided (the next
+    // drawing launch of >= 32 passes warms the grid up); 2 the next one is timed untiled, then a
+    // tile is fitted to the hits; 3 a tile fitted (the next launch of that length is timed with
+    // it); 4 both timed, deciding when the second has finished; 1 the tile splat over auto_tile;
+    // -1 no tile
     int auto_tile_state = 0;
     uint32_t auto_tile[4] = {0, 0, 0, 0};
     uint32_t auto_tile_wh[2] = {0, 0};
+    uint32_t auto_tile_passes = 0;
+    cudaEvent_t tile_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     int spec_reset = -1;              // the reset setting compiled into the specialised kernel
     int spec_pipe = 0;                // 1: the specialised kernel has the pipelined walker exchange
     uint32_t table_phases = 0;        // phases per pass the shuffle table is pipelined for (0: uniform)

@@ -193,28 +193,32 @@ def test_tile_splat_bit_exact(rk, orc, compiler, specialize, slots, tile, exchan
 
 
 @pytest.mark.parametrize("genome,W,H,want_tile", [("contract", 480, 270, True), ("frame1080", 1920, 1080, False)])
-def test_auto_splat_fits_a_tile_to_compact_attractors(rk, orc, compiler, genome, W, H, want_tile):
-    """RF_SPLAT_AUTO switches to a fitted shared-memory tile after the first drawing launch of >= 32 passes
-    when the attractor is compact (the contracting genome) and keeps warp aggregation when it is
-    spread (the 1080p genome).  Counts stay exact: on the affine contracting genome they equal the
-    FP32 oracle's on the kernel's schedule."""
+def test_auto_splat_fits_a_tile_to_compact_attractors(rk, compiler, genome, W, H, want_tile):
+    """RF_SPLAT_AUTO fits a shared-memory tile after its first drawing launch of >= 32 passes
+    when the hits concentrate (the contracting genome), times one launch through it against that
+    first one and keeps it when faster — on the full GPU, by a wide margin for this genome — and
+    fits none when the attractor is spread (the 1080p genome).  Counts never change: they equal
+    a warp-aggregated run's on the same seed."""
     import os
     xml = open(os.path.join(os.path.dirname(__file__), "golden", "genomes", genome + ".flam3")).read()
     f = rk.Flame.from_xml(xml, compiler)
-    N, F, D = 8192, 20, 96
-    sim = rk.Sim(N, seed=8, steps_per_launch=32)
-    sim.warmup(f, F - 1)
-    bins, hits = _bins(W, H)
-    sim.draw_to_bins(f, bins, hits, W, H, D)
-    tile = sim.splat_tile()
+    N, F, D = 622592, 20, 3 * 256  # one 4096-slot CTA per SM
+    out = {}
+    for splat in (rk.SPLAT_AUTO, rk.SPLAT_WARP):
+        sim = rk.Sim(N, seed=8)
+        sim.set_splat(splat)
+        sim.warmup(f, F - 1)
+        bins, hits = _bins(W, H)
+        sim.draw_to_bins(f, bins, hits, W, H, D)
+        out[splat] = (hits.cpu().numpy(), sim.splat_tile())
+        sim.close()
+    tile = out[rk.SPLAT_AUTO][1]
     print(genome, "tile", tile)
     assert (tile is not None) == want_tile
+    assert out[rk.SPLAT_WARP][1] is None
     if want_tile:
         assert tile[2] * tile[3] > 0 and tile[0] + tile[2] <= W and tile[1] + tile[3] <= H
-        r = orc.Genome(xml).chaos(N, W, H, fuse=F, draw=D, seed=8, fp64=False, shuffle_mode=1, cta_slots=4096,
-                                  steps_per_launch=32, table_size=1024, want_rgba=False)
-        assert np.array_equal(hits.cpu().numpy().astype(np.uint64), r["hits"])
-    sim.close()
+    assert np.array_equal(out[rk.SPLAT_AUTO][0], out[rk.SPLAT_WARP][0])
 
 
 def test_tile_splat_rejects_bad_tiles(rk, compiler):
