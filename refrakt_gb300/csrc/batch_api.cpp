@@ -97,6 +97,10 @@ struct rf_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // the persistent launches after the first run on their own streams, forked from and joined to
+    // `stream`: a launch's CTAs take the SMs the previous launch's finished CTAs leave
+    std::vector<cudaStream_t> aux;
+    std::vector<cudaEvent_t> fork_join;  // [0] fork, [1 + k] join of aux[k]
     uint64_t points = 0;
 };
 
@@ -112,6 +116,10 @@ void destroy_batch(rf_batch* b) {
     for (void* p : ptrs) if (p) cudaFree(p);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
+    for (auto ev : b->fork_join)
+        if (ev) cudaEventDestroy(ev);
+    for (auto s : b->aux)
+        if (s) cudaStreamDestroy(s);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
@@ -244,15 +252,40 @@ int enqueue(rf_batch* b) {
         if (e == cudaSuccess) e = cudaMemsetAsync(it.hits, 0, nb * sizeof(uint32_t), st);
     }
     if (e != cudaSuccess) return cuda_err(e, "batch clear");
-    for (size_t g = 0; g < b->groups.size() && e == cudaSuccess; g++) {
-        const SpecGroup& G = b->groups[g];
-        if (G.count)
-            e = launch_batch_spec(G.kernel, (int)b->threads, (int)b->slots, G.grid,
-                                  args_for(b, G.first, G.count, (uint32_t)g), st);
+    // the persistent launches: the first on `st`, each further one on an auxiliary stream forked
+    // after the clears, all joined before the image passes
+    std::vector<int> launches;  // group index, or groups.size() for the interpreted launch
+    for (size_t g = 0; g < b->groups.size(); g++)
+        if (b->groups[g].count) launches.push_back((int)g);
+    if (b->interp_count) launches.push_back((int)b->groups.size());
+    const size_t extra = launches.empty() ? 0 : launches.size() - 1;
+    while (e == cudaSuccess && b->aux.size() < extra) {
+        cudaStream_t s2 = nullptr;
+        e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
+        if (e == cudaSuccess) b->aux.push_back(s2);
     }
-    if (e == cudaSuccess && b->interp_count)
-        e = launch_batch((int)b->threads, (int)b->slots,
-                         args_for(b, b->interp_first, b->interp_count, (uint32_t)b->groups.size()), st, nullptr);
+    while (e == cudaSuccess && b->fork_join.size() < extra + 1) {
+        cudaEvent_t ev = nullptr;
+        e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) b->fork_join.push_back(ev);
+    }
+    if (e == cudaSuccess && extra) e = cudaEventRecord(b->fork_join[0], st);
+    for (size_t k = 0; k < launches.size() && e == cudaSuccess; k++) {
+        cudaStream_t ls = k ? b->aux[k - 1] : st;
+        if (k) e = cudaStreamWaitEvent(ls, b->fork_join[0], 0);
+        const int g = launches[k];
+        if (e != cudaSuccess) break;
+        if (g < (int)b->groups.size()) {
+            const SpecGroup& G = b->groups[g];
+            e = launch_batch_spec(G.kernel, (int)b->threads, (int)b->slots, G.grid,
+                                  args_for(b, G.first, G.count, (uint32_t)g), ls);
+        } else {
+            e = launch_batch((int)b->threads, (int)b->slots,
+                             args_for(b, b->interp_first, b->interp_count, (uint32_t)b->groups.size()), ls, nullptr);
+        }
+        if (e == cudaSuccess && k) e = cudaEventRecord(b->fork_join[k], ls);
+    }
+    for (size_t k = 1; k < launches.size() && e == cudaSuccess; k++) e = cudaStreamWaitEvent(st, b->fork_join[k], 0);
     if (e != cudaSuccess) return cuda_err(e, "batch kernel");
     for (size_t i = 0; i < b->items.size(); i++) {
         Item& it = b->items[i];
