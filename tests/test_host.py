@@ -411,3 +411,15 @@ def test_gemm_and_conv_validate_arguments_before_device_work(rk):
     assert conv(B=Q + 4) == INVALID                     # weights not 16-byte aligned
     assert conv(mode=9) == INVALID
     assert b"rf_conv3x3_bf16" in L.rf_last_error()
+
+
+def test_sim_setters_and_queries_reject_null_handles(rk):
+    """The Sim's tuning switches and queries check their arguments before touching a device."""
+    import ctypes
+    lib = rk.library()
+    out = (ctypes.c_uint32 * 4)()
+    assert lib.rf_set_exchange(None, rk.EXCHANGE_AUTO) == 1
+    assert lib.rf_sim_exchange(None) == -1
+    assert lib.rf_sim_splat_tile(None, out) == -1
+    assert lib.rf_set_splat(None, rk.SPLAT_AUTO) == 1
+    assert lib.rf_set_bad_value_reset(None, 1) == 1
