@@ -127,8 +127,8 @@ double fit_splat_tile(const std::vector<uint32_t>& h, uint32_t W, uint32_t H, ui
 // RF_SPLAT_AUTO for compact attractors.  After the second drawing launch of >= 32 passes on a grid
 // (timed; the first warms the grid up), the counts are read back once and a tile fitted; if it
 // holds >= 25 % of the hits, the next launch of the same length runs with it (timed) and the
-// faster form is kept.  Grids above
-// kAutoTileMaxBins are not read back (their planes go through interleaved records by default).
+// faster splat is kept.  Grids above kAutoTileMaxBins are not read back (their planes go through
+// interleaved records by default).
 constexpr uint64_t kAutoTileMaxBins = 1ull << 24;
 int fit_auto_tile(rf_sim* s, const uint32_t* hits, uint32_t W, uint32_t H) {
     s->auto_tile_state = -1;
@@ -145,7 +145,7 @@ int fit_auto_tile(rf_sim* s, const uint32_t* hits, uint32_t W, uint32_t H) {
     return RF_OK;
 }
 
-// state 4: keep the tile if its timed launch was faster, once that launch has finished
+// RF_SPLAT_AUTO, both launches timed: keep the tile if its launch was faster, once it has finished
 void decide_auto_tile(rf_sim* s) {
     const cudaError_t q = cudaEventQuery(s->tile_ev[3]);
     if (q == cudaErrorNotReady) {
