@@ -400,7 +400,7 @@ def run_native(args):
     cta = args.cta_slots or WL.get("cta_slots", 4096)
     walkers = WL.get("walkers") or sms * args.ctas_per_sm * cta
     sim = R.Sim(walkers, cta_slots=cta, cta_threads=args.cta_threads, steps_per_launch=args.steps_per_launch,
-                seed=1000 + rank, device=local, specialize={"auto": 0, "on": 1, "off": -1}[args.specialize])
+                seed=1000 + rank, device=local, specialize={"auto": 0, "on": 1, "off": -1, "all": 0}[args.specialize])
     passes = (POINTS + walkers - 1) // walkers
     launches = (passes + args.steps_per_launch - 1) // args.steps_per_launch
     bins = torch.zeros(H, W, 4, device="cuda")
@@ -617,7 +617,11 @@ def run_batch(args):
     points = sum(it[3] for it in items)
     n_img = len(items)
     reset = not args.no_badval_reset
-    b = R.Batch(items, fuse_passes=FUSE, density_estimation=True, device=local, bad_value_reset=reset)
+    # the bench renders this batch again and again: every structure gets a specialised kernel
+    # (compiled once, in the first warm-up step; the cache keeps them)
+    bspec = {"auto": 2, "on": 1, "off": -1, "all": 2}[args.specialize]
+    b = R.Batch(items, fuse_passes=FUSE, density_estimation=True, device=local, bad_value_reset=reset,
+                specialize=bspec)
     info = b.info()
     spec_groups = len({items[i][0].kernel_source() for i, sp in enumerate(info["specialized"]) if sp})
 
@@ -653,7 +657,8 @@ def run_batch(args):
         barrier()
         t_a = time.perf_counter()
         fl = [(R.Flame.from_xml(x, comp), w, h, p, s) for x, w, h, p, s in xmls]
-        bb = R.Batch(fl, fuse_passes=FUSE, density_estimation=True, device=local, bad_value_reset=reset)
+        bb = R.Batch(fl, fuse_passes=FUSE, density_estimation=True, device=local, bad_value_reset=reset,
+                     specialize=bspec)
         bb.run()
         for k in range(n_img):
             bb.image(k, outs[k])
@@ -949,7 +954,7 @@ def main():
     ap.add_argument("--exchange", default="auto", choices=["auto", "pipelined", "barrier"],
                     help="walker exchange of the specialised chaos kernel: the faster of the two timed on the first "
                          "drawing launches (default), mbarrier-pipelined, or one CTA barrier per pass")
-    ap.add_argument("--specialize", default="auto", choices=["auto", "on", "off"],
+    ap.add_argument("--specialize", default="auto", choices=["auto", "on", "off", "all"],
                     help="genome-specialised chaos kernel compiled at run time")
     ap.add_argument("--learned-train", type=int, default=2000)
     ap.add_argument("--learned-test", type=int, default=200)

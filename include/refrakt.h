@@ -410,7 +410,10 @@ typedef struct {
     int32_t  specialize;        /* genome structures with >= 2 units per SM (or the only
                                    structure of the batch) get their own launch of a specialised
                                    kernel compiled at run time: 0 = when the run-time compiler
-                                   loads, 1 = required, -1 = never */
+                                   loads, 1 = required, -1 = never; 2 = every structure (a one-time
+                                   compilation of about a second per structure, in parallel, for
+                                   batches rendered repeatedly; the launches overlap on forked
+                                   streams) */
     int32_t  bad_value_reset;   /* 1: walkers that leave the plane restart, as rf_set_bad_value_reset */
 } rf_batch_desc;
 RF_API int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc* d, rf_batch** out);

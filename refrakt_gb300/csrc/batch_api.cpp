@@ -515,7 +515,9 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
     b->unit_passes = (uint32_t)per;
     // --- genome-specialised kernels for the structures with >= 2 units per SM (animation frames
     // share one), compiled in parallel and cached across batches, each a persistent launch of its
-    // own; the other structures share the interpreted persistent launch.  (Giving every structure
+    // own; the other structures share the interpreted persistent launch, or with specialize = 2 get
+    // their own kernels too (the launches overlap on forked streams; their compilation costs about
+    // a second per structure once, and the cache keeps them).  (Giving every structure
     // its own kernel, the small ones launched concurrently on auxiliary streams, measured slower:
     // 24.9 against 26.9 Gpoints/s on the 184-image batch — a CTA per unit balances worse than one
     // persistent queue.)  Structures whose kernel does not compile stay interpreted.
@@ -528,7 +530,7 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
         }
         std::vector<std::pair<uint64_t, std::string>> order;
         for (auto& kv : units_of)  // (a batch of one structure always: no other launch to balance against)
-            if (kv.second >= (uint64_t)kSpecMinUnitsPerSM * sms || units_of.size() == 1)
+            if (kv.second >= (uint64_t)kSpecMinUnitsPerSM * sms || units_of.size() == 1 || d->specialize == 2)
                 order.push_back({kv.second, kv.first});
         std::sort(order.rbegin(), order.rend());
         std::vector<const void*> kern(order.size(), nullptr);
@@ -548,7 +550,7 @@ int rf_batch_create(const rf_batch_item* items, uint32_t n, const rf_batch_desc*
         for (size_t j = 0; j < order.size(); j++) {
             int grid = rcs[j] == RF_OK ? batch_spec_grid(kern[j], (int)b->threads, (int)b->slots, b->max_prog_words) : 0;
             if (rcs[j] != RF_OK || grid == 0) {
-                if (d->specialize > 0)
+                if (d->specialize == 1)
                     return bail(rcs[j] != RF_OK ? rcs[j] : fail(RF_ERR_CUDA, "specialised batch kernel: no resident CTA"));
                 continue;
             }

@@ -197,3 +197,25 @@ def test_specialised_group_equals_interpreted(rk, compiler, kind):
     for i in range(3):
         assert np.array_equal(a[i][1], c[i][1]), i
         assert np.allclose(a[i][0], c[i][0], rtol=1e-4, atol=1e-3)
+
+
+def test_every_structure_specialised_equals_interpreted(rk, compiler):
+    """specialize = 2: every genome structure gets its own specialised persistent launch (the
+    launches overlap on forked streams); every item's counts equal the interpreted kernel's."""
+    fl = [rk.Flame.synthesize(compiler, rk.SYNTH_RANDOM, 40 + k, 96, 96, n_xforms=2 + k % 6, final_xform=k % 2 == 1)
+          for k in range(6)]
+    items = [(f, 96, 96, 3 * 1024 * 16, 60 + k) for k, f in enumerate(fl)]
+    res = []
+    for spec in (2, -1):
+        b = rk.Batch(items, cta_slots=1024, unit_passes=16, density_estimation=False, specialize=spec)
+        info = b.info()
+        assert info["specialized"] == ([1] * 6 if spec == 2 else [0] * 6)
+        b.run()
+        st = b.sync()
+        res.append(([b.bins(i) for i in range(6)], st))
+        b.close()
+    (a, sa), (c, sc) = res
+    assert sa["points"] == sc["points"] and sa["binned"] == sc["binned"]
+    for i in range(6):
+        assert np.array_equal(a[i][1], c[i][1]), i
+        assert np.allclose(a[i][0], c[i][0], rtol=1e-4, atol=1e-3)
