@@ -619,7 +619,7 @@ def run_batch(args):
     reset = not args.no_badval_reset
     # the bench renders this batch again and again: every structure gets a specialised kernel
     # (compiled once, in the first warm-up step; the cache keeps them)
-    bspec = {"auto": 2, "on": 1, "off": -1, "all": 2}[args.specialize]
+    bspec = {"auto": 2, "on": 0, "off": -1, "all": 2}[args.specialize]
     b = R.Batch(items, fuse_passes=FUSE, density_estimation=True, device=local, bad_value_reset=reset,
                 specialize=bspec)
     info = b.info()
@@ -955,7 +955,8 @@ def main():
                     help="walker exchange of the specialised chaos kernel: the faster of the two timed on the first "
                          "drawing launches (default), mbarrier-pipelined, or one CTA barrier per pass")
     ap.add_argument("--specialize", default="auto", choices=["auto", "on", "off", "all"],
-                    help="genome-specialised chaos kernel compiled at run time")
+                    help="genome-specialised chaos kernels compiled at run time (the batch workload: auto and all = "
+                         "every structure its own kernel, on = the large structures only, off = interpreted)")
     ap.add_argument("--learned-train", type=int, default=2000)
     ap.add_argument("--learned-test", type=int, default=200)
     ap.add_argument("--learned-steps", type=int, default=2000)
